@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Benchmark: atom-steps/s of the LJ particle path on one GB300.
+
+Workload (default): fcc 64x64x64 unit cells = 1,048,576 atoms, rho 0.8442, T 1.44,
+rc 2.5, skin 0.3, dt 0.005, one type, periodic cube.  A "step" is one MD time step of
+the reference's loop (integrate, rebuild when due, LJ force, integrate, thermo at
+its cadence) over all atoms.  The headline arm is the mixed-precision path (FP32
+force on compensated FP32 positions, FP64 integration/guard/reductions); the plain
+FP64 path is timed on the same workload and reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU restatement of the reference's algorithm
+(oracle/lj_oracle.c, every host thread) on the same workload.  With N > 1 (torchrun)
+each rank runs an independent replica (replicas only: the path does not shard);
+value = atoms * steps summed over ranks / max rank time.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s on 1 GB300: mixed+learned vs plain FP64 at equal energy drift"
+UNIT = "atom-steps/s"
+
+WORKLOADS = {
+    "lj64": dict(n=(64, 64, 64)),
+    "lj32": dict(n=(32, 32, 32)),
+    "lj128": dict(n=(128, 128, 128)),
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows, self.proc = [], None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        return dist, int(os.environ["RANK"]), ws, int(os.environ.get("LOCAL_RANK", "0"))
+    return None, 0, 1, 0
+
+
+def traffic_from_profiles(kernel):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 2 and parts[0] == kernel:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+# ------------------------------------------------------------------------------ our arm
+
+def run_ours(args, rank, world, dist):
+    import torch
+    from pairs_gb300 import _capi as A
+    from pairs_gb300 import lattice
+    from pairs_gb300.engine import LJEngine
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    wl = WORKLOADS[args.workload]
+    st = lattice.copper_fcc_lattice(*wl["n"])
+    n = len(st["mass"])
+    lib = A.load()
+
+    def make(precision, half):
+        return LJEngine(st, precision=precision, half=half, sync="exact", every=20, policy="fixed",
+                        device=str(dev))
+
+    def timed(eng, steps, warmup, force_events=True):
+        for _ in range(warmup):
+            eng.step()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        stream = eng.stream
+        ev = []
+        orig_force = eng.force
+
+        def force_timed(energy=False):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            orig_force(energy)
+            b.record(stream)
+            ev.append((a, b))
+
+        if force_events:
+            eng.force = force_timed
+        l0 = lib.pg_kernel_launches()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(steps):
+            eng.step()
+        s1.record(stream)
+        torch.cuda.synchronize()
+        launches = lib.pg_kernel_launches() - l0
+        eng.force = orig_force
+        ms = s0.elapsed_time(s1)
+        fms = [a.elapsed_time(b) for a, b in ev]
+        return ms, fms, launches
+
+    # headline: mixed precision, half list (Newton's third law), fixed reference schedule
+    eng = make("mixed", True)
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    ms, fms, launches = timed(eng, args.steps, args.warmup)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * args.steps * world / (ms / 1e3)
+    pairs_total = int(eng.t["count"][:n].sum().item())
+    # algorithmic bytes of one force launch: own hi+lo position (32), count (4),
+    # force (16), 4 bytes per list entry, half list: reaction add per particle (16)
+    b_force = n * (32 + 4 + 16) + 4 * pairs_total + (n * 16 if eng.list.half else 0)
+    f_avg = statistics.mean(fms) if fms else float("nan")
+    pk, pk_kind = peaks()
+    achieved = b_force / (f_avg / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / pk["hbm_gbs"], 4), "peak_kind": pk_kind,
+                "traffic": traffic_from_profiles("k_lj_mixed"), "kernel": "k_lj_mixed<half>",
+                "kernel_ms": round(f_avg, 4), "algorithmic_bytes": b_force, "list_entries": pairs_total}
+    nbuilds = eng.nbuilds
+
+    # plain FP64 path on the same workload (full list and half list; best reported)
+    fp64 = {}
+    for half in (False, True):
+        e64 = make("fp64", half)
+        k64 = max(10, args.steps // 10)
+        ms64, f64ms, _ = timed(e64, k64, min(args.warmup, 5))
+        fp64["half" if half else "full"] = {"value": n * k64 / (ms64 / 1e3), "steps": k64,
+                                            "force_ms": round(statistics.mean(f64ms), 4)}
+        del e64
+    best64 = max(v["value"] for v in fp64.values())
+
+    # end to end through the public engine API from pinned host state
+    e2e = None
+    if True:
+        chunk = min(100, args.steps)
+        nchunks = max(1, args.steps // chunk)
+        pad4 = lambda a: np.concatenate([a, np.zeros((len(a), 1))], axis=1)
+        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
+                (("pos", pad4(st["pos"])), ("vel", pad4(st["vel"])), ("mass", st["mass"]),
+                 ("type", st["type"]), ("uid", st["uid"]))}
+        out_pos = torch.empty((n, 4), dtype=torch.float64).pin_memory()
+        out_vel = torch.empty((n, 4), dtype=torch.float64).pin_memory()
+        ee = make("mixed", True)
+        ee.run(args.warmup)
+        torch.cuda.synchronize()
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for _ in range(nchunks):
+            ee.upload(host["pos"], host["vel"], host["mass"], host["type"], host["uid"])
+            h2d += sum(v.numel() * v.element_size() for v in host.values())
+            ee.run(chunk)
+            out_pos.copy_(ee.t["pos"][:n], non_blocking=True)
+            out_vel.copy_(ee.t["vel"][:n], non_blocking=True)
+            thermo = ee.compute_thermo()
+            d2h += 2 * n * 32 + 24
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        e2e = {"value": n * chunk * nchunks / el, "unit": UNIT, "h2d_bytes_per_step": h2d // (chunk * nchunks),
+               "d2h_bytes_per_step": d2h // (chunk * nchunks),
+               "definition": f"public engine API: per call upload full particle state from pinned host, "
+                             f"advance {chunk} MD steps, download positions+velocities and thermo"}
+        del ee
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(st, args.cpu_steps)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 force / f64 integrate",
+        "data": "synthetic (fcc lattice, Park-Miller velocities as the reference)",
+        "config": {"workload": f"LJ fcc {wl['n'][0]}x{wl['n'][1]}x{wl['n'][2]} = {n} atoms, rho 0.8442, T 1.44, "
+                               "rc 2.5, skin 0.3, dt 0.005, mixed precision, half list, rebuild every 20",
+                   "atoms": n, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (Verlet list %.0f MB)" % (pairs_total * 4 / 1e6),
+                   "rebuilds_in_timed_region": nbuilds},
+        "roofline": roofline,
+        "fp64": {"best_value": best64, **fp64, "speedup_mixed_vs_fp64": value / world / best64},
+        "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def cpu_baseline(st, steps):
+    """The oracle port (C restatement of the reference's loop) on every host thread."""
+    from oracle import lj as olj
+    nth = os.cpu_count() or 1
+    sim = olj.Sim(st, every=20, exact_sync=True, nthreads=nth)
+    t0 = time.perf_counter()
+    sim.run(steps)
+    el = time.perf_counter() - t0
+    n = len(st["mass"])
+    return {"value": n * steps / el, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"{steps} MD steps of the full {n}-atom system (incl. rebuilds every 20) "
+                      f"with oracle/lj_oracle.c, OpenMP {nth} threads"}
+
+
+# ------------------------------------------------------------------------------ reference arm
+
+def run_reference(args, rank, world, dist):
+    if rank != 0:
+        return
+    from pairs_gb300 import lattice
+    wl = WORKLOADS[args.workload]
+    st = lattice.copper_fcc_lattice(*wl["n"])
+    n = len(st["mass"])
+    from oracle import lj as olj
+    nth = os.cpu_count() or 1
+    sim = olj.Sim(st, every=20, exact_sync=True, nthreads=nth)
+    sim.run(args.warmup)
+    budget = args.reference_budget_s
+    t0 = time.perf_counter()
+    done = 0
+    while done < args.steps:
+        sim.step()
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    v = n * done / el
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": args.warmup,
+        "ms_per_step": el * 1e3 / done, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (fcc lattice, Park-Miller velocities as the reference)",
+        "config": {"workload": f"LJ fcc {wl['n'][0]}x{wl['n'][1]}x{wl['n'][2]} = {n} atoms, rho 0.8442, T 1.44, "
+                               "rc 2.5, skin 0.3, dt 0.005, reference CPU algorithm (FP64, ghosts), "
+                               "rebuild every 20", "atoms": n},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
+                         "sample": f"{done} MD steps of the full system, oracle/lj_oracle.c, OpenMP {nth} threads"
+                                   + (f", stopped at the {budget:.0f} s budget" if done < args.steps else "")},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="lj64")
+    ap.add_argument("--cpu-steps", type=int, default=40)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist, rank, world, _ = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world, dist)
+    else:
+        run_ours(args, rank, world, dist)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

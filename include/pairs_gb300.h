@@ -1,0 +1,218 @@
+/*
+ * pairs_gb300.h -- C ABI of the GB300 particle hot path (libpairs_gb300.so).
+ *
+ * One entry point per module of the reference's generated time step that it
+ * replaces.  The reference prints each module as a C/CUDA function taking raw
+ * pointers and sizes (src/pairs/code_gen/cgen.py:119-251) and calls it from the
+ * generated main(); these entry points take the same kind of arguments: plain
+ * structs of device pointers, sizes and capacities, plus a cudaStream_t passed as
+ * void*.  No C++ or torch type crosses the boundary.
+ *
+ * Memory: the caller owns every buffer (the Python front end allocates them as
+ * torch tensors).  The library allocates nothing; kernels that need scratch take it
+ * from pg_workspace.
+ *
+ * Errors: every entry point returns an int status (PG_OK, or a PG_ERR_* code, or
+ * PG_OVERFLOW when a capacity was too small).  On PG_OVERFLOW the needed size is in
+ * pg_status (device memory written by the kernel, read by the host after the
+ * stream is synchronised) -- the reference's resizes[] protocol
+ * (src/pairs/transformations/modules.py:37-205, runtime/devices/device.hpp:63-71).
+ * Kernels never trap or assert.
+ *
+ * Layouts (all device memory, "sorted order" = cell order of the last rebuild):
+ *   double4 pos[n]      x, y, z, (unused)          FP64 master positions
+ *   double4 vel[n]      vx, vy, vz, (unused)
+ *   double4 force[n]    FP64 force (precision PG_FP64)
+ *   float4  force32[n]  FP32 force (precision PG_MIXED)
+ *   float4  pos_hi[n], pos_lo[n]   compensated FP32 positions: hi on a 2^-k grid so
+ *                      hi differences and periodic shifts are exact in FP32, lo the
+ *                      FP32 residual x - hi
+ *   int     nbr[k * stride + i]    Verlet entry k of particle i (column-major, as
+ *                      the reference's GPU layout, sim/neighbor_lists.py:14); bits
+ *                      0-25 the partner index, bits 26-31 the periodic image code
+ *                      (2 bits per dimension: 0 none, 1 plus one box, 2 minus one)
+ */
+#ifndef PAIRS_GB300_H
+#define PAIRS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_OK              0
+#define PG_OVERFLOW        1     /* a capacity was exceeded; see pg_status */
+#define PG_ERR_ARGUMENT   -1     /* invalid argument (sizes, null pointers, alignment) */
+#define PG_ERR_CUDA       -2     /* a CUDA call failed (launch or runtime error) */
+#define PG_ERR_NONFINITE  -3     /* a non-finite position/velocity/force was found */
+
+#define PG_FP64   0              /* FP64 force, FP64 everything */
+#define PG_MIXED  1              /* FP32 force on compensated FP32 positions, FP64 integration */
+
+#define PG_SYNC_EXACT      0     /* periodic images always at the partner's current position */
+#define PG_SYNC_REFERENCE  1     /* images refreshed like the reference's halo sync:
+                                    an image shifted in k>1 dimensions uses the partner's
+                                    position from min(k-1, steps since rebuild) steps ago
+                                    (src/pairs/sim/comm.py:46-54, 369-442) */
+
+#define PG_NBR_INDEX_BITS 26
+#define PG_NBR_INDEX_MASK ((1u << PG_NBR_INDEX_BITS) - 1u)
+
+/* Device-side status, written by kernels (mirrors the reference's resizes[]). */
+typedef struct {
+    int32_t overflow;            /* bit 0 cells, bit 1 neighbours, bit 2 contacts */
+    int32_t max_cell_count;      /* largest cell occupancy seen */
+    int32_t max_neighbors;       /* largest per-particle Verlet count seen */
+    int32_t nonfinite;           /* set when a non-finite value was met */
+    int32_t guard_tripped;       /* first step at which a displacement > skin/2 was seen;
+                                    INT32_MAX while none was */
+    int32_t max_contacts;        /* DEM contact-history slots needed */
+    int32_t pad[2];
+} pg_status;
+
+/* Periodic (or walled) orthorhombic box, sim/domain_partitioning.py:46-57. */
+typedef struct {
+    double lo[3];
+    double hi[3];
+    double len[3];               /* hi - lo, as the reference's grid.length() */
+    int    periodic[3];
+    float  len_hi[3];            /* len split on the compensated FP32 grid */
+    float  len_lo[3];
+    double quantum;              /* grid step of pos_hi (a power of two) */
+} pg_box;
+
+/* Per-particle state, sorted order.  Optional arrays may be NULL. */
+typedef struct {
+    int32_t n;                   /* particles in use */
+    int32_t capacity;
+    double *pos;                 /* double4[capacity] */
+    double *pos_prev1;           /* double4[capacity], PG_SYNC_REFERENCE only */
+    double *pos_prev2;           /* double4[capacity], PG_SYNC_REFERENCE only */
+    double *vel;                 /* double4[capacity] */
+    double *force;               /* double4[capacity] (PG_FP64) */
+    float  *force32;             /* float4[capacity]  (PG_MIXED) */
+    float  *pos_hi;              /* float4[capacity]  (PG_MIXED); w = type as float bits */
+    float  *pos_lo;              /* float4[capacity]  (PG_MIXED) */
+    double *pos_ref;             /* double4[capacity] positions at last rebuild (guard) */
+    double *mass;                /* [capacity] */
+    int32_t *type;               /* [capacity] */
+    int32_t *uid;                /* [capacity] user id (the reference's uid property) */
+    int32_t *flags;              /* [capacity] reference flag bits: 1 infinite, 4 fixed */
+} pg_particles;
+
+/* Cell grid over the box, counting-sort layout (cell_start/cell_count). */
+typedef struct {
+    int32_t dims[3];
+    int32_t ncells;
+    double  cell_len[3];         /* len[d] / dims[d] >= list radius */
+    int32_t *cell_start;         /* [ncells + 2]: cells, then the bucket of infinite shapes */
+    int32_t *cell_count;         /* [ncells + 1] */
+    int32_t *particle_cell;      /* [capacity] */
+} pg_cells;
+
+/* Verlet list, column-major ELL. */
+typedef struct {
+    int32_t stride;              /* >= capacity of particles */
+    int32_t max_neighbors;       /* entries per particle */
+    int32_t half;                /* 1: each unordered pair once (Newton's third law) */
+    int32_t *nbr;                /* [max_neighbors * stride] */
+    int32_t *count;              /* [stride] */
+    int32_t steps_since_build;   /* host-maintained, for PG_SYNC_REFERENCE */
+} pg_neighbor_list;
+
+/* Lennard-Jones parameters per type pair (examples/md.py:5-8, feature tables). */
+typedef struct {
+    int32_t ntypes;              /* <= 16 */
+    double  cutoff2;             /* rc^2 (6.25 for rc = 2.5) */
+    double  epsilon[256];        /* [ti * ntypes + tj] */
+    double  sigma6[256];
+} pg_lj_params;
+
+/* Scratch memory provided by the caller (bytes). */
+typedef struct {
+    void   *ptr;
+    int64_t bytes;
+} pg_workspace;
+
+/* ---------------------------------------------------------------------------- */
+
+/* Library version and the size of each struct, so a binding can check layouts. */
+int pg_version(void);
+
+/* Number of CUDA kernels this library has launched since it was loaded. */
+int64_t pg_kernel_launches(void);
+int pg_struct_sizes(int64_t *out, int n);
+
+/* Scratch bytes pg_bin_particles / pg_compute_thermo need for n particles. */
+int64_t pg_workspace_bytes(int32_t n, int32_t ncells);
+
+/* Wrap particles that left a periodic box back in (x < lo -> x + len, x > hi ->
+ * x - len, as the reference's exchange, sim/comm.py:101-151), bin them into the
+ * cell grid, and permute every per-particle array into cell order (stable within a
+ * cell by uid).  Replaces build_cell_lists + partition_cell_lists
+ * (sim/cell_lists.py:90-171) and the exchange half of the halo code. */
+int pg_bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells,
+                     pg_workspace ws, pg_status *status, void *stream);
+
+/* Build the Verlet list within r_list (the reference's build_neighbor_lists,
+ * sim/neighbor_lists.py:21-48 with interaction.py:90-120).  The acceptance test
+ * rsq < r_list2 is evaluated exactly as the reference: FP64, image position
+ * fl(x_j + s*len), delta, (dx*dx + dy*dy) + dz*dz, no fused multiply-add.  Also
+ * records pos_ref for the displacement guard. */
+int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
+                            pg_neighbor_list *list, double r_list2, pg_status *status,
+                            void *stream);
+
+/* Lennard-Jones forces over the Verlet list (the reference's lennard_jones module:
+ * examples/md.py:5-8, sim/interaction.py:222-232, ir/apply.py:112-125).
+ * precision PG_FP64 writes p->force, PG_MIXED writes p->force32.  sync_mode selects
+ * PG_SYNC_EXACT or PG_SYNC_REFERENCE (FP64 only).  energy, if not NULL, is a device
+ * double[2] that receives potential energy and virial sum r.F (FP64 sums). */
+int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list,
+                const pg_lj_params *lj, int precision, int sync_mode, double *energy,
+                pg_workspace ws, void *stream);
+
+/* Velocity-Verlet half steps of examples/md.py:11-17 (the reference's
+ * initial_integrate / final_integrate modules), same operation order:
+ *   initial: v = v + ((dt*0.5)*F)/m;  x = x + dt*v      (pre_step, skip_first)
+ *   final:   v = v + ((dt*0.5)*F)/m                     (skip_first)
+ * precision selects which force array is read.  The initial step also tests every
+ * particle's displacement since the last list build against half_skin2 in FP64
+ * (the guard; the first offending step is kept in status->guard_tripped) and
+ * refreshes pos_hi/pos_lo when present.  With sync_mode PG_SYNC_REFERENCE the caller
+ * rotates the position ring first (prev2 <- prev1 <- pos <- old prev2); the kernel
+ * then reads pos_prev1 and writes pos. */
+int pg_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,
+                         double half_skin2, int32_t step, int sync_mode, pg_status *status,
+                         void *stream);
+int pg_final_integrate(const pg_box *box, pg_particles *p, double dt, int precision, void *stream);
+
+/* Final half kick of step k fused with the initial kick + drift of step k+1: one
+ * pass instead of two, identical arithmetic to calling both in order. */
+int pg_final_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,
+                               double half_skin2, int32_t step, int sync_mode, pg_status *status,
+                               void *stream);
+
+/* Sum m v^2 over particles (FP64, fixed reduction tree, deterministic) and
+ * write out[0] = T = sum/(3N-3), out[1] = kinetic pressure T(3N-3)/(3V), out[2] = sum
+ * (runtime/thermo.hpp:11-51).  out is device memory (double[3]). */
+int pg_compute_thermo(const pg_box *box, const pg_particles *p, double *out,
+                      pg_workspace ws, void *stream);
+
+/* Refresh pos_hi / pos_lo from pos (after a host upload or a permutation). */
+int pg_split_positions(const pg_box *box, pg_particles *p, void *stream);
+
+/* dst[k] = src[perm[k]] for k < n, elements of elem_bytes (4, 8, 16 or 32): applies
+ * the last binning permutation to caller-held per-particle arrays. */
+int pg_permute(int32_t n, const int32_t *perm, const void *src, void *dst, int elem_bytes,
+               void *stream);
+
+/* cudaStreamSynchronize, returning PG_OK or PG_ERR_CUDA. */
+int pg_stream_sync(void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

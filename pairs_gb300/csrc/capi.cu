@@ -1,0 +1,107 @@
+// extern "C" entry points of libpairs_gb300.so (declared in include/pairs_gb300.h).
+#include "common.cuh"
+
+namespace pg {
+int64_t bin_workspace_bytes(int32_t n, int32_t ncells);
+int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_workspace ws,
+                  pg_status *status, cudaStream_t st, int32_t **perm_out);
+int gather_array(int n, const int32_t *perm, const void *src, void *dst, int elem_bytes, cudaStream_t st);
+int split_positions(const pg_box *box, pg_particles *p, cudaStream_t st);
+int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
+                         pg_neighbor_list *list, double r_list2, pg_status *status, cudaStream_t st);
+int lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list,
+             const pg_lj_params *lj, int precision, int sync_mode, double *energy, cudaStream_t st);
+int initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision, double half_skin2,
+                      int32_t step, pg_status *status, int sync_mode, cudaStream_t st);
+int final_integrate(const pg_box *box, pg_particles *p, double dt, int precision, cudaStream_t st);
+int final_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,
+                            double half_skin2, int32_t step, pg_status *status, int sync_mode,
+                            cudaStream_t st);
+int64_t thermo_workspace_bytes();
+int compute_thermo(const pg_box *box, const pg_particles *p, double *out, double *partials,
+                   cudaStream_t st);
+}  // namespace pg
+
+unsigned long long pg::g_kernel_launches = 0;
+
+static inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+extern "C" {
+
+int pg_version(void) { return 1; }
+
+int64_t pg_kernel_launches(void) { return (int64_t) __atomic_load_n(&pg::g_kernel_launches, __ATOMIC_RELAXED); }
+
+int pg_struct_sizes(int64_t *out, int n) {
+    const int64_t sizes[] = {
+        (int64_t) sizeof(pg_status), (int64_t) sizeof(pg_box), (int64_t) sizeof(pg_particles),
+        (int64_t) sizeof(pg_cells), (int64_t) sizeof(pg_neighbor_list), (int64_t) sizeof(pg_lj_params),
+        (int64_t) sizeof(pg_workspace),
+    };
+    const int m = (int) (sizeof(sizes) / sizeof(sizes[0]));
+    if(out == nullptr) { return m; }
+    for(int k = 0; k < n && k < m; k++) { out[k] = sizes[k]; }
+    return m;
+}
+
+int64_t pg_workspace_bytes(int32_t n, int32_t ncells) {
+    const int64_t a = pg::bin_workspace_bytes(n, ncells);
+    const int64_t b = pg::thermo_workspace_bytes();
+    return a > b ? a : b;
+}
+
+int pg_bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_workspace ws,
+                     pg_status *status, void *stream) {
+    return pg::bin_particles(box, p, cells, ws, status, S(stream), nullptr);
+}
+
+int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
+                            pg_neighbor_list *list, double r_list2, pg_status *status, void *stream) {
+    return pg::build_neighbor_lists(box, p, cells, list, r_list2, status, S(stream));
+}
+
+int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list,
+                const pg_lj_params *lj, int precision, int sync_mode, double *energy,
+                pg_workspace ws, void *stream) {
+    (void) ws;
+    return pg::lj_force(box, p, list, lj, precision, sync_mode, energy, S(stream));
+}
+
+int pg_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,
+                         double half_skin2, int32_t step, int sync_mode, pg_status *status,
+                         void *stream) {
+    return pg::initial_integrate(box, p, dt, precision, half_skin2, step, status, sync_mode, S(stream));
+}
+
+int pg_final_integrate(const pg_box *box, pg_particles *p, double dt, int precision, void *stream) {
+    return pg::final_integrate(box, p, dt, precision, S(stream));
+}
+
+int pg_final_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,
+                               double half_skin2, int32_t step, int sync_mode, pg_status *status,
+                               void *stream) {
+    return pg::final_initial_integrate(box, p, dt, precision, half_skin2, step, status, sync_mode,
+                                       S(stream));
+}
+
+int pg_compute_thermo(const pg_box *box, const pg_particles *p, double *out, pg_workspace ws,
+                      void *stream) {
+    if(ws.ptr == nullptr || ws.bytes < pg::thermo_workspace_bytes()) { return PG_ERR_ARGUMENT; }
+    return pg::compute_thermo(box, p, out, (double *) ws.ptr, S(stream));
+}
+
+int pg_split_positions(const pg_box *box, pg_particles *p, void *stream) {
+    return pg::split_positions(box, p, S(stream));
+}
+
+int pg_permute(int32_t n, const int32_t *perm, const void *src, void *dst, int elem_bytes, void *stream) {
+    if(n < 0 || (n > 0 && (!perm || !src || !dst)) || src == dst) { return PG_ERR_ARGUMENT; }
+    if(n == 0) { return PG_OK; }
+    return pg::gather_array(n, perm, src, dst, elem_bytes, S(stream));
+}
+
+int pg_stream_sync(void *stream) {
+    return cudaStreamSynchronize(S(stream)) == cudaSuccess ? PG_OK : PG_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,267 @@
+// Cell binning and counting sort of particles into cell order.
+//
+// Replaces the reference's build_cell_lists / partition_cell_lists modules
+// (sim/cell_lists.py:90-171) and the wrap half of its exchange step
+// (sim/comm.py:101-151).  The reference appends particle indices into fixed-size
+// per-cell slots (cell_particles[ncells][64]) with one atomic per particle; here the
+// particles themselves are permuted into cell order (counting sort: count, scan,
+// scatter, per-cell order by uid, gather), so every later kernel streams
+// contiguous, spatially sorted memory and the cell list is just (start, count).
+#include "common.cuh"
+
+namespace pg {
+
+// Wrap into the periodic box exactly as the reference's exchange pack does
+// (x + mult*len with mult = +1 below lo, -1 above hi), then compute the cell.
+__global__ void k_bin_count(pg_box box, pg_particles p, pg_cells cells, int32_t *count,
+                            pg_status *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= p.n) { return; }
+    D4 x = ld_d4_plain(p.pos, i);
+    double c3[3] = {x.x, x.y, x.z};
+    bool moved = false;
+    bool finite = true;
+    for(int d = 0; d < 3; d++) {
+        if(!isfinite(c3[d])) { finite = false; }
+        if(box.periodic[d]) {
+            if(c3[d] < box.lo[d]) { c3[d] = __dadd_rn(c3[d], box.len[d]); moved = true; }
+            else if(c3[d] > box.hi[d]) { c3[d] = __dadd_rn(c3[d], -box.len[d]); moved = true; }
+        }
+    }
+    if(moved) {
+        x.x = c3[0]; x.y = c3[1]; x.z = c3[2];
+        st_d4(p.pos, i, x);
+    }
+    int cell;
+    if(!finite) {
+        atomicExch(&status->nonfinite, 1);
+        cell = cells.ncells;                       // parked in the extra bucket
+    } else if(p.flags != nullptr && (p.flags[i] & kFlagInfinite)) {
+        cell = cells.ncells;                       // infinite shapes (half spaces) last
+    } else {
+        int idx = 0;
+        for(int d = 0; d < 3; d++) {
+            int c = (int) floor((c3[d] - box.lo[d]) / cells.cell_len[d]);
+            c = c < 0 ? 0 : (c >= cells.dims[d] ? cells.dims[d] - 1 : c);
+            idx = idx * cells.dims[d] + c;
+        }
+        cell = idx;
+    }
+    cells.particle_cell[i] = cell;
+    atomicAdd(&count[cell], 1);
+}
+
+// Exclusive scan, three passes over blocks of 1024 entries.
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *smem_warp, int &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+    for(int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if(lane >= o) { incl += t; }
+    }
+    if(lane == 31) { smem_warp[warp] = incl; }
+    __syncthreads();
+    if(warp == 0) {
+        const int nw = blockDim.x >> 5;
+        int w = lane < nw ? smem_warp[lane] : 0;
+        int wi = w;
+        for(int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, wi, o);
+            if(lane >= o) { wi += t; }
+        }
+        if(lane < nw) { smem_warp[lane] = wi - w; }
+        if(lane == nw - 1) { smem_warp[32] = wi; }
+    }
+    __syncthreads();
+    total = smem_warp[32];
+    const int res = incl - v + smem_warp[warp];
+    __syncthreads();
+    return res;
+}
+
+__global__ void k_scan_block_sums(const int32_t *in, int n, int32_t *block_sums) {
+    __shared__ int s[33];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const int v = i < n ? in[i] : 0;
+    int total;
+    block_exclusive_scan(v, s, total);
+    if(threadIdx.x == 0) { block_sums[blockIdx.x] = total; }
+}
+
+__global__ void k_scan_sums(int32_t *block_sums, int nb) {
+    __shared__ int s[33];
+    int carry = 0;
+    for(int base = 0; base < nb; base += kScanBlock) {
+        const int i = base + threadIdx.x;
+        const int v = i < nb ? block_sums[i] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, s, total);
+        if(i < nb) { block_sums[i] = ex + carry; }
+        carry += total;
+        __syncthreads();
+    }
+}
+
+// out[i] = exclusive prefix of in; out[n] = total.  also zeroes cursor[i].
+__global__ void k_scan_apply(const int32_t *in, int n, const int32_t *block_sums, int32_t *out,
+                             int32_t *cursor) {
+    __shared__ int s[33];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const int v = i < n ? in[i] : 0;
+    int total;
+    const int ex = block_exclusive_scan(v, s, total) + block_sums[blockIdx.x];
+    if(i < n) {
+        out[i] = ex;
+        cursor[i] = 0;
+        if(i == n - 1) { out[n] = ex + v; }
+    }
+}
+
+__global__ void k_scatter(int n, const int32_t *particle_cell, const int32_t *start,
+                          int32_t *cursor, int32_t *perm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) { return; }
+    const int c = particle_cell[i];
+    perm[start[c] + atomicAdd(&cursor[c], 1)] = i;
+}
+
+// Order each cell's particles by uid (insertion sort; cells hold ~20 particles),
+// so the result does not depend on the atomic order of the scatter.
+__global__ void k_sort_cells(int ncells_total, const int32_t *start, int32_t *perm,
+                             const int32_t *uid, pg_status *status) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int cnt = 0;
+    if(c < ncells_total) {
+        const int b = start[c], e = start[c + 1];
+        cnt = e - b;
+        for(int k = b + 1; k < e; k++) {
+            const int v = perm[k];
+            const int key = uid[v];
+            int m = k - 1;
+            while(m >= b && uid[perm[m]] > key) { perm[m + 1] = perm[m]; m--; }
+            perm[m + 1] = v;
+        }
+    }
+    const int wm = warp_max(cnt);
+    if((threadIdx.x & 31) == 0 && wm > 0) { atomicMax(&status->max_cell_count, wm); }
+}
+
+// new[k] = old[perm[k]] for element sizes 4, 8, 16, 32 bytes
+template<typename T>
+__global__ void k_gather(int n, const int32_t *perm, const T *src, T *dst) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k < n) { dst[k] = src[perm[k]]; }
+}
+
+struct alignas(32) Blob32 { D4 v; };
+
+int gather_array(int n, const int32_t *perm, const void *src, void *dst, int elem_bytes,
+                 cudaStream_t st) {
+    const int nb = blocks_for(n);
+    switch(elem_bytes) {
+        case 4: k_gather<<<nb, kBlock, 0, st>>>(n, perm, (const int32_t *) src, (int32_t *) dst); note_launch(); break;
+        case 8: k_gather<<<nb, kBlock, 0, st>>>(n, perm, (const int2 *) src, (int2 *) dst); note_launch(); break;
+        case 16: k_gather<<<nb, kBlock, 0, st>>>(n, perm, (const int4 *) src, (int4 *) dst); note_launch(); break;
+        case 32: k_gather<<<nb, kBlock, 0, st>>>(n, perm, (const Blob32 *) src, (Blob32 *) dst); note_launch(); break;
+        default: return PG_ERR_ARGUMENT;
+    }
+    return launch_status();
+}
+
+__global__ void k_split_positions(pg_box box, pg_particles p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= p.n) { return; }
+    const D4 x = ld_d4_plain(p.pos, i);
+    const double q = box.quantum, iq = 1.0 / q;
+    float4 h, l;
+    split_pos(x.x, iq, q, h.x, l.x);
+    split_pos(x.y, iq, q, h.y, l.y);
+    split_pos(x.z, iq, q, h.z, l.z);
+    h.w = __int_as_float(p.type != nullptr ? p.type[i] : 0);
+    l.w = 0.0f;
+    st_f4(p.pos_hi, i, h);
+    st_f4(p.pos_lo, i, l);
+}
+
+// workspace layout for pg_bin_particles (all offsets 256-byte aligned)
+struct BinWs {
+    int32_t *count, *start, *cursor, *block_sums, *perm;
+    char *stage;                      // staging for one gathered array (32 B/particle)
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
+
+static size_t bin_ws_layout(int32_t n, int32_t ncells, char *base, BinWs *w) {
+    const size_t nc = (size_t) ncells + 2;
+    const size_t nb = (nc + kScanBlock - 1) / kScanBlock + 1;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char *p = base ? base + off : nullptr; off += align256(bytes); return p; };
+    BinWs tmp;
+    tmp.count = (int32_t *) take(nc * 4);
+    tmp.start = (int32_t *) take((nc + 1) * 4);
+    tmp.cursor = (int32_t *) take(nc * 4);
+    tmp.block_sums = (int32_t *) take(nb * 4);
+    tmp.perm = (int32_t *) take((size_t) n * 4);
+    tmp.stage = take((size_t) n * 32);
+    if(w) { *w = tmp; }
+    return off;
+}
+
+int64_t bin_workspace_bytes(int32_t n, int32_t ncells) {
+    return (int64_t) bin_ws_layout(n, ncells, nullptr, nullptr);
+}
+
+int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_workspace ws,
+                  pg_status *status, cudaStream_t st, int32_t **perm_out) {
+    if(box == nullptr || p == nullptr || cells == nullptr || status == nullptr) { return PG_ERR_ARGUMENT; }
+    if(p->n < 0 || p->n > p->capacity || p->pos == nullptr) { return PG_ERR_ARGUMENT; }
+    if(cells->ncells != cells->dims[0] * cells->dims[1] * cells->dims[2]) { return PG_ERR_ARGUMENT; }
+    const int n = p->n;
+    const int ntot = cells->ncells + 1;           // + the infinite-shape bucket
+    if(ws.ptr == nullptr || ws.bytes < bin_workspace_bytes(n, cells->ncells)) { return PG_ERR_ARGUMENT; }
+    BinWs w;
+    bin_ws_layout(n, cells->ncells, (char *) ws.ptr, &w);
+    if(perm_out) { *perm_out = w.perm; }
+
+    cudaMemsetAsync(w.count, 0, (size_t) ntot * 4, st);
+    if(n > 0) {
+        k_bin_count<<<blocks_for(n), kBlock, 0, st>>>(*box, *p, *cells, w.count, status); note_launch();
+    }
+    const int nb = (ntot + kScanBlock - 1) / kScanBlock;
+    k_scan_block_sums<<<nb, kScanBlock, 0, st>>>(w.count, ntot, w.block_sums); note_launch();
+    k_scan_sums<<<1, kScanBlock, 0, st>>>(w.block_sums, nb); note_launch();
+    k_scan_apply<<<nb, kScanBlock, 0, st>>>(w.count, ntot, w.block_sums, w.start, w.cursor); note_launch();
+    if(n == 0) { return launch_status(); }
+    k_scatter<<<blocks_for(n), kBlock, 0, st>>>(n, cells->particle_cell, w.start, w.cursor, w.perm); note_launch();
+    if(p->uid != nullptr) {
+        k_sort_cells<<<blocks_for(ntot), kBlock, 0, st>>>(ntot, w.start, w.perm, p->uid, status); note_launch();
+    }
+    // permute every per-particle array through the staging buffer
+    struct Arr { void *ptr; int bytes; } arrs[] = {
+        {p->pos, 32}, {p->vel, 32}, {p->mass, 8}, {p->type, 4}, {p->uid, 4}, {p->flags, 4},
+        {cells->particle_cell, 4},
+    };
+    for(const Arr &a : arrs) {
+        if(a.ptr == nullptr) { continue; }
+        int rc = gather_array(n, w.perm, a.ptr, w.stage, a.bytes, st);
+        if(rc) { return rc; }
+        cudaMemcpyAsync(a.ptr, w.stage, (size_t) n * a.bytes, cudaMemcpyDeviceToDevice, st);
+    }
+    // cell bookkeeping for the sorted order
+    cudaMemcpyAsync(cells->cell_start, w.start, (size_t) (ntot + 1) * 4, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(cells->cell_count, w.count, (size_t) ntot * 4, cudaMemcpyDeviceToDevice, st);
+    if(p->pos_hi != nullptr && p->pos_lo != nullptr) {
+        k_split_positions<<<blocks_for(n), kBlock, 0, st>>>(*box, *p); note_launch();
+    }
+    return launch_status();
+}
+
+int split_positions(const pg_box *box, pg_particles *p, cudaStream_t st) {
+    if(box == nullptr || p == nullptr || p->pos_hi == nullptr || p->pos_lo == nullptr) { return PG_ERR_ARGUMENT; }
+    if(p->n > 0) { k_split_positions<<<blocks_for(p->n), kBlock, 0, st>>>(*box, *p); note_launch(); }
+    return launch_status();
+}
+
+}  // namespace pg

@@ -1,0 +1,239 @@
+// Lennard-Jones pair forces over the Verlet list.
+//
+// The reference's lennard_jones module (examples/md.py:5-8 lowered by
+// sim/interaction.py:222-232 and ir/apply.py:112-125):
+//   rsq < rc^2:  sr2 = 1/rsq;  sr6 = sr2^3 sigma6[ti,tj];
+//                F_i += delta * 48 sr6 (sr6 - 1/2) sr2 epsilon[ti,tj]
+// with a full list (every pair seen from both sides, no atomics) or a half list
+// (each pair once, the reaction -f applied to the partner with an atomic add).
+//
+// Two precisions:
+//   FP64   every operation in double; the cutoff test uses the reference's exact
+//          rsq (no fused multiply-add) so the same pairs interact.
+//   MIXED  delta from compensated FP32 positions (hi on a 2^-k grid, lo residual),
+//          force arithmetic and accumulation in FP32; optional energy/virial in FP64.
+//
+// One thread per particle: consecutive threads read consecutive entries of the
+// column-major list (coalesced 128-byte rows), partner positions are gathered from
+// the cell-sorted arrays (mostly L1/L2 hits).  The list stream is the dominant DRAM
+// traffic: 4 bytes per entry.
+#include "common.cuh"
+
+namespace pg {
+
+constexpr int kMaxTypes = 8;
+
+struct LJTable {
+    int ntypes;
+    float cutoff2f;
+    double cutoff2;
+    double eps[kMaxTypes * kMaxTypes];
+    double sig6[kMaxTypes * kMaxTypes];
+    float epsf[kMaxTypes * kMaxTypes];
+    float sig6f[kMaxTypes * kMaxTypes];
+};
+
+struct ForceArgs {
+    pg_box box;
+    pg_particles p;
+    pg_neighbor_list list;
+    LJTable lj;
+    int sync_ref;
+    double *energy;
+};
+
+__device__ __forceinline__ void block_add_energy(double pe, double vir, double *energy) {
+    __shared__ double s[2][kBlock / 32];
+    pe = warp_sum(pe);
+    vir = warp_sum(vir);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if(lane == 0) { s[0][w] = pe; s[1][w] = vir; }
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for(int k = 0; k < (int) (blockDim.x >> 5); k++) { a += s[0][k]; b += s[1][k]; }
+        atomicAdd(&energy[0], a);
+        atomicAdd(&energy[1], b);
+    }
+}
+
+// ---------------------------------------------------------------------------- FP64
+
+template<bool kHalf, bool kOneType, bool kEnergy>
+__global__ void __launch_bounds__(kBlock) k_lj_fp64(ForceArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double pe = 0.0, vir = 0.0;
+    if(i < a.p.n) {
+        const bool fixed = a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed);
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        if(!fixed) {
+            const D4 xi = ld_d4(a.p.pos, i);
+            const int ti = kOneType ? 0 : a.p.type[i] * a.lj.ntypes;
+            const int cnt = a.list.count[i];
+            const int32_t *nb = a.list.nbr + i;
+            const int stride = a.list.stride;
+            const int since = a.list.steps_since_build;
+            for(int k = 0; k < cnt; k++) {
+                const uint32_t e = (uint32_t) __ldg(nb + (size_t) k * stride);
+                const int j = (int) (e & PG_NBR_INDEX_MASK);
+                const uint32_t code = e >> PG_NBR_INDEX_BITS;
+                const double *base = a.p.pos;
+                if(a.sync_ref && code != 0u) {
+                    const int lag = min(max(image_dims(code) - 1, 0), since);
+                    base = lag == 0 ? a.p.pos : (lag == 1 ? a.p.pos_prev1 : a.p.pos_prev2);
+                }
+                const D4 xj = ld_d4(base, j);
+                double jx = xj.x, jy = xj.y, jz = xj.z;
+                if(code != 0u) {
+                    jx = ref_image(jx, image_shift(code, 0), a.box.len[0]);
+                    jy = ref_image(jy, image_shift(code, 1), a.box.len[1]);
+                    jz = ref_image(jz, image_shift(code, 2), a.box.len[2]);
+                }
+                const double dx = __dsub_rn(xi.x, jx), dy = __dsub_rn(xi.y, jy), dz = __dsub_rn(xi.z, jz);
+                const double rsq = ref_rsq(dx, dy, dz);
+                if(rsq < a.lj.cutoff2) {
+                    const int tij = kOneType ? 0 : ti + a.p.type[j];
+                    const double sr2 = 1.0 / rsq;
+                    const double sr6 = sr2 * sr2 * sr2 * a.lj.sig6[tij];
+                    const double f = 48.0 * sr6 * (sr6 - 0.5) * sr2 * a.lj.eps[tij];
+                    // separately rounded, in the generated order (tmp = tmp + delta*f)
+                    const double ex = __dmul_rn(dx, f), ey = __dmul_rn(dy, f), ez = __dmul_rn(dz, f);
+                    fx = __dadd_rn(fx, ex); fy = __dadd_rn(fy, ey); fz = __dadd_rn(fz, ez);
+                    if(kHalf) {
+                        double *fj = a.p.force + 4 * (size_t) j;
+                        atomicAdd(fj + 0, -ex); atomicAdd(fj + 1, -ey); atomicAdd(fj + 2, -ez);
+                    }
+                    if(kEnergy) {
+                        const double w = kHalf ? 1.0 : 0.5;
+                        pe += w * 4.0 * a.lj.eps[tij] * (sr6 * sr6 - sr6);
+                        vir += w * (dx * ex + dy * ey + dz * ez);
+                    }
+                }
+            }
+        }
+        double *fi = a.p.force + 4 * (size_t) i;
+        if(kHalf) {
+            atomicAdd(fi + 0, fx); atomicAdd(fi + 1, fy); atomicAdd(fi + 2, fz);
+        } else {
+            st_d4(a.p.force, i, make_d4(fx, fy, fz, 0.0));
+        }
+    }
+    if(kEnergy) { block_add_energy(pe, vir, a.energy); }
+}
+
+// ---------------------------------------------------------------------------- MIXED
+
+__device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float c) {
+    // one vector reduction to L2 instead of three scalar atomics (sm_90+)
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
+                 :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(0.0f) : "memory");
+}
+
+template<bool kHalf, bool kOneType, bool kEnergy>
+__global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double pe = 0.0, vir = 0.0;
+    if(i < a.p.n) {
+        const bool fixed = a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed);
+        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        if(!fixed) {
+            const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+            const int ti = kOneType ? 0 : __float_as_int(hi.w) * a.lj.ntypes;
+            const int cnt = a.list.count[i];
+            const int32_t *nb = a.list.nbr + i;
+            const int stride = a.list.stride;
+            const float c2 = a.lj.cutoff2f;
+            for(int k = 0; k < cnt; k++) {
+                const uint32_t e = (uint32_t) __ldg(nb + (size_t) k * stride);
+                const int j = (int) (e & PG_NBR_INDEX_MASK);
+                const uint32_t code = e >> PG_NBR_INDEX_BITS;
+                const float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
+                float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
+                float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
+                if(code != 0u) {
+                    const int sx = image_shift(code, 0), sy = image_shift(code, 1), sz = image_shift(code, 2);
+                    dhx -= sx * a.box.len_hi[0]; dlx -= sx * a.box.len_lo[0];
+                    dhy -= sy * a.box.len_hi[1]; dly -= sy * a.box.len_lo[1];
+                    dhz -= sz * a.box.len_hi[2]; dlz -= sz * a.box.len_lo[2];
+                }
+                const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
+                const float rsq = dx * dx + dy * dy + dz * dz;
+                if(rsq < c2) {
+                    const int tij = kOneType ? 0 : ti + __float_as_int(hj.w);
+                    const float sr2 = __frcp_rn(rsq);
+                    const float sr6 = sr2 * sr2 * sr2 * a.lj.sig6f[tij];
+                    const float f = 48.0f * sr6 * (sr6 - 0.5f) * sr2 * a.lj.epsf[tij];
+                    fx += dx * f; fy += dy * f; fz += dz * f;
+                    if(kHalf) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
+                    if(kEnergy) {
+                        const double w = kHalf ? 1.0 : 0.5;
+                        pe += w * 4.0 * (double) a.lj.epsf[tij] * ((double) sr6 * (double) sr6 - (double) sr6);
+                        vir += w * (double) (rsq * f);
+                    }
+                }
+            }
+        }
+        if(kHalf) {
+            red_add_v4(a.p.force32 + 4 * (size_t) i, fx, fy, fz);
+        } else {
+            st_f4(a.p.force32, i, make_float4(fx, fy, fz, 0.0f));
+        }
+    }
+    if(kEnergy) { block_add_energy(pe, vir, a.energy); }
+}
+
+using KernelFn = void (*)(ForceArgs);
+
+static KernelFn pick_fp64(bool half, bool one, bool en) {
+    if(half) {
+        if(one) { return en ? k_lj_fp64<true, true, true> : k_lj_fp64<true, true, false>; }
+        return en ? k_lj_fp64<true, false, true> : k_lj_fp64<true, false, false>;
+    }
+    if(one) { return en ? k_lj_fp64<false, true, true> : k_lj_fp64<false, true, false>; }
+    return en ? k_lj_fp64<false, false, true> : k_lj_fp64<false, false, false>;
+}
+
+static KernelFn pick_mixed(bool half, bool one, bool en) {
+    if(half) {
+        if(one) { return en ? k_lj_mixed<true, true, true> : k_lj_mixed<true, true, false>; }
+        return en ? k_lj_mixed<true, false, true> : k_lj_mixed<true, false, false>;
+    }
+    if(one) { return en ? k_lj_mixed<false, true, true> : k_lj_mixed<false, true, false>; }
+    return en ? k_lj_mixed<false, false, true> : k_lj_mixed<false, false, false>;
+}
+
+int lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list,
+             const pg_lj_params *lj, int precision, int sync_mode, double *energy, cudaStream_t st) {
+    if(!box || !p || !list || !lj) { return PG_ERR_ARGUMENT; }
+    if(lj->ntypes < 1 || lj->ntypes > kMaxTypes) { return PG_ERR_ARGUMENT; }
+    if(precision != PG_FP64 && precision != PG_MIXED) { return PG_ERR_ARGUMENT; }
+    if(precision == PG_FP64 && (!p->pos || !p->force)) { return PG_ERR_ARGUMENT; }
+    if(precision == PG_MIXED && (!p->pos_hi || !p->pos_lo || !p->force32)) { return PG_ERR_ARGUMENT; }
+    if(lj->ntypes > 1 && !p->type) { return PG_ERR_ARGUMENT; }
+    if(sync_mode == PG_SYNC_REFERENCE && (precision != PG_FP64 || !p->pos_prev1 || !p->pos_prev2)) {
+        return PG_ERR_ARGUMENT;
+    }
+    ForceArgs a;
+    a.box = *box; a.p = *p; a.list = *list;
+    a.sync_ref = sync_mode == PG_SYNC_REFERENCE;
+    a.energy = energy;
+    a.lj.ntypes = lj->ntypes;
+    a.lj.cutoff2 = lj->cutoff2;
+    a.lj.cutoff2f = (float) lj->cutoff2;
+    for(int k = 0; k < lj->ntypes * lj->ntypes; k++) {
+        a.lj.eps[k] = lj->epsilon[k]; a.lj.sig6[k] = lj->sigma6[k];
+        a.lj.epsf[k] = (float) lj->epsilon[k]; a.lj.sig6f[k] = (float) lj->sigma6[k];
+    }
+    const bool half = list->half != 0, one = lj->ntypes == 1, en = energy != nullptr;
+    if(en) { cudaMemsetAsync(energy, 0, 2 * sizeof(double), st); }
+    if(half) {
+        if(precision == PG_FP64) { cudaMemsetAsync(p->force, 0, (size_t) p->n * 32, st); }
+        else { cudaMemsetAsync(p->force32, 0, (size_t) p->n * 16, st); }
+    }
+    if(p->n == 0) { return launch_status(); }
+    KernelFn k = precision == PG_FP64 ? pick_fp64(half, one, en) : pick_mixed(half, one, en);
+    k<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch();
+    return launch_status();
+}
+
+}  // namespace pg

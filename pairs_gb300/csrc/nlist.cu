@@ -1,0 +1,124 @@
+// Verlet neighbour-list build over the sorted cell grid.
+//
+// Replaces the reference's build_neighbor_lists module (sim/neighbor_lists.py:21-48,
+// inner loop sim/interaction.py:90-120): for every particle scan the 27 surrounding
+// cells and keep partners with rsq < r_list^2.  Periodic boundaries are resolved
+// in-kernel: a stencil cell that wraps around the box contributes its particles as
+// images x_j + s*len (s in {-1,0,1} per dimension), exactly the positions the
+// reference's ghost particles carry (sim/comm.py:302-330), so the accepted set is the
+// reference's set of (particle, partner, image) triples.
+//
+// Acceptance is decided bit-exactly as the reference decides it (FP64, separately
+// rounded, (dx*dx + dy*dy) + dz*dz < r_list2).  Evaluating every candidate in FP64
+// would make the build FP64-ALU bound (GB300 FP64 is ~1/60 of FP32), so candidates
+// are first screened with compensated FP32 positions (relative error of rsq below
+// 1e-6); only candidates within a relative band of 1e-4 around r_list2 are decided
+// in FP64.
+#include "common.cuh"
+
+namespace pg {
+
+constexpr float kBand = 1.0e-4f;
+
+struct ListArgs {
+    pg_box box;
+    pg_particles p;
+    pg_cells cells;
+    pg_neighbor_list list;
+    double r_list2;
+    float r2_lo, r2_hi;      // screening band
+};
+
+__device__ __forceinline__ float comp_delta(float hi_i, float lo_i, float hi_j, float lo_j, int s,
+                                            float len_hi, float len_lo) {
+    const float sh = s == 0 ? 0.0f : (s > 0 ? len_hi : -len_hi);
+    const float sl = s == 0 ? 0.0f : (s > 0 ? len_lo : -len_lo);
+    const float dh = __fsub_rn(__fsub_rn(hi_i, hi_j), sh);       // exact on the hi grid
+    const float dl = __fsub_rn(__fsub_rn(lo_i, lo_j), sl);
+    return __fadd_rn(dh, dl);
+}
+
+__global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= a.p.n) { return; }
+    const D4 xi = ld_d4(a.p.pos, i);
+    st_d4(a.p.pos_ref, i, xi);
+    int cnt = 0;
+    const bool fixed = a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed);
+    const int ci = a.cells.particle_cell[i];
+    if(!fixed && ci < a.cells.ncells) {
+        const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+        const int dz_ = a.cells.dims[2], dy_ = a.cells.dims[1], dx_ = a.cells.dims[0];
+        const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
+        const int stride = a.list.stride, cap = a.list.max_neighbors;
+        int32_t *out = a.list.nbr + i;
+        for(int ox = -1; ox <= 1; ox++) {
+            int nx = cx + ox, sx = 0;
+            if(nx < 0) { if(!a.box.periodic[0]) { continue; } nx += dx_; sx = -1; }
+            else if(nx >= dx_) { if(!a.box.periodic[0]) { continue; } nx -= dx_; sx = 1; }
+            for(int oy = -1; oy <= 1; oy++) {
+                int ny = cy + oy, sy = 0;
+                if(ny < 0) { if(!a.box.periodic[1]) { continue; } ny += dy_; sy = -1; }
+                else if(ny >= dy_) { if(!a.box.periodic[1]) { continue; } ny -= dy_; sy = 1; }
+                for(int oz = -1; oz <= 1; oz++) {
+                    int nz = cz + oz, sz = 0;
+                    if(nz < 0) { if(!a.box.periodic[2]) { continue; } nz += dz_; sz = -1; }
+                    else if(nz >= dz_) { if(!a.box.periodic[2]) { continue; } nz -= dz_; sz = 1; }
+                    const int c = (nx * dy_ + ny) * dz_ + nz;
+                    const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
+                    const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
+                    for(int j = b; j < e; j++) {
+                        if(j == i) { continue; }
+                        if(a.list.half && j < i) { continue; }
+                        const float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
+                        const float fx = comp_delta(hi.x, lo.x, hj.x, lj.x, sx, a.box.len_hi[0], a.box.len_lo[0]);
+                        const float fy = comp_delta(hi.y, lo.y, hj.y, lj.y, sy, a.box.len_hi[1], a.box.len_lo[1]);
+                        const float fz = comp_delta(hi.z, lo.z, hj.z, lj.z, sz, a.box.len_hi[2], a.box.len_lo[2]);
+                        const float r2f = fx * fx + fy * fy + fz * fz;
+                        bool keep;
+                        if(r2f < a.r2_lo) { keep = true; }
+                        else if(r2f > a.r2_hi) { keep = false; }
+                        else {
+                            const D4 xj = ld_d4(a.p.pos, j);
+                            const double ddx = __dsub_rn(xi.x, ref_image(xj.x, sx, a.box.len[0]));
+                            const double ddy = __dsub_rn(xi.y, ref_image(xj.y, sy, a.box.len[1]));
+                            const double ddz = __dsub_rn(xi.z, ref_image(xj.z, sz, a.box.len[2]));
+                            keep = ref_rsq(ddx, ddy, ddz) < a.r_list2;
+                        }
+                        if(keep) {
+                            if(cnt < cap) { out[(size_t) cnt * stride] = (int32_t) (code | (uint32_t) j); }
+                            cnt++;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    a.list.count[i] = cnt < a.list.max_neighbors ? cnt : a.list.max_neighbors;
+    const int wm = warp_max(cnt);
+    if((threadIdx.x & 31) == 0 && wm > 0) {
+        atomicMax(&status->max_neighbors, wm);
+        if(wm > a.list.max_neighbors) { atomicOr(&status->overflow, 2); }
+    }
+}
+
+int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
+                         pg_neighbor_list *list, double r_list2, pg_status *status, cudaStream_t st) {
+    if(!box || !p || !cells || !list || !status) { return PG_ERR_ARGUMENT; }
+    if(!p->pos || !p->pos_hi || !p->pos_lo || !p->pos_ref || !list->nbr || !list->count) { return PG_ERR_ARGUMENT; }
+    if(list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS)) { return PG_ERR_ARGUMENT; }
+    for(int d = 0; d < 3; d++) {
+        // a stencil of one cell each side covers r_list only if cells are >= r_list
+        if(cells->cell_len[d] * cells->cell_len[d] < r_list2) { return PG_ERR_ARGUMENT; }
+        if(box->periodic[d] && box->len[d] * box->len[d] <= r_list2) { return PG_ERR_ARGUMENT; }
+    }
+    ListArgs a;
+    a.box = *box; a.p = *p; a.cells = *cells; a.list = *list; a.r_list2 = r_list2;
+    a.r2_lo = (float) r_list2 * (1.0f - kBand);
+    a.r2_hi = (float) r_list2 * (1.0f + kBand);
+    list->steps_since_build = 0;
+    if(p->n > 0) { k_build_list<<<blocks_for(p->n), kBlock, 0, st>>>(a, status); note_launch(); }
+    return launch_status();
+}
+
+}  // namespace pg

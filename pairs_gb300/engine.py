@@ -1,0 +1,338 @@
+"""Device state and time stepping of the LJ particle path on one GPU.
+
+`LJEngine` owns every buffer as a torch tensor (the C library allocates nothing)
+and runs the reference's time-step order (sim/simulation.py:387-417,
+sim/timestep.py:36-61) through the C ABI:
+
+    ts > 0:   initial_integrate            (pre_step, skip_first)
+    rebuild:  bin particles (wrap + cell sort) + build Verlet list
+    always:   LJ force
+    ts > 0:   final_integrate              (skip_first)
+    cadence:  thermo
+
+A rebuild happens when the schedule asks for it ((ts+1) % every == 0 or ts == 0 for
+the reference's fixed schedule) and also whenever the FP64 displacement guard saw a
+particle move more than skin/2 since the last build (policy "guard").  Capacity
+overflow follows the reference's resize protocol: the kernel reports the size it
+needed, the host grows the buffer and re-runs the build
+(transformations/modules.py:159-205).
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _capi as A
+
+INT32_MAX = 2 ** 31 - 1
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _box_quantum(lo, hi):
+    span = max(max(abs(lo[d]), abs(hi[d])) + (hi[d] - lo[d]) for d in range(3))
+    return 2.0 ** (math.ceil(math.log2(span)) - 22)
+
+
+class LJEngine:
+    """One periodic (or walled) box of point masses with Lennard-Jones forces."""
+
+    def __init__(self, state, *, lo=None, hi=None, periodic=(True, True, True), cutoff=2.5, skin=0.3,
+                 dt=0.005, ntypes=1, epsilon=None, sigma6=None, precision="fp64", half=False,
+                 sync="exact", every=20, neighbor_capacity=100, policy="fixed", device="cuda",
+                 capacity=None, fused=True):
+        A.load()
+        if not torch.cuda.is_available():
+            raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
+        self.dev = torch.device(device)
+        self.precision = {"fp64": A.PG_FP64, "mixed": A.PG_MIXED}[precision]
+        self.sync = {"exact": A.PG_SYNC_EXACT, "reference": A.PG_SYNC_REFERENCE}[sync]
+        if self.sync == A.PG_SYNC_REFERENCE and self.precision != A.PG_FP64:
+            raise ValueError("reference image sync is defined for the FP64 path only")
+        if policy not in ("fixed", "guard", "fixed+guard"):
+            raise ValueError(f"unknown rebuild policy {policy!r}")
+        self.policy = policy
+        self.fused = fused and self.sync == A.PG_SYNC_EXACT
+        pos = np.asarray(state["pos"], dtype=np.float64)
+        n = len(pos)
+        box = np.asarray(state["box"], dtype=np.float64)
+        lo = np.zeros(3) if lo is None else np.asarray(lo, dtype=np.float64)
+        hi = lo + box if hi is None else np.asarray(hi, dtype=np.float64)
+        self.n = n
+        self.cap = int(capacity or n)
+        self.cutoff, self.skin, self.dt, self.every = cutoff, skin, dt, every
+        self.r_list = cutoff + skin
+        self.r_list2 = self.r_list * self.r_list
+        self.half_skin2 = (0.5 * skin) ** 2
+        self.ts = 0
+        self.since_build = 0
+        self.nbuilds = 0
+        self.thermo_log = []
+
+        # ---- box
+        self.box = A.PgBox()
+        q = _box_quantum(lo, hi)
+        for d in range(3):
+            self.box.lo[d], self.box.hi[d] = lo[d], hi[d]
+            self.box.len[d] = hi[d] - lo[d]
+            self.box.periodic[d] = int(bool(periodic[d]))
+            lh = round(self.box.len[d] / q) * q
+            self.box.len_hi[d] = lh
+            self.box.len_lo[d] = self.box.len[d] - lh
+        self.box.quantum = q
+
+        # ---- particles
+        f64, f32, i32 = torch.float64, torch.float32, torch.int32
+        cap = self.cap
+        z = lambda shape, dt: torch.zeros(shape, dtype=dt, device=self.dev)
+        self.t = {}
+        t = self.t
+        t["pos"] = z((cap, 4), f64)
+        t["vel"] = z((cap, 4), f64)
+        t["pos_ref"] = z((cap, 4), f64)
+        t["pos_hi"] = z((cap, 4), f32)
+        t["pos_lo"] = z((cap, 4), f32)
+        t["mass"] = z((cap,), f64)
+        t["type"] = z((cap,), i32)
+        t["uid"] = z((cap,), i32)
+        t["flags"] = z((cap,), i32)
+        if self.precision == A.PG_FP64:
+            t["force"] = z((cap, 4), f64)
+        else:
+            t["force32"] = z((cap, 4), f32)
+        if self.sync == A.PG_SYNC_REFERENCE:
+            t["pos_prev1"] = z((cap, 4), f64)
+            t["pos_prev2"] = z((cap, 4), f64)
+        hp = torch.zeros((n, 4), dtype=f64)
+        hp[:, :3] = torch.from_numpy(pos)
+        t["pos"][:n].copy_(hp)
+        hv = torch.zeros((n, 4), dtype=f64)
+        hv[:, :3] = torch.from_numpy(np.asarray(state["vel"], dtype=np.float64))
+        t["vel"][:n].copy_(hv)
+        t["mass"][:n].copy_(torch.from_numpy(np.asarray(state["mass"], dtype=np.float64)))
+        t["type"][:n].copy_(torch.from_numpy(np.asarray(state["type"], dtype=np.int32)))
+        uid = state.get("uid")
+        uid = np.arange(n, dtype=np.int32) if uid is None else np.asarray(uid, dtype=np.int32)
+        t["uid"][:n].copy_(torch.from_numpy(uid))
+        if state.get("flags") is not None:
+            t["flags"][:n].copy_(torch.from_numpy(np.asarray(state["flags"], dtype=np.int32)))
+        self.p = A.PgParticles()
+        self.p.n, self.p.capacity = n, cap
+        self._bind_particles()
+
+        # ---- cells
+        self.cells = A.PgCells()
+        ncells = 1
+        for d in range(3):
+            L = self.box.len[d]
+            dims = max(1, int(math.floor(L / self.r_list)))
+            self.cells.dims[d] = dims
+            self.cells.cell_len[d] = L / dims
+            ncells *= dims
+        self.cells.ncells = ncells
+        t["cell_start"] = z((ncells + 2,), i32)
+        t["cell_count"] = z((ncells + 1,), i32)
+        t["particle_cell"] = z((cap,), i32)
+        self.cells.cell_start = t["cell_start"].data_ptr()
+        self.cells.cell_count = t["cell_count"].data_ptr()
+        self.cells.particle_cell = t["particle_cell"].data_ptr()
+
+        # ---- neighbour list
+        self.list = A.PgNeighborList()
+        self.list.stride = cap
+        self.list.half = int(bool(half))
+        self._alloc_list(int(neighbor_capacity))
+
+        # ---- LJ parameters
+        self.lj = A.PgLJParams()
+        self.lj.ntypes = ntypes
+        self.lj.cutoff2 = cutoff * cutoff
+        eps = np.ones(ntypes * ntypes) if epsilon is None else np.asarray(epsilon, dtype=np.float64)
+        sig6 = np.ones(ntypes * ntypes) if sigma6 is None else np.asarray(sigma6, dtype=np.float64)
+        for k in range(ntypes * ntypes):
+            self.lj.epsilon[k], self.lj.sigma6[k] = eps[k], sig6[k]
+
+        # ---- status, workspace, small outputs
+        init = A.PgStatus()
+        init.guard_tripped = INT32_MAX
+        t["status_init"] = torch.tensor(np.frombuffer(bytes(init), dtype=np.int32).copy(), device=self.dev)
+        t["status"] = t["status_init"].clone()
+        self.status_ptr = C.c_void_p(t["status"].data_ptr())
+        wsb = A.load().pg_workspace_bytes(cap, ncells)
+        t["ws"] = torch.empty((int(wsb),), dtype=torch.uint8, device=self.dev)
+        self.ws = A.PgWorkspace(t["ws"].data_ptr(), int(wsb))
+        t["thermo"] = z((3,), f64)
+        t["energy"] = z((2,), f64)
+        self.stream = torch.cuda.current_stream(self.dev)
+        self.sh = C.c_void_p(self.stream.cuda_stream)
+        A.call("pg_split_positions", C.byref(self.box), C.byref(self.p), self.sh)
+
+    # ------------------------------------------------------------------ buffers
+
+    def _bind_particles(self):
+        t, p = self.t, self.p
+        for name in ("pos", "pos_prev1", "pos_prev2", "vel", "force", "force32", "pos_hi", "pos_lo",
+                     "pos_ref", "mass", "type", "uid", "flags"):
+            setattr(p, name, t[name].data_ptr() if name in t else None)
+
+    def _alloc_list(self, max_nb):
+        self.list.max_neighbors = max_nb
+        self.t["nbr"] = torch.zeros((max_nb, self.cap), dtype=torch.int32, device=self.dev)
+        self.t["count"] = torch.zeros((self.cap,), dtype=torch.int32, device=self.dev)
+        self.list.nbr = self.t["nbr"].data_ptr()
+        self.list.count = self.t["count"].data_ptr()
+
+    def _rotate_ring(self):
+        t = self.t
+        t["pos_prev2"], t["pos_prev1"], t["pos"] = t["pos_prev1"], t["pos"], t["pos_prev2"]
+        self._bind_particles()
+
+    def read_status(self):
+        s = self.t["status"].cpu().numpy()
+        return A.PgStatus.from_buffer_copy(s.tobytes())
+
+    def reset_status(self):
+        self.t["status"].copy_(self.t["status_init"])
+
+    # ------------------------------------------------------------------ modules
+
+    def rebuild(self):
+        """Bin + sort + Verlet build, growing the list until it fits."""
+        by = C.byref
+        A.call("pg_bin_particles", by(self.box), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
+        while True:
+            self.t["status"][0] = 0                     # overflow bits
+            self.t["status"][2] = 0                     # max_neighbors
+            A.call("pg_build_neighbor_lists", by(self.box), by(self.p), by(self.cells), by(self.list),
+                   self.r_list2, self.status_ptr, self.sh)
+            st = self.read_status()
+            if st.nonfinite:
+                raise A.PairsError("non-finite particle position met while binning")
+            if st.overflow & 2:
+                self._alloc_list(int(st.max_neighbors * 1.2) + 8)
+                continue
+            break
+        self.list.steps_since_build = 0
+        self.since_build = 0
+        self.nbuilds += 1
+        self.t["status"][4] = INT32_MAX                 # guard reset
+        self._guard_armed = False
+
+    def force(self, energy=False):
+        e = C.c_void_p(self.t["energy"].data_ptr()) if energy else None
+        A.call("pg_lj_force", C.byref(self.box), C.byref(self.p), C.byref(self.list), C.byref(self.lj),
+               self.precision, self.sync, e, self.ws, self.sh)
+
+    def initial_integrate(self):
+        if self.sync == A.PG_SYNC_REFERENCE:
+            self._rotate_ring()
+        A.call("pg_initial_integrate", C.byref(self.box), C.byref(self.p), self.dt, self.precision,
+               self.half_skin2, self.ts, self.sync, self.status_ptr, self.sh)
+
+    def final_integrate(self):
+        A.call("pg_final_integrate", C.byref(self.box), C.byref(self.p), self.dt, self.precision, self.sh)
+
+    def final_initial_integrate(self):
+        A.call("pg_final_initial_integrate", C.byref(self.box), C.byref(self.p), self.dt, self.precision,
+               self.half_skin2, self.ts, self.sync, self.status_ptr, self.sh)
+
+    def compute_thermo(self):
+        A.call("pg_compute_thermo", C.byref(self.box), C.byref(self.p), C.c_void_p(self.t["thermo"].data_ptr()),
+               self.ws, self.sh)
+        out = self.t["thermo"].cpu().numpy()
+        return float(out[0]), float(out[1])
+
+    def potential_energy(self):
+        """(PE, virial sum r.F) of the current positions (FP64 sums)."""
+        self.force(energy=True)
+        e = self.t["energy"].cpu().numpy()
+        return float(e[0]), float(e[1])
+
+    # ------------------------------------------------------------------ schedule
+
+    def needs_rebuild(self, ts):
+        fixed = ((ts + 1) % self.every == 0) or ts == 0
+        if self.policy == "fixed":
+            return fixed
+        guard = self.guard_tripped()
+        if self.policy == "guard":
+            return ts == 0 or guard
+        return fixed or guard
+
+    def guard_tripped(self):
+        return int(self.t["status"][4].item()) != INT32_MAX
+
+    def step(self, thermo_every=0):
+        """One iteration of the reference's time loop."""
+        ts = self.ts
+        if ts > 0:
+            self.initial_integrate()
+        if self.needs_rebuild(ts):
+            self.rebuild()
+        else:
+            self.since_build += 1
+            self.list.steps_since_build = self.since_build
+        self.force()
+        if ts > 0:
+            self.final_integrate()
+        if thermo_every and (ts == 0 or (ts + 1) % thermo_every == 0):
+            self.thermo_log.append((ts,) + self.compute_thermo())
+        self.ts += 1
+
+    def run(self, nsteps, thermo_every=0):
+        for _ in range(nsteps):
+            self.step(thermo_every)
+
+    def upload(self, pos, vel, mass=None, type=None, uid=None):
+        """Replace the particle state with host arrays (n x 4 or n x 3 FP64 pos/vel,
+        in any order; pinned memory makes the copies asynchronous).  The next step is
+        a fresh first step (force only, rebuild)."""
+        n = self.n
+        t = self.t
+        for key, src in (("pos", pos), ("vel", vel)):
+            if src.shape[1] == 4:
+                t[key][:n].copy_(src, non_blocking=True)
+            else:
+                t[key][:n, :3].copy_(src, non_blocking=True)
+        for key, src in (("mass", mass), ("type", type), ("uid", uid)):
+            if src is not None:
+                t[key][:n].copy_(src, non_blocking=True)
+        self.ts = 0
+
+    # ------------------------------------------------------------------ readback
+
+    def state(self):
+        """Positions, velocities, forces as numpy arrays in uid order."""
+        n = self.n
+        uid = self.t["uid"][:n].cpu().numpy()
+        order = np.argsort(uid, kind="stable")
+        pos = self.t["pos"][:n, :3].cpu().numpy()[order]
+        vel = self.t["vel"][:n, :3].cpu().numpy()[order]
+        if self.precision == A.PG_FP64:
+            frc = self.t["force"][:n, :3].cpu().numpy()[order]
+        else:
+            frc = self.t["force32"][:n, :3].cpu().numpy().astype(np.float64)[order]
+        return pos, vel, frc
+
+    def pairs(self):
+        """Verlet entries as (uid_i, uid_j, sx, sy, sz) rows (list order per particle)."""
+        n = self.n
+        cnt = self.t["count"][:n].cpu().numpy()
+        nbr = self.t["nbr"][:, :n].cpu().numpy().astype(np.uint32)
+        uid = self.t["uid"][:n].cpu().numpy()
+        rows = []
+        kk = np.arange(nbr.shape[0])[:, None]
+        mask = kk < cnt[None, :]
+        e = nbr[mask.nonzero()]
+        ii = np.broadcast_to(np.arange(n)[None, :], nbr.shape)[mask.nonzero()]
+        j = (e & ((1 << A.NBR_INDEX_BITS) - 1)).astype(np.int64)
+        code = e >> A.NBR_INDEX_BITS
+        dec = lambda c: np.where(c == 1, 1, np.where(c == 2, -1, 0))
+        rows = np.stack([uid[ii], uid[j], dec(code & 3), dec((code >> 2) & 3), dec((code >> 4) & 3)], axis=1)
+        return rows.astype(np.int32)
+
+    def cell_occupancy(self):
+        return self.t["cell_count"][: self.cells.ncells].cpu().numpy()

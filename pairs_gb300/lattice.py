@@ -1,0 +1,121 @@
+"""Initial particle states: the reference's fcc lattice and its thermo adjustment.
+
+Host-side setup (like the reference's runtime, which builds the lattice on the host
+before the time loop).  Restates, vectorised and bit-identical in FP64:
+
+* runtime/copper_fcc_lattice.hpp:64-145 -- fcc sites (i+j+k even on a 2n grid of
+  a/2) visited in 8^3 sub-box order, per-site Park-Miller velocities
+  (:18-26 without masking; seed = site index + 1, five discarded draws before each
+  component), mass 1, type = rand() % ntypes in visiting order;
+* runtime/thermo.hpp:53-97 -- subtract the mean velocity, rescale to T, with the
+  reference's sequential FP64 summation order.
+
+rand() is the C library generator the reference calls unseeded; glibc's is an
+additive lagged-Fibonacci generator (r[i] = r[i-3] + r[i-31] mod 2^32, 34 seeded
+words from the minimal-standard LCG, first 310 outputs discarded, result r >> 1),
+restated here so the type stream matches.
+"""
+import numpy as np
+
+_IA, _IM, _IQ, _IR = 16807, 2147483647, 127773, 2836
+
+
+def _park_miller(seed):
+    """One Park-Miller step on an int64 array of seeds; returns (seed, value)."""
+    k = seed // _IQ
+    seed = _IA * (seed - k * _IQ) - _IR * k
+    seed = np.where(seed < 0, seed + _IM, seed)
+    return seed, (1.0 / _IM) * seed.astype(np.float64)
+
+
+def glibc_rand(count, seed=1):
+    """First `count` outputs of glibc rand() after srand(seed)."""
+    r = [0] * 34
+    r[0] = seed
+    for i in range(1, 31):
+        hi, lo = divmod(r[i - 1], 127773)
+        w = 16807 * lo - 2836 * hi
+        if w < 0:
+            w += 2147483647
+        r[i] = w
+    for i in range(31, 34):
+        r[i] = r[i - 31]
+    out = []
+    buf = r
+    total = 344 + count
+    for i in range(34, total):
+        buf.append((buf[i - 31] + buf[i - 3]) & 0xFFFFFFFF)
+        if i >= 344:
+            out.append(buf[i] >> 1)
+    return np.array(out, dtype=np.int64)
+
+
+def fcc_sites(nx, ny, nz, rho):
+    """Lattice sites of copper_fcc_lattice in the reference's visiting order.
+
+    Returns (i, j, k) integer arrays and the lattice constant."""
+    alat = pow(4.0 / rho, 1.0 / 3.0)
+    xprd, yprd, zprd = nx * alat, ny * alat, nz * alat
+    half = 0.5 * alat
+    ihi = min(int(xprd / half + 1), 2 * nx - 1)
+    jhi = min(int(yprd / half + 1), 2 * ny - 1)
+    khi = min(int(zprd / half + 1), 2 * nz - 1)
+    sub = 8
+    nox, noy, noz = ihi // sub + 1, jhi // sub + 1, khi // sub + 1
+    # order: sx fastest, then sy, sz, ox, oy, oz
+    oz, oy, ox, sz, sy, sx = np.meshgrid(np.arange(noz), np.arange(noy), np.arange(nox),
+                                         np.arange(sub), np.arange(sub), np.arange(sub), indexing="ij")
+    i = (ox * sub + sx).ravel().astype(np.int64)
+    j = (oy * sub + sy).ravel().astype(np.int64)
+    k = (oz * sub + sz).ravel().astype(np.int64)
+    keep = ((i + j + k) % 2 == 0) & (i <= ihi) & (j <= jhi) & (k <= khi)
+    i, j, k = i[keep], j[keep], k[keep]
+    x, y, z = half * i, half * j, half * k
+    small = 0.00001                               # regular_6d_stencil.hpp:6
+    inside = (x >= 0.0) & (x < xprd - small) & (y >= 0.0) & (y < yprd - small) & \
+             (z >= 0.0) & (z < zprd - small)
+    return i[inside], j[inside], k[inside], alat
+
+
+def copper_fcc_lattice(nx, ny, nz, rho=0.8442, temperature=1.44, ntypes=1):
+    """The reference's LJ initial state.  Returns a dict with pos, vel (n, 3) float64,
+    mass (n,), type (n,) int32, uid (n,) = creation index, and box (3,)."""
+    i, j, k, alat = fcc_sites(nx, ny, nz, rho)
+    half = 0.5 * alat
+    pos = np.stack([half * i, half * j, half * k], axis=1)
+    seed = k * (2 * ny) * (2 * nx) + j * (2 * nx) + i + 1
+    vel = np.empty_like(pos)
+    for c in range(3):
+        for _ in range(5):
+            seed, _v = _park_miller(seed)
+        seed, vel[:, c] = _park_miller(seed)
+    n = len(pos)
+    mass = np.ones(n)
+    if ntypes > 1:
+        typ = (glibc_rand(n) % ntypes).astype(np.int32)
+    else:
+        typ = np.zeros(n, dtype=np.int32)
+    box = np.array([nx * alat, ny * alat, nz * alat])
+    adjust_thermo(mass, vel, box, temperature)
+    return dict(pos=pos, vel=vel, mass=mass, type=typ, uid=np.arange(n, dtype=np.int32), box=box)
+
+
+def _seq_sum(a):
+    """Left-to-right FP64 sum (the reference's loop order)."""
+    return np.cumsum(a)[-1] if len(a) else 0.0
+
+
+def temperature(mass, vel):
+    """T = sum m (vx*vx + vy*vy + vz*vz) / (3N-3), reference summation order."""
+    n = len(mass)
+    s = mass * ((vel[:, 0] * vel[:, 0] + vel[:, 1] * vel[:, 1]) + vel[:, 2] * vel[:, 2])
+    return _seq_sum(s) * (1.0 / (n * 3 - 3))
+
+
+def adjust_thermo(mass, vel, box, temp):
+    """Zero the total momentum (mean velocity) and rescale to `temp`, in place."""
+    n = len(mass)
+    for c in range(3):
+        vel[:, c] -= _seq_sum(vel[:, c]) / n
+    t = temperature(mass, vel)
+    vel *= np.sqrt(temp / t)
