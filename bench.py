@@ -170,7 +170,9 @@ def run_ours(args, rank, world, dist):
         return ms, fms, launches
 
     # headline: mixed precision, half list (Newton's third law), fixed reference schedule
-    eng = make("mixed", True)
+    prec, half = {"mixed-half": ("mixed", True), "mixed-full": ("mixed", False),
+                  "fp64-half": ("fp64", True), "fp64-full": ("fp64", False)}[args.variant]
+    eng = make(prec, half)
     clocks = ClockSampler(dev.index or 0)
     clocks.start()
     ms, fms, launches = timed(eng, args.steps, args.warmup)
@@ -181,17 +183,23 @@ def run_ours(args, rank, world, dist):
         ms = float(t.item())
     value = n * args.steps * world / (ms / 1e3)
     pairs_total = int(eng.t["count"][:n].sum().item())
-    # algorithmic bytes of one force launch: own hi+lo position (32), count (4),
-    # force (16), 4 bytes per list entry, half list: reaction add per particle (16)
-    b_force = n * (32 + 4 + 16) + 4 * pairs_total + (n * 16 if eng.list.half else 0)
+    # algorithmic bytes of one force launch: own position (32: FP32 hi+lo, or FP64
+    # x,y,z,pad), neighbour count (4), force write (16 FP32 / 32 FP64), 4 bytes per
+    # Verlet entry; a half list adds one reaction write per particle (b_F)
+    b_f = 16 if prec == "mixed" else 32
+    b_force = n * (32 + 4 + b_f) + 4 * pairs_total + (n * b_f if eng.list.half else 0)
     f_avg = statistics.mean(fms) if fms else float("nan")
     pk, pk_kind = peaks()
     achieved = b_force / (f_avg / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_kind": pk_kind,
-                "traffic": traffic_from_profiles("k_lj_mixed"), "kernel": "k_lj_mixed<half>",
+                "traffic": traffic_from_profiles("k_lj_mixed"), "kernel": "k_lj_%s" % args.variant,
                 "kernel_ms": round(f_avg, 4), "algorithmic_bytes": b_force, "list_entries": pairs_total}
     nbuilds = eng.nbuilds
+    if args.only_headline:
+        print(json.dumps({"variant": args.variant, "value": value, "ms_per_step": ms / args.steps,
+                          "roofline": roofline, "gpu_launches": launches, "clocks": clk}))
+        return
 
     # plain FP64 path on the same workload (full list and half list; best reported)
     fp64 = {}
@@ -321,6 +329,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    ap.add_argument("--variant", choices=["mixed-half", "mixed-full", "fp64-half", "fp64-full"],
+                    default="mixed-half")
+    ap.add_argument("--only-headline", action="store_true",
+                    help="time the headline arm only (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist, rank, world, _ = dist_setup()

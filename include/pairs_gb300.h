@@ -95,6 +95,8 @@ typedef struct {
     float  *pos_hi;              /* float4[capacity]  (PG_MIXED); w = type as float bits */
     float  *pos_lo;              /* float4[capacity]  (PG_MIXED) */
     double *pos_ref;             /* double4[capacity] positions at last rebuild (guard) */
+    float  *ref_hi;              /* float4[capacity]  pos_hi at last rebuild (guard screen) */
+    float  *ref_lo;              /* float4[capacity]  pos_lo at last rebuild */
     double *mass;                /* [capacity] */
     int32_t *type;               /* [capacity] */
     int32_t *uid;                /* [capacity] user id (the reference's uid property) */
@@ -193,6 +195,14 @@ int pg_final_integrate(const pg_box *box, pg_particles *p, double dt, int precis
 int pg_final_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,
                                double half_skin2, int32_t step, int sync_mode, pg_status *status,
                                void *stream);
+
+/* Mixed-precision integration (FP32 force in, FP64 velocity/position update):
+ * kicks = 1 or 2 half kicks merged into one (v += kicks*(dt/2)*F/m), then, if drift,
+ * x += dt*v in FP64, pos_hi/pos_lo re-split from the new x, and the FP64
+ * displacement guard (screened in FP32 against ref_hi/ref_lo, decided in FP64 near
+ * the threshold) recorded in status->guard_tripped. */
+int pg_integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks, int drift,
+                       double half_skin2, int32_t step, pg_status *status, void *stream);
 
 /* Sum m v^2 over particles (FP64, fixed reduction tree, deterministic) and
  * write out[0] = T = sum/(3N-3), out[1] = kinetic pressure T(3N-3)/(3V), out[2] = sum

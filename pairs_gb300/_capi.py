@@ -41,6 +41,7 @@ class PgParticles(C.Structure):
                 ("pos", C.c_void_p), ("pos_prev1", C.c_void_p), ("pos_prev2", C.c_void_p),
                 ("vel", C.c_void_p), ("force", C.c_void_p), ("force32", C.c_void_p),
                 ("pos_hi", C.c_void_p), ("pos_lo", C.c_void_p), ("pos_ref", C.c_void_p),
+                ("ref_hi", C.c_void_p), ("ref_lo", C.c_void_p),
                 ("mass", C.c_void_p), ("type", C.c_void_p), ("uid", C.c_void_p),
                 ("flags", C.c_void_p)]
 
@@ -84,6 +85,8 @@ SIGNATURES = {
     "pg_final_integrate": (C.c_int, [P(PgBox), P(PgParticles), C.c_double, C.c_int, C.c_void_p]),
     "pg_final_initial_integrate": (C.c_int, [P(PgBox), P(PgParticles), C.c_double, C.c_int, C.c_double,
                                              C.c_int32, C.c_int, C.c_void_p, C.c_void_p]),
+    "pg_integrate_mixed": (C.c_int, [P(PgBox), P(PgParticles), C.c_double, C.c_int, C.c_int, C.c_double,
+                                     C.c_int32, C.c_void_p, C.c_void_p]),
     "pg_compute_thermo": (C.c_int, [P(PgBox), P(PgParticles), C.c_void_p, PgWorkspace, C.c_void_p]),
     "pg_split_positions": (C.c_int, [P(PgBox), P(PgParticles), C.c_void_p]),
     "pg_permute": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),

@@ -18,6 +18,8 @@ int final_initial_integrate(const pg_box *box, pg_particles *p, double dt, int p
                             double half_skin2, int32_t step, pg_status *status, int sync_mode,
                             cudaStream_t st);
 int64_t thermo_workspace_bytes();
+int integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks, int drift,
+                    double half_skin2, int32_t step, pg_status *status, cudaStream_t st);
 int compute_thermo(const pg_box *box, const pg_particles *p, double *out, double *partials,
                    cudaStream_t st);
 }  // namespace pg
@@ -82,6 +84,11 @@ int pg_final_initial_integrate(const pg_box *box, pg_particles *p, double dt, in
                                void *stream) {
     return pg::final_initial_integrate(box, p, dt, precision, half_skin2, step, status, sync_mode,
                                        S(stream));
+}
+
+int pg_integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks, int drift,
+                       double half_skin2, int32_t step, pg_status *status, void *stream) {
+    return pg::integrate_mixed(box, p, dt, kicks, drift, half_skin2, step, status, S(stream));
 }
 
 int pg_compute_thermo(const pg_box *box, const pg_particles *p, double *out, pg_workspace ws,

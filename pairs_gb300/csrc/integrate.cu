@@ -37,7 +37,9 @@ __device__ __forceinline__ double3 load_force(const IntArgs &a, int i) {
 }
 
 __device__ __forceinline__ double kick(double v, double h, double f, double m) {
-    return __dadd_rn(v, __ddiv_rn(__dmul_rn(h, f), m));
+    // (h*F)/m; dividing by 1.0 is exact, so unit masses skip the (slow) FP64 divide
+    const double hf = __dmul_rn(h, f);
+    return __dadd_rn(v, m == 1.0 ? hf : __ddiv_rn(hf, m));
 }
 
 __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
@@ -82,6 +84,100 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
     if(__any_sync(0xffffffffu, tripped) && (threadIdx.x & 31) == 0) {
         atomicMin(&a.status->guard_tripped, a.step);
     }
+}
+
+// ------------------------------------------------------------------ mixed precision
+// Mixed-precision step: FP32 forces in, FP64 velocity and position update, compensated
+// FP32 positions re-split from the new FP64 positions, FP64 displacement guard.
+// GB300 issues ~2 FP64 instructions per clock per SM, so FP64 work is kept to what
+// the method needs: the kicks of a deferred final half step and the next initial
+// half step are merged into one (v += k*(dt/2)*F/m, k = 1 or 2), and the guard is
+// screened with the FP32 displacement (hi - hi_ref) + (lo - lo_ref); only particles
+// within a relative band of 1e-3 of the threshold are decided by the exact FP64
+// test |x - x_ref|^2 > (skin/2)^2, so the outcome is the FP64 test's outcome.
+
+struct MixArgs {
+    pg_box box;
+    pg_particles p;
+    double dt;
+    double kick;              // k * dt/2
+    float half_skin2_lo, half_skin2_hi;
+    double half_skin2;
+    int32_t step;
+    int drift;                // 0: kick only (a final half step before thermo)
+    pg_status *status;
+};
+
+__device__ __forceinline__ void resplit(double x, float q, float iq, float &hi, float &lo) {
+    const float xf = (float) x;
+    const float h = rintf(xf * iq) * q;        // grid point near x (exact multiple of q)
+    hi = h;
+    lo = (float) (x - (double) h);
+}
+
+__global__ void __launch_bounds__(kBlock) k_integrate_mixed(MixArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool tripped = false;
+    if(i < a.p.n && !(a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed))) {
+        const float4 f = ld_f4(a.p.force32, i);
+        const double m = a.p.mass[i];
+        const double c = m == 1.0 ? a.kick : a.kick / m;
+        D4 v = ld_d4_plain(a.p.vel, i);
+        v.x = fma(c, (double) f.x, v.x);
+        v.y = fma(c, (double) f.y, v.y);
+        v.z = fma(c, (double) f.z, v.z);
+        st_d4(a.p.vel, i, v);
+        if(a.drift) {
+            D4 x = ld_d4_plain(a.p.pos, i);
+            x.x = fma(a.dt, v.x, x.x);
+            x.y = fma(a.dt, v.y, x.y);
+            x.z = fma(a.dt, v.z, x.z);
+            st_d4(a.p.pos, i, x);
+            const float q = (float) a.box.quantum, iq = 1.0f / q;
+            float4 h, l;
+            resplit(x.x, q, iq, h.x, l.x);
+            resplit(x.y, q, iq, h.y, l.y);
+            resplit(x.z, q, iq, h.z, l.z);
+            h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);   // type bits
+            l.w = 0.0f;
+            st_f4(a.p.pos_hi, i, h);
+            st_f4(a.p.pos_lo, i, l);
+            // guard, screened in FP32 against the positions of the last list build
+            const float4 rh = ld_f4(a.p.ref_hi, i);
+            const float4 rl = ld_f4(a.p.ref_lo, i);
+            const float dx = (h.x - rh.x) + (l.x - rl.x);
+            const float dy = (h.y - rh.y) + (l.y - rl.y);
+            const float dz = (h.z - rh.z) + (l.z - rl.z);
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            if(d2 > a.half_skin2_hi) {
+                tripped = true;
+            } else if(d2 > a.half_skin2_lo) {
+                const D4 r = ld_d4_plain(a.p.pos_ref, i);
+                const double ex = x.x - r.x, ey = x.y - r.y, ez = x.z - r.z;
+                tripped = (ex * ex + ey * ey + ez * ez) > a.half_skin2;
+            }
+        }
+    }
+    if(__any_sync(0xffffffffu, tripped) && (threadIdx.x & 31) == 0) {
+        atomicMin(&a.status->guard_tripped, a.step);
+    }
+}
+
+int integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks, int drift,
+                    double half_skin2, int32_t step, pg_status *status, cudaStream_t st) {
+    if(!box || !p || !p->pos || !p->vel || !p->mass || !p->force32 || !p->pos_hi || !p->pos_lo) {
+        return PG_ERR_ARGUMENT;
+    }
+    if(drift && (!p->pos_ref || !p->ref_hi || !p->ref_lo || !status)) { return PG_ERR_ARGUMENT; }
+    if(kicks < 1 || kicks > 2) { return PG_ERR_ARGUMENT; }
+    MixArgs a;
+    a.box = *box; a.p = *p; a.dt = dt; a.kick = kicks * (dt * 0.5); a.drift = drift;
+    a.half_skin2 = half_skin2;
+    a.half_skin2_lo = (float) (half_skin2 * (1.0 - 1e-3));
+    a.half_skin2_hi = (float) (half_skin2 * (1.0 + 1e-3));
+    a.step = step; a.status = status;
+    if(p->n > 0) { k_integrate_mixed<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch(); }
+    return launch_status();
 }
 
 static int launch_integrate(const pg_box *box, pg_particles *p, double dt, int precision,

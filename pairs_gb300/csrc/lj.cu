@@ -5,7 +5,9 @@
 //   rsq < rc^2:  sr2 = 1/rsq;  sr6 = sr2^3 sigma6[ti,tj];
 //                F_i += delta * 48 sr6 (sr6 - 1/2) sr2 epsilon[ti,tj]
 // with a full list (every pair seen from both sides, no atomics) or a half list
-// (each pair once, the reaction -f applied to the partner with an atomic add).
+// (each interior pair once, the reaction -f applied to the partner with an atomic
+// add; pairs through a periodic image are in both lists and get no reaction, as the
+// reference's ghost images).
 //
 // Two precisions:
 //   FP64   every operation in double; the cutoff test uses the reference's exact
@@ -99,12 +101,12 @@ __global__ void __launch_bounds__(kBlock) k_lj_fp64(ForceArgs a) {
                     // separately rounded, in the generated order (tmp = tmp + delta*f)
                     const double ex = __dmul_rn(dx, f), ey = __dmul_rn(dy, f), ez = __dmul_rn(dz, f);
                     fx = __dadd_rn(fx, ex); fy = __dadd_rn(fy, ey); fz = __dadd_rn(fz, ez);
-                    if(kHalf) {
+                    if(kHalf && code == 0u) {
                         double *fj = a.p.force + 4 * (size_t) j;
                         atomicAdd(fj + 0, -ex); atomicAdd(fj + 1, -ey); atomicAdd(fj + 2, -ez);
                     }
                     if(kEnergy) {
-                        const double w = kHalf ? 1.0 : 0.5;
+                        const double w = (kHalf && code == 0u) ? 1.0 : 0.5;
                         pe += w * 4.0 * a.lj.eps[tij] * (sr6 * sr6 - sr6);
                         vir += w * (dx * ex + dy * ey + dz * ez);
                     }
@@ -164,9 +166,9 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
                     const float sr6 = sr2 * sr2 * sr2 * a.lj.sig6f[tij];
                     const float f = 48.0f * sr6 * (sr6 - 0.5f) * sr2 * a.lj.epsf[tij];
                     fx += dx * f; fy += dy * f; fz += dz * f;
-                    if(kHalf) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
+                    if(kHalf && code == 0u) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
                     if(kEnergy) {
-                        const double w = kHalf ? 1.0 : 0.5;
+                        const double w = (kHalf && code == 0u) ? 1.0 : 0.5;
                         pe += w * 4.0 * (double) a.lj.epsf[tij] * ((double) sr6 * (double) sr6 - (double) sr6);
                         vir += w * (double) (rsq * f);
                     }

@@ -14,6 +14,10 @@
 // are first screened with compensated FP32 positions (relative error of rsq below
 // 1e-6); only candidates within a relative band of 1e-4 around r_list2 are decided
 // in FP64.
+//
+// Half lists follow the reference's compute_half() semantics: a pair inside the box
+// is stored once (Newton's third law applies the reaction); a pair through a periodic
+// image is stored in both particles' lists and each side computes its own force.
 #include "common.cuh"
 
 namespace pg {
@@ -43,6 +47,10 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
     if(i >= a.p.n) { return; }
     const D4 xi = ld_d4(a.p.pos, i);
     st_d4(a.p.pos_ref, i, xi);
+    if(a.p.ref_hi != nullptr) {
+        st_f4(a.p.ref_hi, i, ld_f4(a.p.pos_hi, i));
+        st_f4(a.p.ref_lo, i, ld_f4(a.p.pos_lo, i));
+    }
     int cnt = 0;
     const bool fixed = a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed);
     const int ci = a.cells.particle_cell[i];
@@ -69,7 +77,10 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
                     const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
                     for(int j = b; j < e; j++) {
                         if(j == i) { continue; }
-                        if(a.list.half && j < i) { continue; }
+                        // half list: an interior pair once (i < j); a pair through a
+                        // periodic image from both sides, as the reference's ghosts
+                        // always pass its i < j test (sim/interaction.py:107-113)
+                        if(a.list.half && code == 0u && j < i) { continue; }
                         const float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
                         const float fx = comp_delta(hi.x, lo.x, hj.x, lj.x, sx, a.box.len_hi[0], a.box.len_lo[0]);
                         const float fy = comp_delta(hi.y, lo.y, hj.y, lj.y, sy, a.box.len_hi[1], a.box.len_lo[1]);

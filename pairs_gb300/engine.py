@@ -55,7 +55,7 @@ class LJEngine:
         if policy not in ("fixed", "guard", "fixed+guard"):
             raise ValueError(f"unknown rebuild policy {policy!r}")
         self.policy = policy
-        self.fused = fused and self.sync == A.PG_SYNC_EXACT
+        self.fused = fused
         pos = np.asarray(state["pos"], dtype=np.float64)
         n = len(pos)
         box = np.asarray(state["box"], dtype=np.float64)
@@ -68,6 +68,7 @@ class LJEngine:
         self.r_list2 = self.r_list * self.r_list
         self.half_skin2 = (0.5 * skin) ** 2
         self.ts = 0
+        self._pending_final = False
         self.since_build = 0
         self.nbuilds = 0
         self.thermo_log = []
@@ -95,6 +96,8 @@ class LJEngine:
         t["pos_ref"] = z((cap, 4), f64)
         t["pos_hi"] = z((cap, 4), f32)
         t["pos_lo"] = z((cap, 4), f32)
+        t["ref_hi"] = z((cap, 4), f32)
+        t["ref_lo"] = z((cap, 4), f32)
         t["mass"] = z((cap,), f64)
         t["type"] = z((cap,), i32)
         t["uid"] = z((cap,), i32)
@@ -175,7 +178,7 @@ class LJEngine:
     def _bind_particles(self):
         t, p = self.t, self.p
         for name in ("pos", "pos_prev1", "pos_prev2", "vel", "force", "force32", "pos_hi", "pos_lo",
-                     "pos_ref", "mass", "type", "uid", "flags"):
+                     "pos_ref", "ref_hi", "ref_lo", "mass", "type", "uid", "flags"):
             setattr(p, name, t[name].data_ptr() if name in t else None)
 
     def _alloc_list(self, max_nb):
@@ -226,20 +229,34 @@ class LJEngine:
         A.call("pg_lj_force", C.byref(self.box), C.byref(self.p), C.byref(self.list), C.byref(self.lj),
                self.precision, self.sync, e, self.ws, self.sh)
 
-    def initial_integrate(self):
+    def advance(self, kicks):
+        """Initial half step of this time step, preceded by the deferred final half
+        step of the previous one when kicks == 2 (one fused pass)."""
+        by = C.byref
+        if self.precision == A.PG_MIXED:
+            A.call("pg_integrate_mixed", by(self.box), by(self.p), self.dt, kicks, 1, self.half_skin2,
+                   self.ts, self.status_ptr, self.sh)
+            return
         if self.sync == A.PG_SYNC_REFERENCE:
             self._rotate_ring()
-        A.call("pg_initial_integrate", C.byref(self.box), C.byref(self.p), self.dt, self.precision,
-               self.half_skin2, self.ts, self.sync, self.status_ptr, self.sh)
+        name = "pg_final_initial_integrate" if kicks == 2 else "pg_initial_integrate"
+        A.call(name, by(self.box), by(self.p), self.dt, self.precision, self.half_skin2, self.ts, self.sync,
+               self.status_ptr, self.sh)
 
-    def final_integrate(self):
-        A.call("pg_final_integrate", C.byref(self.box), C.byref(self.p), self.dt, self.precision, self.sh)
-
-    def final_initial_integrate(self):
-        A.call("pg_final_initial_integrate", C.byref(self.box), C.byref(self.p), self.dt, self.precision,
-               self.half_skin2, self.ts, self.sync, self.status_ptr, self.sh)
+    def flush(self):
+        """Apply a deferred final half step (velocities at full step)."""
+        if not self._pending_final:
+            return
+        self._pending_final = False
+        by = C.byref
+        if self.precision == A.PG_MIXED:
+            A.call("pg_integrate_mixed", by(self.box), by(self.p), self.dt, 1, 0, self.half_skin2, self.ts,
+                   self.status_ptr, self.sh)
+        else:
+            A.call("pg_final_integrate", by(self.box), by(self.p), self.dt, self.precision, self.sh)
 
     def compute_thermo(self):
+        self.flush()
         A.call("pg_compute_thermo", C.byref(self.box), C.byref(self.p), C.c_void_p(self.t["thermo"].data_ptr()),
                self.ws, self.sh)
         out = self.t["thermo"].cpu().numpy()
@@ -266,10 +283,12 @@ class LJEngine:
         return int(self.t["status"][4].item()) != INT32_MAX
 
     def step(self, thermo_every=0):
-        """One iteration of the reference's time loop."""
+        """One iteration of the reference's time loop.  The final half step of a time
+        step is deferred and fused with the next step's initial half step."""
         ts = self.ts
         if ts > 0:
-            self.initial_integrate()
+            self.advance(2 if self._pending_final else 1)
+            self._pending_final = False
         if self.needs_rebuild(ts):
             self.rebuild()
         else:
@@ -277,7 +296,9 @@ class LJEngine:
             self.list.steps_since_build = self.since_build
         self.force()
         if ts > 0:
-            self.final_integrate()
+            self._pending_final = True
+            if not self.fused:
+                self.flush()
         if thermo_every and (ts == 0 or (ts + 1) % thermo_every == 0):
             self.thermo_log.append((ts,) + self.compute_thermo())
         self.ts += 1
@@ -301,11 +322,13 @@ class LJEngine:
             if src is not None:
                 t[key][:n].copy_(src, non_blocking=True)
         self.ts = 0
+        self._pending_final = False
 
     # ------------------------------------------------------------------ readback
 
     def state(self):
         """Positions, velocities, forces as numpy arrays in uid order."""
+        self.flush()
         n = self.n
         uid = self.t["uid"][:n].cpu().numpy()
         order = np.argsort(uid, kind="stable")
@@ -316,6 +339,16 @@ class LJEngine:
         else:
             frc = self.t["force32"][:n, :3].cpu().numpy().astype(np.float64)[order]
         return pos, vel, frc
+
+    def _uid_order(self):
+        uid = self.t["uid"][: self.n].cpu().numpy()
+        return np.argsort(uid, kind="stable")
+
+    def masses(self):
+        return self.t["mass"][: self.n].cpu().numpy()[self._uid_order()]
+
+    def flags(self):
+        return self.t["flags"][: self.n].cpu().numpy()[self._uid_order()]
 
     def pairs(self):
         """Verlet entries as (uid_i, uid_j, sx, sy, sz) rows (list order per particle)."""
