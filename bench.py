@@ -132,13 +132,23 @@ def run_ours(args, rank, world, dist):
     n = len(st["mass"])
     lib = A.load()
 
-    def make(precision, half):
-        return LJEngine(st, precision=precision, half=half, sync="exact", every=20, policy="fixed",
+    def make(precision, half, policy):
+        return LJEngine(st, precision=precision, half=half, sync="exact", every=20, policy=policy,
                         device=str(dev))
 
+    def calibrate(eng):
+        """Train the learned schedule on the run's own first rebuild cycles (setup)."""
+        t0 = time.perf_counter()
+        k = 0
+        if eng.schedule is not None:
+            while not eng.schedule.trained and k < 2000:
+                eng.step()
+                k += 1
+        torch.cuda.synchronize()
+        return k, time.perf_counter() - t0
+
     def timed(eng, steps, warmup, force_events=True):
-        for _ in range(warmup):
-            eng.step()
+        eng.run(warmup)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -157,25 +167,27 @@ def run_ours(args, rank, world, dist):
         if force_events:
             eng.force = force_timed
         l0 = lib.pg_kernel_launches()
+        c0 = dict(builds=eng.nbuilds, syncs=eng.host_syncs, rewinds=eng.rewinds, skipped=eng.skipped_steps)
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record(stream)
-        for _ in range(steps):
-            eng.step()
+        eng.run(steps)
         s1.record(stream)
         torch.cuda.synchronize()
         launches = lib.pg_kernel_launches() - l0
         eng.force = orig_force
         ms = s0.elapsed_time(s1)
         fms = [a.elapsed_time(b) for a, b in ev]
-        return ms, fms, launches
+        counters = {"rebuilds": eng.nbuilds - c0["builds"], "host_syncs": eng.host_syncs - c0["syncs"],
+                    "rewinds": eng.rewinds - c0["rewinds"], "skipped_steps": eng.skipped_steps - c0["skipped"]}
+        return ms, fms, launches, counters
 
-    # headline: mixed precision, half list (Newton's third law), fixed reference schedule
     prec, half = {"mixed-half": ("mixed", True), "mixed-full": ("mixed", False),
                   "fp64-half": ("fp64", True), "fp64-full": ("fp64", False)}[args.variant]
-    eng = make(prec, half)
+    eng = make(prec, half, args.policy)
+    calib_steps, calib_s = calibrate(eng)
     clocks = ClockSampler(dev.index or 0)
     clocks.start()
-    ms, fms, launches = timed(eng, args.steps, args.warmup)
+    ms, fms, launches, counters = timed(eng, args.steps, args.warmup)
     clk = clocks.stop()
     if dist:
         t = torch.tensor([ms], device=dev)
@@ -193,56 +205,87 @@ def run_ours(args, rank, world, dist):
     achieved = b_force / (f_avg / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_kind": pk_kind,
-                "traffic": traffic_from_profiles("k_lj_mixed"), "kernel": "k_lj_%s" % args.variant,
+                "traffic": traffic_from_profiles("k_lj_" + prec), "kernel": "k_lj_%s" % args.variant,
                 "kernel_ms": round(f_avg, 4), "algorithmic_bytes": b_force, "list_entries": pairs_total}
-    nbuilds = eng.nbuilds
+    schedule = dict(counters, policy=args.policy, calibration_steps=calib_steps,
+                    calibration_s=round(calib_s, 3),
+                    mean_cycle=round(args.steps / max(1, counters["rebuilds"]), 2))
     if args.only_headline:
-        print(json.dumps({"variant": args.variant, "value": value, "ms_per_step": ms / args.steps,
-                          "roofline": roofline, "gpu_launches": launches, "clocks": clk}))
+        print(json.dumps({"variant": args.variant, "policy": args.policy, "value": value,
+                          "ms_per_step": ms / args.steps, "roofline": roofline, "schedule": schedule,
+                          "gpu_launches": launches, "clocks": clk}))
         return
 
-    # plain FP64 path on the same workload (full list and half list; best reported)
+    # energy drift of the headline method over --drift-steps (untimed): E = KE + PE
+    def drift(eng_d, steps, every=100):
+        e0 = None
+        worst = 0.0
+        for k in range(0, steps + 1, every):
+            if k:
+                eng_d.run(every)
+            t, _ = eng_d.compute_thermo()
+            ke = 0.5 * float(eng_d.t["thermo"][2].item())
+            pe, _ = eng_d.potential_energy()
+            e = ke + pe
+            e0 = e if e0 is None else e0
+            worst = max(worst, abs(e - e0) / abs(e0))
+        return worst
+
+    drift_headline = None
+    if args.drift_steps:
+        ed = make(prec, half, args.policy)
+        calibrate(ed)
+        drift_headline = drift(ed, args.drift_steps)
+        del ed
+
+    # plain FP64 path on the same workload: fixed every-20 schedule and exact guard
     fp64 = {}
-    for half in (False, True):
-        e64 = make("fp64", half)
-        k64 = max(10, args.steps // 10)
-        ms64, f64ms, _ = timed(e64, k64, min(args.warmup, 5))
-        fp64["half" if half else "full"] = {"value": n * k64 / (ms64 / 1e3), "steps": k64,
-                                            "force_ms": round(statistics.mean(f64ms), 4)}
+    k64 = max(10, args.steps // 10)
+    for half64, pol in ((True, "fixed"), (True, "guard"), (False, "fixed")):
+        e64 = make("fp64", half64, pol)
+        ms64, f64ms, _, c64 = timed(e64, k64, min(args.warmup, 5))
+        fp64[f"{'half' if half64 else 'full'}_{pol}"] = {
+            "value": n * k64 / (ms64 / 1e3), "steps": k64, "force_ms": round(statistics.mean(f64ms), 4),
+            "rebuilds": c64["rebuilds"]}
         del e64
     best64 = max(v["value"] for v in fp64.values())
+    drift64 = None
+    if args.drift_steps:
+        e64 = make("fp64", True, "guard")
+        drift64 = drift(e64, args.drift_steps)
+        del e64
 
     # end to end through the public engine API from pinned host state
-    e2e = None
-    if True:
-        chunk = min(100, args.steps)
-        nchunks = max(1, args.steps // chunk)
-        pad4 = lambda a: np.concatenate([a, np.zeros((len(a), 1))], axis=1)
-        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
-                (("pos", pad4(st["pos"])), ("vel", pad4(st["vel"])), ("mass", st["mass"]),
-                 ("type", st["type"]), ("uid", st["uid"]))}
-        out_pos = torch.empty((n, 4), dtype=torch.float64).pin_memory()
-        out_vel = torch.empty((n, 4), dtype=torch.float64).pin_memory()
-        ee = make("mixed", True)
-        ee.run(args.warmup)
-        torch.cuda.synchronize()
-        h2d = d2h = 0
-        t0 = time.perf_counter()
-        for _ in range(nchunks):
-            ee.upload(host["pos"], host["vel"], host["mass"], host["type"], host["uid"])
-            h2d += sum(v.numel() * v.element_size() for v in host.values())
-            ee.run(chunk)
-            out_pos.copy_(ee.t["pos"][:n], non_blocking=True)
-            out_vel.copy_(ee.t["vel"][:n], non_blocking=True)
-            thermo = ee.compute_thermo()
-            d2h += 2 * n * 32 + 24
-        torch.cuda.synchronize()
-        el = time.perf_counter() - t0
-        e2e = {"value": n * chunk * nchunks / el, "unit": UNIT, "h2d_bytes_per_step": h2d // (chunk * nchunks),
-               "d2h_bytes_per_step": d2h // (chunk * nchunks),
-               "definition": f"public engine API: per call upload full particle state from pinned host, "
-                             f"advance {chunk} MD steps, download positions+velocities and thermo"}
-        del ee
+    chunk = min(100, args.steps)
+    nchunks = max(1, args.steps // chunk)
+    pad4 = lambda a: np.concatenate([a, np.zeros((len(a), 1))], axis=1)
+    host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
+            (("pos", pad4(st["pos"])), ("vel", pad4(st["vel"])), ("mass", st["mass"]),
+             ("type", st["type"]), ("uid", st["uid"]))}
+    out_pos = torch.empty((n, 4), dtype=torch.float64).pin_memory()
+    out_vel = torch.empty((n, 4), dtype=torch.float64).pin_memory()
+    ee = make(prec, half, args.policy)
+    calibrate(ee)
+    ee.run(args.warmup)
+    torch.cuda.synchronize()
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+    for _ in range(nchunks):
+        ee.upload(host["pos"], host["vel"], host["mass"], host["type"], host["uid"])
+        h2d += sum(v.numel() * v.element_size() for v in host.values())
+        ee.run(chunk)
+        ee.flush()
+        out_pos.copy_(ee.t["pos"][:n], non_blocking=True)
+        out_vel.copy_(ee.t["vel"][:n], non_blocking=True)
+        ee.compute_thermo()
+        d2h += 2 * n * 32 + 24
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    e2e = {"value": n * chunk * nchunks / el, "unit": UNIT, "h2d_bytes_per_step": h2d // (chunk * nchunks),
+           "d2h_bytes_per_step": d2h // (chunk * nchunks),
+           "definition": f"public engine API: per call upload the full particle state from pinned host, "
+                         f"advance {chunk} MD steps, download positions+velocities and thermo"}
+    del ee
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -254,12 +297,13 @@ def run_ours(args, rank, world, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 force / f64 integrate",
         "data": "synthetic (fcc lattice, Park-Miller velocities as the reference)",
         "config": {"workload": f"LJ fcc {wl['n'][0]}x{wl['n'][1]}x{wl['n'][2]} = {n} atoms, rho 0.8442, T 1.44, "
-                               "rc 2.5, skin 0.3, dt 0.005, mixed precision, half list, rebuild every 20",
+                               f"rc 2.5, skin 0.3, dt 0.005, {args.variant}, rebuild policy {args.policy} "
+                               "(exact FP64 displacement guard)",
                    "atoms": n, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (Verlet list %.0f MB)" % (pairs_total * 4 / 1e6),
-                   "rebuilds_in_timed_region": nbuilds},
-        "roofline": roofline,
-        "fp64": {"best_value": best64, **fp64, "speedup_mixed_vs_fp64": value / world / best64},
+                   "l2": "inputs larger than L2 (Verlet list %.0f MB)" % (pairs_total * 4 / 1e6)},
+        "roofline": roofline, "schedule": schedule,
+        "energy_drift_1000": {"headline": drift_headline, "fp64_guard": drift64, "steps": args.drift_steps},
+        "fp64": {"best_value": best64, **fp64, "speedup_headline_vs_fp64": value / world / best64},
         "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
     }
     if rank == 0:
@@ -331,6 +375,8 @@ def main():
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--variant", choices=["mixed-half", "mixed-full", "fp64-half", "fp64-full"],
                     default="mixed-half")
+    ap.add_argument("--policy", default="learned", help="rebuild policy: learned | guard | fixed | interval:k")
+    ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline arm only (profiling runs)")
     args = ap.parse_args()

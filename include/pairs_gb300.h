@@ -101,6 +101,13 @@ typedef struct {
     int32_t *type;               /* [capacity] */
     int32_t *uid;                /* [capacity] user id (the reference's uid property) */
     int32_t *flags;              /* [capacity] reference flag bits: 1 infinite, 4 fixed */
+    /* Speculative stepping: when `guard` is not NULL it points at
+     * status->guard_tripped; a force pass of time step `step` does nothing once the
+     * guard tripped at a step <= `step`, an integration pass once it tripped at a
+     * step < `step`.  The host later rebuilds at the tripped step and resumes. */
+    const int32_t *guard;
+    int32_t step;
+    int32_t pad_;
 } pg_particles;
 
 /* Cell grid over the box, counting-sort layout (cell_start/cell_count). */
@@ -217,6 +224,36 @@ int pg_split_positions(const pg_box *box, pg_particles *p, void *stream);
  * the last binning permutation to caller-held per-particle arrays. */
 int pg_permute(int32_t n, const int32_t *perm, const void *src, void *dst, int elem_bytes,
                void *stream);
+
+/* ---- learned rebuild schedule (no counterpart in the reference, which rebuilds
+ * on a fixed period: sim/simulation.py:232-233, sim/timestep.py:47) ----------- */
+
+/* Number of FP32 parameters of the 3-64-64-1 network: W1[64][3] b1[64] W2[64][64]
+ * b2[64] W3[64] b3. */
+int pg_mlp_param_count(void);
+
+/* Per-cell features [ncells][4]: max|v|*dt/(skin/2), mean(|F|/m)*dt^2/(skin/2),
+ * steps_since_build/20, 1 if the cell holds particles else 0. */
+int pg_cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t steps_since_build,
+                     double dt, double half_skin, float *features, void *stream);
+
+/* out[c] = network output (log steps until the cell's first displacement > skin/2)
+ * for non-empty cells, +inf for empty ones. */
+int pg_mlp_forward(const float *params, const float *features, int32_t ncells, float *out, void *stream);
+
+/* result[0] = soft minimum of out (temperature T), result[1] = min (ordered int
+ * bits), result[2] = partition sum; result is device float[4]. */
+int pg_mlp_softmin(const float *out, int32_t ncells, float temperature, float *result, void *stream);
+
+/* Accumulate the gradient of (P - target_log)^2 (censored: min(P - target_log, 0)^2)
+ * into grads[param_count] and the loss into *loss (device). */
+int pg_mlp_backward(const float *params, const float *features, const float *out, int32_t ncells,
+                    const float *result, float target_log, int censored, float temperature, float *grads,
+                    float *loss, void *stream);
+
+/* One Adam step on params with grads * grad_scale; zeroes grads. t counts from 1. */
+int pg_mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float beta1, float beta2,
+                float eps, int32_t t, float grad_scale, void *stream);
 
 /* cudaStreamSynchronize, returning PG_OK or PG_ERR_CUDA. */
 int pg_stream_sync(void *stream);

@@ -43,7 +43,7 @@ class PgParticles(C.Structure):
                 ("pos_hi", C.c_void_p), ("pos_lo", C.c_void_p), ("pos_ref", C.c_void_p),
                 ("ref_hi", C.c_void_p), ("ref_lo", C.c_void_p),
                 ("mass", C.c_void_p), ("type", C.c_void_p), ("uid", C.c_void_p),
-                ("flags", C.c_void_p)]
+                ("flags", C.c_void_p), ("guard", C.c_void_p), ("step", C.c_int32), ("pad_", C.c_int32)]
 
 
 class PgCells(C.Structure):
@@ -91,6 +91,15 @@ SIGNATURES = {
     "pg_split_positions": (C.c_int, [P(PgBox), P(PgParticles), C.c_void_p]),
     "pg_permute": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "pg_stream_sync": (C.c_int, [C.c_void_p]),
+    "pg_mlp_param_count": (C.c_int, []),
+    "pg_cell_features": (C.c_int, [P(PgParticles), P(PgCells), C.c_int, C.c_int32, C.c_double, C.c_double,
+                                   C.c_void_p, C.c_void_p]),
+    "pg_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "pg_mlp_softmin": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.c_void_p]),
+    "pg_mlp_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_int,
+                                  C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pg_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_float,
+                              C.c_float, C.c_int32, C.c_float, C.c_void_p]),
 }
 
 _lib = None

@@ -22,6 +22,15 @@ int integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks, in
                     double half_skin2, int32_t step, pg_status *status, cudaStream_t st);
 int compute_thermo(const pg_box *box, const pg_particles *p, double *out, double *partials,
                    cudaStream_t st);
+int cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t since, double dt,
+                  double half_skin, float *feat, cudaStream_t st);
+int mlp_forward(const float *params, const float *feat, int32_t ncells, float *out, cudaStream_t st);
+int mlp_softmin(const float *out, int32_t ncells, float temperature, float *result, cudaStream_t st);
+int mlp_backward(const float *params, const float *feat, const float *out, int32_t ncells, const float *result,
+                 float target_log, int censored, float temperature, float *grads, float *loss, cudaStream_t st);
+int mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float b1, float b2, float eps,
+             int32_t t, float scale, cudaStream_t st);
+int mlp_param_count();
 }  // namespace pg
 
 unsigned long long pg::g_kernel_launches = 0;
@@ -105,6 +114,33 @@ int pg_permute(int32_t n, const int32_t *perm, const void *src, void *dst, int e
     if(n < 0 || (n > 0 && (!perm || !src || !dst)) || src == dst) { return PG_ERR_ARGUMENT; }
     if(n == 0) { return PG_OK; }
     return pg::gather_array(n, perm, src, dst, elem_bytes, S(stream));
+}
+
+int pg_mlp_param_count(void) { return pg::mlp_param_count(); }
+
+int pg_cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t steps_since_build,
+                     double dt, double half_skin, float *features, void *stream) {
+    return pg::cell_features(p, cells, precision, steps_since_build, dt, half_skin, features, S(stream));
+}
+
+int pg_mlp_forward(const float *params, const float *features, int32_t ncells, float *out, void *stream) {
+    return pg::mlp_forward(params, features, ncells, out, S(stream));
+}
+
+int pg_mlp_softmin(const float *out, int32_t ncells, float temperature, float *result, void *stream) {
+    return pg::mlp_softmin(out, ncells, temperature, result, S(stream));
+}
+
+int pg_mlp_backward(const float *params, const float *features, const float *out, int32_t ncells,
+                    const float *result, float target_log, int censored, float temperature, float *grads,
+                    float *loss, void *stream) {
+    return pg::mlp_backward(params, features, out, ncells, result, target_log, censored, temperature, grads,
+                            loss, S(stream));
+}
+
+int pg_mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float beta1, float beta2,
+                float eps, int32_t t, float grad_scale, void *stream) {
+    return pg::mlp_adam(params, grads, m1, m2, lr, beta1, beta2, eps, t, grad_scale, S(stream));
 }
 
 int pg_stream_sync(void *stream) {

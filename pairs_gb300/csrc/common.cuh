@@ -98,6 +98,17 @@ __device__ __forceinline__ void split_pos(double x, double inv_q, double q, floa
     lo = (float) (x - h);
 }
 
+// Speculative stepping (see pg_particles.guard): a force pass of step p.step is
+// skipped once the guard tripped at a step <= p.step, an integration pass once it
+// tripped before p.step.  Every thread reads the same word (one broadcast load).
+__device__ __forceinline__ bool frozen_force(const pg_particles &p) {
+    return p.guard != nullptr && *((volatile const int32_t *) p.guard) <= p.step;
+}
+
+__device__ __forceinline__ bool frozen_integrate(const pg_particles &p) {
+    return p.guard != nullptr && *((volatile const int32_t *) p.guard) < p.step;
+}
+
 // warp/block reductions
 __device__ __forceinline__ double warp_sum(double v) {
     for(int o = 16; o > 0; o >>= 1) { v += __shfl_xor_sync(0xffffffffu, v, o); }

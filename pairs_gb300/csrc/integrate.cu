@@ -43,6 +43,7 @@ __device__ __forceinline__ double kick(double v, double h, double f, double m) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
+    if(a.do_initial ? frozen_integrate(a.p) : frozen_force(a.p)) { return; }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool tripped = false;
     if(i < a.p.n && !(a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed))) {
@@ -116,6 +117,7 @@ __device__ __forceinline__ void resplit(double x, float q, float iq, float &hi, 
 }
 
 __global__ void __launch_bounds__(kBlock) k_integrate_mixed(MixArgs a) {
+    if(a.drift ? frozen_integrate(a.p) : frozen_force(a.p)) { return; }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool tripped = false;
     if(i < a.p.n && !(a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed))) {

@@ -63,6 +63,7 @@ __device__ __forceinline__ void block_add_energy(double pe, double vir, double *
 
 template<bool kHalf, bool kOneType, bool kEnergy>
 __global__ void __launch_bounds__(kBlock) k_lj_fp64(ForceArgs a) {
+    if(frozen_force(a.p)) { return; }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double pe = 0.0, vir = 0.0;
     if(i < a.p.n) {
@@ -133,6 +134,7 @@ __device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float 
 
 template<bool kHalf, bool kOneType, bool kEnergy>
 __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
+    if(frozen_force(a.p)) { return; }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double pe = 0.0, vir = 0.0;
     if(i < a.p.n) {
@@ -186,6 +188,15 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
 
 using KernelFn = void (*)(ForceArgs);
 
+// zero the force array before a half-list pass (skipped like the pass when frozen)
+__global__ void k_zero_force(pg_particles p, int fp64) {
+    if(frozen_force(p)) { return; }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= p.n) { return; }
+    if(fp64) { st_d4(p.force, i, make_d4(0.0, 0.0, 0.0, 0.0)); }
+    else { st_f4(p.force32, i, make_float4(0.0f, 0.0f, 0.0f, 0.0f)); }
+}
+
 static KernelFn pick_fp64(bool half, bool one, bool en) {
     if(half) {
         if(one) { return en ? k_lj_fp64<true, true, true> : k_lj_fp64<true, true, false>; }
@@ -228,9 +239,8 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *l
     }
     const bool half = list->half != 0, one = lj->ntypes == 1, en = energy != nullptr;
     if(en) { cudaMemsetAsync(energy, 0, 2 * sizeof(double), st); }
-    if(half) {
-        if(precision == PG_FP64) { cudaMemsetAsync(p->force, 0, (size_t) p->n * 32, st); }
-        else { cudaMemsetAsync(p->force32, 0, (size_t) p->n * 16, st); }
+    if(half && p->n > 0) {
+        k_zero_force<<<blocks_for(p->n), kBlock, 0, st>>>(*p, precision == PG_FP64); note_launch();
     }
     if(p->n == 0) { return launch_status(); }
     KernelFn k = precision == PG_FP64 ? pick_fp64(half, one, en) : pick_mixed(half, one, en);

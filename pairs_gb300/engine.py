@@ -52,8 +52,10 @@ class LJEngine:
         self.sync = {"exact": A.PG_SYNC_EXACT, "reference": A.PG_SYNC_REFERENCE}[sync]
         if self.sync == A.PG_SYNC_REFERENCE and self.precision != A.PG_FP64:
             raise ValueError("reference image sync is defined for the FP64 path only")
-        if policy not in ("fixed", "guard", "fixed+guard"):
+        if policy not in ("fixed", "guard", "fixed+guard", "learned") and not str(policy).startswith("interval:"):
             raise ValueError(f"unknown rebuild policy {policy!r}")
+        if (policy == "learned" or str(policy).startswith("interval:")) and sync == "reference":
+            raise ValueError("speculative rebuild policies need exact image sync")
         self.policy = policy
         self.fused = fused
         pos = np.asarray(state["pos"], dtype=np.float64)
@@ -71,7 +73,13 @@ class LJEngine:
         self._pending_final = False
         self.since_build = 0
         self.nbuilds = 0
+        self.host_syncs = 0
+        self.rewinds = 0
+        self.skipped_steps = 0
         self.thermo_log = []
+        self.schedule = None
+        self.next_rebuild = 0
+        self._cycle_start = 0
 
         # ---- box
         self.box = A.PgBox()
@@ -172,6 +180,15 @@ class LJEngine:
         self.stream = torch.cuda.current_stream(self.dev)
         self.sh = C.c_void_p(self.stream.cuda_stream)
         A.call("pg_split_positions", C.byref(self.box), C.byref(self.p), self.sh)
+        if self.speculative:
+            self.p.guard = t["status"].data_ptr() + 4 * 4         # &status->guard_tripped
+        if policy == "learned":
+            from .schedule import LearnedSchedule
+            self.schedule = LearnedSchedule(self)
+
+    @property
+    def speculative(self):
+        return self.policy == "learned" or str(self.policy).startswith("interval:")
 
     # ------------------------------------------------------------------ buffers
 
@@ -194,6 +211,7 @@ class LJEngine:
         self._bind_particles()
 
     def read_status(self):
+        self.host_syncs += 1
         s = self.t["status"].cpu().numpy()
         return A.PgStatus.from_buffer_copy(s.tobytes())
 
@@ -203,15 +221,18 @@ class LJEngine:
     # ------------------------------------------------------------------ modules
 
     def rebuild(self):
-        """Bin + sort + Verlet build, growing the list until it fits."""
+        """Bin + sort + Verlet build, growing the list until it fits.  Returns the
+        step at which the guard had tripped before this build (INT32_MAX if none)."""
         by = C.byref
         A.call("pg_bin_particles", by(self.box), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
+        guard = None
         while True:
             self.t["status"][0] = 0                     # overflow bits
             self.t["status"][2] = 0                     # max_neighbors
             A.call("pg_build_neighbor_lists", by(self.box), by(self.p), by(self.cells), by(self.list),
                    self.r_list2, self.status_ptr, self.sh)
             st = self.read_status()
+            guard = st.guard_tripped if guard is None else guard
             if st.nonfinite:
                 raise A.PairsError("non-finite particle position met while binning")
             if st.overflow & 2:
@@ -222,7 +243,7 @@ class LJEngine:
         self.since_build = 0
         self.nbuilds += 1
         self.t["status"][4] = INT32_MAX                 # guard reset
-        self._guard_armed = False
+        return guard
 
     def force(self, energy=False):
         e = C.c_void_p(self.t["energy"].data_ptr()) if energy else None
@@ -248,6 +269,7 @@ class LJEngine:
         if not self._pending_final:
             return
         self._pending_final = False
+        self.p.step = max(self.ts - 1, 0)
         by = C.byref
         if self.precision == A.PG_MIXED:
             A.call("pg_integrate_mixed", by(self.box), by(self.p), self.dt, 1, 0, self.half_skin2, self.ts,
@@ -256,6 +278,7 @@ class LJEngine:
             A.call("pg_final_integrate", by(self.box), by(self.p), self.dt, self.precision, self.sh)
 
     def compute_thermo(self):
+        self.settle()
         self.flush()
         A.call("pg_compute_thermo", C.byref(self.box), C.byref(self.p), C.c_void_p(self.t["thermo"].data_ptr()),
                self.ws, self.sh)
@@ -264,33 +287,111 @@ class LJEngine:
 
     def potential_energy(self):
         """(PE, virial sum r.F) of the current positions (FP64 sums)."""
+        self.settle()
+        if self.nbuilds == 0:
+            self.rebuild()
+        self.p.step = self.ts - 1 if self.ts > 0 else 0
         self.force(energy=True)
         e = self.t["energy"].cpu().numpy()
         return float(e[0]), float(e[1])
 
     # ------------------------------------------------------------------ schedule
 
+    def guard_step(self):
+        """Step at which the guard tripped since the last build (INT32_MAX if none)."""
+        self.host_syncs += 1
+        return int(self.t["status"][4].item())
+
+    def guard_tripped(self):
+        return self.guard_step() != INT32_MAX
+
     def needs_rebuild(self, ts):
         fixed = ((ts + 1) % self.every == 0) or ts == 0
         if self.policy == "fixed":
             return fixed
-        guard = self.guard_tripped()
         if self.policy == "guard":
-            return ts == 0 or guard
-        return fixed or guard
+            return ts == 0 or self.guard_tripped()
+        return fixed or self.guard_tripped()
 
-    def guard_tripped(self):
-        return int(self.t["status"][4].item()) != INT32_MAX
+    def _rewind(self, s):
+        """The guard tripped at step s < ts: every pass after advance(s) was skipped on
+        the device; continue from step s (positions x(s), forces still to compute)."""
+        self.skipped_steps += self.ts - s
+        self.rewinds += 1
+        self.ts = s
+        self._pending_final = False
+        self.thermo_log = [e for e in self.thermo_log if e[0] < s]
+
+    def _speculative_rebuild_point(self, ts):
+        """Rebuild point of the learned / interval policies at step ts (after the
+        advance of ts).  The list is rebuilt from the current positions; if the
+        guard had tripped at s < ts, the device froze at step s, so those positions
+        are x(s) and the build is the one step s needed: rewind to s."""
+        if ts != 0 and ts != self.next_rebuild:
+            return False
+        s = self.rebuild()
+        tripped_at = None
+        if ts > 0 and s <= ts:
+            tripped_at = s
+            if s < ts:
+                self._rewind(s)
+        self._cycle_start = self.ts
+        self._after_rebuild_schedule(self.ts, tripped_at)
+        return True
+
+    def _after_rebuild_schedule(self, ts, tripped_at):
+        """Close the finished cycle and choose the next rebuild step."""
+        sch = self.schedule
+        if self.policy.startswith("interval:"):
+            self.next_rebuild = ts + max(1, int(self.policy.split(":")[1]))
+            return
+        if ts > 0:
+            sch.close_cycle(tripped_at, ts + 1 if tripped_at is None else None)
+        if not sch.trained:
+            # warm-up: exact guard every step, samples along the cycle
+            sch.record(ts)
+            if sch.cycles >= sch.warmup_cycles:
+                sch.train()
+        if sch.trained:
+            r, slot = sch.predicted_steps()
+            sch.pending.append((slot, ts))
+            sch.history.append((ts, r))
+            self.next_rebuild = ts + max(1, int(math.floor(r * sch.margin)))
 
     def step(self, thermo_every=0):
         """One iteration of the reference's time loop.  The final half step of a time
         step is deferred and fused with the next step's initial half step."""
         ts = self.ts
+        self.p.step = ts
         if ts > 0:
             self.advance(2 if self._pending_final else 1)
             self._pending_final = False
-        if self.needs_rebuild(ts):
+        if self.speculative and (self.schedule is None or self.schedule.trained):
+            self._post_advance(False, None, thermo_every, built=self._speculative_rebuild_point(ts))
+            return
+        elif self.speculative:
+            # learned policy warm-up: exact guard read every step
+            g = ts == 0 or self.guard_tripped()
+            rebuild, tripped_at = g, (ts if g and ts > 0 else None)
+            if not rebuild and self.schedule.pending and \
+                    (ts - self._cycle_start) % 2 == 0 and len(self.schedule.pending) < self.schedule.samples_per_cycle:
+                self.schedule.record(ts)
+        else:
+            rebuild, tripped_at = self.needs_rebuild(ts), None
+        self._post_advance(rebuild, tripped_at, thermo_every)
+
+    def _post_advance(self, rebuild, tripped_at, thermo_every=0, built=False):
+        """Second half of a time step (after the integration pass): rebuild if asked,
+        force, defer the final half step, thermo."""
+        ts = self.ts
+        self.p.step = ts
+        if built:
+            pass
+        elif rebuild:
             self.rebuild()
+            self._cycle_start = ts
+            if self.speculative:
+                self._after_rebuild_schedule(ts, tripped_at)
         else:
             self.since_build += 1
             self.list.steps_since_build = self.since_build
@@ -303,8 +404,27 @@ class LJEngine:
             self.thermo_log.append((ts,) + self.compute_thermo())
         self.ts += 1
 
+    def settle(self):
+        """Speculative policies: make sure no guard trip is pending, so the state is
+        the exact one at the current step (redo steps from a trip if needed)."""
+        if not self.speculative or self.ts == 0:
+            return
+        target = self.ts
+        for _ in range(10000):
+            s = self.guard_step()
+            if s >= target:
+                return
+            self._rewind(s)
+            self._post_advance(True, s)
+            while self.ts < target:
+                self.step()
+        raise A.PairsError("settle(): guard kept tripping")
+
     def run(self, nsteps, thermo_every=0):
-        for _ in range(nsteps):
+        """Advance until nsteps more time steps are done (a speculative policy may
+        step back to a guard trip and redo steps)."""
+        target = self.ts + nsteps
+        while self.ts < target:
             self.step(thermo_every)
 
     def upload(self, pos, vel, mass=None, type=None, uid=None):
@@ -328,6 +448,7 @@ class LJEngine:
 
     def state(self):
         """Positions, velocities, forces as numpy arrays in uid order."""
+        self.settle()
         self.flush()
         n = self.n
         uid = self.t["uid"][:n].cpu().numpy()

@@ -1,0 +1,154 @@
+"""Learned neighbour-list rebuild schedule, trained on the run's own guard trips.
+
+Policy "learned" of LJEngine.  The exact FP64 displacement guard (a particle moved
+more than skin/2 since the last list build, evaluated every step inside the
+integration kernel) remains the judge of list validity.  What the network decides is
+when the host rebuilds and synchronises:
+
+* Warm-up: the host reads the guard after every step and rebuilds exactly at each
+  trip (policy "guard").  At several points of each rebuild cycle the per-cell
+  features are stored; when the cycle's trip step s is seen, each stored sample
+  (features at step t) gets the label R = s - t (steps that remained).
+* Training: Adam on the stored samples, all on the GPU through the library's own
+  forward / soft-minimum / backward / Adam kernels.
+* Inference: right after every rebuild the network predicts R for the new cycle;
+  the host enqueues steps up to the predicted trip without reading anything back,
+  then rebuilds proactively.  If the guard tripped earlier, every force and
+  integration pass after the trip did nothing (pg_particles.guard), so the host
+  rewinds to the trip step, rebuilds there and continues: a misprediction costs
+  skipped launches, never a wrong force.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _capi as A
+
+
+class LearnedSchedule:
+    def __init__(self, engine, warmup_cycles=6, samples_per_cycle=4, margin=1.3, temperature=0.05, lr=3e-3,
+                 train_steps=300, seed=0, max_samples=64, top_cells=256, online_every=16, online_steps=2):
+        self.e = engine
+        lib = A.load()
+        self.np = lib.pg_mlp_param_count()
+        self.ncells_all = engine.cells.ncells
+        self.ncells = min(top_cells, self.ncells_all)       # cells per sample: the fastest ones
+        self.online_every = online_every
+        self.online_steps = online_steps
+        self.warmup_cycles = warmup_cycles
+        self.samples_per_cycle = samples_per_cycle
+        self.margin = margin
+        self.temperature = temperature
+        self.lr = lr
+        self.train_steps = train_steps
+        self.max_samples = max_samples
+        dev = engine.dev
+        g = torch.Generator().manual_seed(seed)
+        p = torch.zeros(self.np, dtype=torch.float32)
+        # Xavier-style init; the output bias starts at log(10 steps)
+        H, IN = 64, 3
+        p[0:H * IN] = torch.randn(H * IN, generator=g) * math.sqrt(1.0 / IN)
+        p[H * IN + H: H * IN + H + H * H] = torch.randn(H * H, generator=g) * math.sqrt(1.0 / H)
+        o3 = H * IN + H + H * H + H
+        p[o3:o3 + H] = torch.randn(H, generator=g) * math.sqrt(1.0 / H) * 0.1
+        p[-1] = math.log(10.0)
+        self.params = p.to(dev)
+        self.grads = torch.zeros(self.np, dtype=torch.float32, device=dev)
+        self.m1 = torch.zeros_like(self.grads)
+        self.m2 = torch.zeros_like(self.grads)
+        self.adam_t = 0
+        self.out = torch.zeros(self.ncells, dtype=torch.float32, device=dev)
+        self.result = torch.zeros(4, dtype=torch.float32, device=dev)
+        self.loss = torch.zeros(1, dtype=torch.float32, device=dev)
+        self.feat = torch.zeros((max_samples, self.ncells, 4), dtype=torch.float32, device=dev)
+        self.feat_all = torch.zeros((self.ncells_all, 4), dtype=torch.float32, device=dev)
+        self.labels = []                  # (slot, log R, censored)
+        self.pending = []                 # (slot, step) samples of the open cycle
+        self.cycles = 0
+        self.trained = False
+        self.history = []                 # (cycle start, predicted R, observed R or None)
+        self.train_log = []
+
+    def _ptr(self, t):
+        return C.c_void_p(t.data_ptr())
+
+    # ---------------------------------------------------------------- features / prediction
+    def features_into(self, slot):
+        """Per-cell features of the current state; the sample keeps the `ncells`
+        cells with the fastest particle (the soft minimum is decided there)."""
+        e = self.e
+        A.call("pg_cell_features", C.byref(e.p), C.byref(e.cells), e.precision, e.since_build, e.dt,
+               0.5 * e.skin, self._ptr(self.feat_all), e.sh)
+        if self.ncells == self.ncells_all:
+            self.feat[slot].copy_(self.feat_all)
+        else:
+            idx = torch.topk(self.feat_all[:, 0], self.ncells, sorted=False).indices
+            torch.index_select(self.feat_all, 0, idx, out=self.feat[slot])
+
+    def predict_log(self, slot):
+        """Soft-min prediction for the features in `slot` (device scalar in result[0])."""
+        e = self.e
+        A.call("pg_mlp_forward", self._ptr(self.params), self._ptr(self.feat[slot]), self.ncells,
+               self._ptr(self.out), e.sh)
+        A.call("pg_mlp_softmin", self._ptr(self.out), self.ncells, self.temperature, self._ptr(self.result), e.sh)
+
+    def _slot(self):
+        used = {s for s, _, _ in self.labels} | {s for s, _ in self.pending}
+        for k in range(self.max_samples):
+            if k not in used:
+                return k
+        # overwrite the oldest labelled sample
+        s = self.labels.pop(0)[0]
+        return s
+
+    # ---------------------------------------------------------------- cycle bookkeeping
+    def record(self, step):
+        """Store the features of the current state as a sample of the open cycle."""
+        slot = self._slot()
+        self.features_into(slot)
+        self.pending.append((slot, step))
+
+    def close_cycle(self, trip_step, end_step):
+        """Label the open cycle: tripped at trip_step (exact), or censored at end_step."""
+        for slot, step in self.pending:
+            if trip_step is not None:
+                r = max(trip_step - step, 1)
+                self.labels.append((slot, math.log(r), 0))
+            else:
+                r = max(end_step - step, 1)
+                self.labels.append((slot, math.log(r), 1))
+        self.pending = []
+        self.cycles += 1
+        if self.trained and self.online_every and self.cycles % self.online_every == 0:
+            self.train(self.online_steps)
+
+    # ---------------------------------------------------------------- training
+    def train(self, steps=None):
+        e = self.e
+        steps = self.train_steps if steps is None else steps
+        if not self.labels:
+            return None
+        ns = len(self.labels)
+        for _ in range(steps):
+            self.loss.zero_()
+            for slot, target, cens in self.labels:
+                self.predict_log(slot)
+                A.call("pg_mlp_backward", self._ptr(self.params), self._ptr(self.feat[slot]), self._ptr(self.out),
+                       self.ncells, self._ptr(self.result), float(target), int(cens), self.temperature,
+                       self._ptr(self.grads), self._ptr(self.loss), e.sh)
+            self.adam_t += 1
+            A.call("pg_mlp_adam", self._ptr(self.params), self._ptr(self.grads), self._ptr(self.m1),
+                   self._ptr(self.m2), self.lr, 0.9, 0.999, 1e-8, self.adam_t, 1.0 / ns, e.sh)
+        final = float(self.loss.item()) / ns
+        self.train_log.append(final)
+        self.trained = True
+        return final
+
+    def predicted_steps(self):
+        """Predict R for the current state (features at since_build) -> float steps."""
+        slot = self._slot()
+        self.features_into(slot)
+        self.predict_log(slot)
+        return math.exp(float(self.result[0].item())), slot

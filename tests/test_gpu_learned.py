@@ -1,0 +1,125 @@
+"""Learned rebuild schedule: kernels vs the FP64 oracle, training, safety, gain."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp_oracle as mo
+from pairs_gb300 import _capi as A
+from pairs_gb300 import lattice
+
+pytestmark = pytest.mark.gpu
+
+
+def _random_problem(ncells=48, seed=1):
+    rng = np.random.default_rng(seed)
+    p = rng.normal(0, 0.3, mo.NPARAMS).astype(np.float32)
+    feat = np.zeros((ncells, 4), dtype=np.float32)
+    feat[:, 0] = rng.uniform(0.02, 0.3, ncells)
+    feat[:, 1] = rng.uniform(0.0, 0.05, ncells)
+    feat[:, 2] = rng.integers(0, 10, ncells) / 20.0
+    feat[:, 3] = 1.0
+    feat[5, 3] = 0.0                                   # one empty cell
+    return p, feat
+
+
+def _gpu(p, feat, target, cens, temp):
+    dev = torch.device("cuda")
+    tp = torch.from_numpy(p).to(dev)
+    tf = torch.from_numpy(feat).to(dev)
+    out = torch.zeros(len(feat), dtype=torch.float32, device=dev)
+    res = torch.zeros(4, dtype=torch.float32, device=dev)
+    grads = torch.zeros(mo.NPARAMS, dtype=torch.float32, device=dev)
+    loss = torch.zeros(1, dtype=torch.float32, device=dev)
+    sh = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    A.call("pg_mlp_forward", ptr(tp), ptr(tf), len(feat), ptr(out), sh)
+    A.call("pg_mlp_softmin", ptr(out), len(feat), temp, ptr(res), sh)
+    A.call("pg_mlp_backward", ptr(tp), ptr(tf), ptr(out), len(feat), ptr(res), target, cens, temp, ptr(grads),
+           ptr(loss), sh)
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), float(res[0]), grads.cpu().numpy(), float(loss[0])
+
+
+def test_forward_and_softmin_match_oracle():
+    p, feat = _random_problem()
+    out, P, _, _ = _gpu(p, feat, 2.0, 0, 0.05)
+    o, _ = mo.forward(p, feat)
+    valid = np.isfinite(o)
+    assert np.isinf(out[5]) and not valid[5]
+    assert np.allclose(out[valid], o[valid], rtol=1e-5, atol=1e-5)
+    assert abs(P - mo.softmin(o, 0.05)) < 1e-4
+
+
+@pytest.mark.parametrize("cens,target", [(0, 2.0), (0, 0.5), (1, 3.0)])
+def test_gradient_matches_oracle(cens, target):
+    p, feat = _random_problem(seed=3)
+    _, P, g, L = _gpu(p, feat, target, cens, 0.05)
+    Lo, go, Po = mo.loss_and_grad(p, feat, target, cens, 0.05)
+    assert abs(L - Lo) <= 1e-4 * max(1.0, Lo)
+    scale = np.abs(go).max()
+    assert scale > 0
+    assert np.abs(g - go).max() <= 2e-3 * scale
+
+
+def test_gradient_oracle_matches_finite_differences():
+    """Pin the oracle's analytic gradient itself (central differences, FP64)."""
+    p, feat = _random_problem(ncells=12, seed=5)
+    p = p.astype(np.float64)
+    L0, g, _ = mo.loss_and_grad(p, feat, 1.5, 0, 0.05)
+    rng = np.random.default_rng(0)
+    for k in rng.choice(mo.NPARAMS, 25, replace=False):
+        h = 1e-6
+        pp, pm = p.copy(), p.copy()
+        pp[k] += h; pm[k] -= h
+        fd = (mo.loss_and_grad(pp, feat, 1.5, 0, 0.05)[0] - mo.loss_and_grad(pm, feat, 1.5, 0, 0.05)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(g[k]))
+
+
+def _max_disp(eng):
+    n = eng.n
+    x = eng.t["pos"][:n, :3].cpu().numpy()
+    r = eng.t["pos_ref"][:n, :3].cpu().numpy()
+    return np.sqrt(((x - r) ** 2).sum(axis=1).max())
+
+
+def test_learned_schedule_never_computes_forces_on_a_stale_list():
+    from pairs_gb300.engine import LJEngine, INT32_MAX
+    st = lattice.copper_fcc_lattice(12, 12, 12)
+    eng = LJEngine(st, precision="mixed", sync="exact", policy="learned")
+    half = 0.5 * eng.skin
+    checked = 0
+    while eng.ts < 260:
+        ts = eng.ts
+        eng.step()
+        s = int(eng.t["status"][4].item())
+        if s == INT32_MAX or s > ts:
+            # the force of step ts was computed: every particle within skin/2
+            assert _max_disp(eng) <= half + 1e-12, ts
+            checked += 1
+    assert eng.schedule.trained
+    assert checked > 200
+
+
+def test_learned_schedule_gain_over_guard_every_step():
+    from pairs_gb300.engine import LJEngine
+    st = lattice.copper_fcc_lattice(16, 16, 16)
+    runs = {}
+    for policy in ("guard", "learned"):
+        eng = LJEngine(st, precision="mixed", sync="exact", policy=policy)
+        eng.run(80)                        # warm-up (and training for "learned")
+        s0, b0 = eng.host_syncs, eng.nbuilds
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        eng.run(300)
+        ev1.record()
+        torch.cuda.synchronize()
+        runs[policy] = dict(syncs=eng.host_syncs - s0, builds=eng.nbuilds - b0, ms=ev0.elapsed_time(ev1),
+                            rewinds=eng.rewinds)
+    g, l = runs["guard"], runs["learned"]
+    # one host round trip per cycle instead of one per step
+    assert l["syncs"] * 3 < g["syncs"], runs
+    # rebuilds: never many more than the exact-on-trip count
+    assert l["builds"] <= 1.6 * g["builds"], runs
