@@ -136,6 +136,19 @@ def run_ours(args, rank, world, dist):
         return LJEngine(st, precision=precision, half=half, sync="exact", every=20, policy=policy,
                         device=str(dev))
 
+    def kernel_times(eng, k):
+        stream = eng.stream
+        eng.p.step = max(eng.ts - 1, 0)
+        out = []
+        for _ in range(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.force()
+            b.record(stream)
+            out.append((a, b))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in out[2:]]
+
     def calibrate(eng):
         """Train the learned schedule on the run's own first rebuild cycles (setup)."""
         t0 = time.perf_counter()
@@ -187,13 +200,18 @@ def run_ours(args, rank, world, dist):
     calib_steps, calib_s = calibrate(eng)
     clocks = ClockSampler(dev.index or 0)
     clocks.start()
-    ms, fms, launches, counters = timed(eng, args.steps, args.warmup)
+    ms, _, launches, counters = timed(eng, args.steps, args.warmup, force_events=False)
     clk = clocks.stop()
     if dist:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = n * args.steps * world / (ms / 1e3)
+    # force-kernel time for the roofline: a speculative policy issues passes that the
+    # device skips after a guard trip, so time the kernel on its own on the settled
+    # state (same stream, CUDA events around each launch)
+    eng.settle()
+    fms = kernel_times(eng, 20)
     pairs_total = int(eng.t["count"][:n].sum().item())
     # algorithmic bytes of one force launch: own position (32: FP32 hi+lo, or FP64
     # x,y,z,pad), neighbour count (4), force write (16 FP32 / 32 FP64), 4 bytes per
@@ -216,8 +234,10 @@ def run_ours(args, rank, world, dist):
                           "gpu_launches": launches, "clocks": clk}))
         return
 
-    # energy drift of the headline method over --drift-steps (untimed): E = KE + PE
+    # energy drift over --drift-steps (untimed): E = KE + PE, sampled every 100 steps,
+    # both methods started from the same state after 100 equilibration steps
     def drift(eng_d, steps, every=100):
+        eng_d.run(max(0, 100 - eng_d.ts))
         e0 = None
         worst = 0.0
         for k in range(0, steps + 1, every):
@@ -243,7 +263,8 @@ def run_ours(args, rank, world, dist):
     k64 = max(10, args.steps // 10)
     for half64, pol in ((True, "fixed"), (True, "guard"), (False, "fixed")):
         e64 = make("fp64", half64, pol)
-        ms64, f64ms, _, c64 = timed(e64, k64, min(args.warmup, 5))
+        ms64, _, _, c64 = timed(e64, k64, min(args.warmup, 5), force_events=False)
+        f64ms = kernel_times(e64, 6)
         fp64[f"{'half' if half64 else 'full'}_{pol}"] = {
             "value": n * k64 / (ms64 / 1e3), "steps": k64, "force_ms": round(statistics.mean(f64ms), 4),
             "rebuilds": c64["rebuilds"]}

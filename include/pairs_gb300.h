@@ -61,14 +61,16 @@ extern "C" {
 
 /* Device-side status, written by kernels (mirrors the reference's resizes[]). */
 typedef struct {
-    int32_t overflow;            /* bit 0 cells, bit 1 neighbours, bit 2 contacts */
+    int32_t overflow;            /* bit 0 cells, bit 1 neighbours, bit 2 tile
+                                    neighbourhood, bit 3 contacts */
     int32_t max_cell_count;      /* largest cell occupancy seen */
     int32_t max_neighbors;       /* largest per-particle Verlet count seen */
     int32_t nonfinite;           /* set when a non-finite value was met */
     int32_t guard_tripped;       /* first step at which a displacement > skin/2 was seen;
                                     INT32_MAX while none was */
     int32_t max_contacts;        /* DEM contact-history slots needed */
-    int32_t pad[2];
+    int32_t max_tile_staged;     /* largest tile neighbourhood seen (overflow bit 2) */
+    int32_t pad;
 } pg_status;
 
 /* Periodic (or walled) orthorhombic box, sim/domain_partitioning.py:46-57. */
@@ -120,14 +122,22 @@ typedef struct {
     int32_t *particle_cell;      /* [capacity] */
 } pg_cells;
 
-/* Verlet list, column-major ELL. */
+/* Verlet list, column-major ELL.  Two entry formats:
+ *   nbr   32-bit global partner index + image code (any precision);
+ *   nbr16 16-bit slot in the shared-memory neighbourhood of the particle's tile
+ *         (mixed precision; used when not NULL): a tile is tile_z cells of one
+ *         z column, its neighbourhood the 3x3 columns around it, staged with the
+ *         periodic images applied, at most tile_capacity particles. */
 typedef struct {
     int32_t stride;              /* >= capacity of particles */
     int32_t max_neighbors;       /* entries per particle */
-    int32_t half;                /* 1: each unordered pair once (Newton's third law) */
-    int32_t *nbr;                /* [max_neighbors * stride] */
+    int32_t half;                /* 1: interior pairs once (Newton's third law) */
+    int32_t *nbr;                /* [max_neighbors * stride] or NULL */
     int32_t *count;              /* [stride] */
     int32_t steps_since_build;   /* host-maintained, for PG_SYNC_REFERENCE */
+    uint16_t *nbr16;             /* [max_neighbors * stride] or NULL */
+    int32_t tile_z;              /* cells per tile along z (nbr16 lists) */
+    int32_t tile_capacity;       /* shared-memory particles per tile (<= 65535) */
 } pg_neighbor_list;
 
 /* Lennard-Jones parameters per type pair (examples/md.py:5-8, feature tables). */
@@ -177,10 +187,11 @@ int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_c
  * examples/md.py:5-8, sim/interaction.py:222-232, ir/apply.py:112-125).
  * precision PG_FP64 writes p->force, PG_MIXED writes p->force32.  sync_mode selects
  * PG_SYNC_EXACT or PG_SYNC_REFERENCE (FP64 only).  energy, if not NULL, is a device
- * double[2] that receives potential energy and virial sum r.F (FP64 sums). */
-int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list,
-                const pg_lj_params *lj, int precision, int sync_mode, double *energy,
-                pg_workspace ws, void *stream);
+ * double[2] that receives potential energy and virial sum r.F (FP64 sums).  cells
+ * is needed for nbr16 (tile) lists and may be NULL otherwise. */
+int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
+                const pg_neighbor_list *list, const pg_lj_params *lj, int precision, int sync_mode,
+                double *energy, pg_workspace ws, void *stream);
 
 /* Velocity-Verlet half steps of examples/md.py:11-17 (the reference's
  * initial_integrate / final_integrate modules), same operation order:

@@ -27,7 +27,7 @@ class PgStatus(C.Structure):
     _fields_ = [("overflow", C.c_int32), ("max_cell_count", C.c_int32),
                 ("max_neighbors", C.c_int32), ("nonfinite", C.c_int32),
                 ("guard_tripped", C.c_int32), ("max_contacts", C.c_int32),
-                ("pad", C.c_int32 * 2)]
+                ("max_tile_staged", C.c_int32), ("pad", C.c_int32)]
 
 
 class PgBox(C.Structure):
@@ -54,7 +54,8 @@ class PgCells(C.Structure):
 
 class PgNeighborList(C.Structure):
     _fields_ = [("stride", C.c_int32), ("max_neighbors", C.c_int32), ("half", C.c_int32),
-                ("nbr", C.c_void_p), ("count", C.c_void_p), ("steps_since_build", C.c_int32)]
+                ("nbr", C.c_void_p), ("count", C.c_void_p), ("steps_since_build", C.c_int32),
+                ("nbr16", C.c_void_p), ("tile_z", C.c_int32), ("tile_capacity", C.c_int32)]
 
 
 class PgLJParams(C.Structure):
@@ -78,8 +79,8 @@ SIGNATURES = {
     "pg_bin_particles": (C.c_int, [P(PgBox), P(PgParticles), P(PgCells), PgWorkspace, C.c_void_p, C.c_void_p]),
     "pg_build_neighbor_lists": (C.c_int, [P(PgBox), P(PgParticles), P(PgCells), P(PgNeighborList), C.c_double,
                                           C.c_void_p, C.c_void_p]),
-    "pg_lj_force": (C.c_int, [P(PgBox), P(PgParticles), P(PgNeighborList), P(PgLJParams), C.c_int, C.c_int,
-                              C.c_void_p, PgWorkspace, C.c_void_p]),
+    "pg_lj_force": (C.c_int, [P(PgBox), P(PgParticles), P(PgCells), P(PgNeighborList), P(PgLJParams), C.c_int,
+                              C.c_int, C.c_void_p, PgWorkspace, C.c_void_p]),
     "pg_initial_integrate": (C.c_int, [P(PgBox), P(PgParticles), C.c_double, C.c_int, C.c_double, C.c_int32,
                                        C.c_int, C.c_void_p, C.c_void_p]),
     "pg_final_integrate": (C.c_int, [P(PgBox), P(PgParticles), C.c_double, C.c_int, C.c_void_p]),

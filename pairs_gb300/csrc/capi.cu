@@ -9,7 +9,7 @@ int gather_array(int n, const int32_t *perm, const void *src, void *dst, int ele
 int split_positions(const pg_box *box, pg_particles *p, cudaStream_t st);
 int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                          pg_neighbor_list *list, double r_list2, pg_status *status, cudaStream_t st);
-int lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list,
+int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, const pg_neighbor_list *list,
              const pg_lj_params *lj, int precision, int sync_mode, double *energy, cudaStream_t st);
 int initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision, double half_skin2,
                       int32_t step, pg_status *status, int sync_mode, cudaStream_t st);
@@ -71,11 +71,11 @@ int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_c
     return pg::build_neighbor_lists(box, p, cells, list, r_list2, status, S(stream));
 }
 
-int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list,
-                const pg_lj_params *lj, int precision, int sync_mode, double *energy,
-                pg_workspace ws, void *stream) {
+int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
+                const pg_neighbor_list *list, const pg_lj_params *lj, int precision, int sync_mode,
+                double *energy, pg_workspace ws, void *stream) {
     (void) ws;
-    return pg::lj_force(box, p, list, lj, precision, sync_mode, energy, S(stream));
+    return pg::lj_force(box, p, cells, list, lj, precision, sync_mode, energy, S(stream));
 }
 
 int pg_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,

@@ -109,6 +109,14 @@ __device__ __forceinline__ bool frozen_integrate(const pg_particles &p) {
     return p.guard != nullptr && *((volatile const int32_t *) p.guard) < p.step;
 }
 
+// FP32 Lennard-Jones table (mixed precision kernels), up to 8 types
+struct LJTableF {
+    int ntypes;
+    float cutoff2;
+    float eps[64];
+    float sig6[64];
+};
+
 // warp/block reductions
 __device__ __forceinline__ double warp_sum(double v) {
     for(int o = 16; o > 0; o >>= 1) { v += __shfl_xor_sync(0xffffffffu, v, o); }

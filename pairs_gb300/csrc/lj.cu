@@ -215,7 +215,10 @@ static KernelFn pick_mixed(bool half, bool one, bool en) {
     return en ? k_lj_mixed<false, false, true> : k_lj_mixed<false, false, false>;
 }
 
-int lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list,
+int tile_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list, const pg_cells *cells,
+                  const LJTableF &lj, double *energy, cudaStream_t st);
+
+int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, const pg_neighbor_list *list,
              const pg_lj_params *lj, int precision, int sync_mode, double *energy, cudaStream_t st) {
     if(!box || !p || !list || !lj) { return PG_ERR_ARGUMENT; }
     if(lj->ntypes < 1 || lj->ntypes > kMaxTypes) { return PG_ERR_ARGUMENT; }
@@ -238,11 +241,21 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *l
         a.lj.epsf[k] = (float) lj->epsilon[k]; a.lj.sig6f[k] = (float) lj->sigma6[k];
     }
     const bool half = list->half != 0, one = lj->ntypes == 1, en = energy != nullptr;
+    const bool tile = precision == PG_MIXED && list->nbr16 != nullptr;
+    if(tile && !cells) { return PG_ERR_ARGUMENT; }
+    if(!tile && !list->nbr) { return PG_ERR_ARGUMENT; }
     if(en) { cudaMemsetAsync(energy, 0, 2 * sizeof(double), st); }
     if(half && p->n > 0) {
         k_zero_force<<<blocks_for(p->n), kBlock, 0, st>>>(*p, precision == PG_FP64); note_launch();
     }
     if(p->n == 0) { return launch_status(); }
+    if(tile) {
+        LJTableF tf;
+        tf.ntypes = lj->ntypes;
+        tf.cutoff2 = (float) lj->cutoff2;
+        for(int k = 0; k < lj->ntypes * lj->ntypes; k++) { tf.eps[k] = (float) lj->epsilon[k]; tf.sig6[k] = (float) lj->sigma6[k]; }
+        return tile_lj_force(box, p, list, cells, tf, energy, st);
+    }
     KernelFn k = precision == PG_FP64 ? pick_fp64(half, one, en) : pick_mixed(half, one, en);
     k<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch();
     return launch_status();

@@ -15,8 +15,7 @@
 // Parameters (FP32, contiguous): W1[64][3] b1[64] W2[64][64] b2[64] W3[64] b3.
 // Loss of one sample with target R (steps remaining, observed):
 //   e = P - log R;  L = e^2 (trip observed) or min(e, 0)^2 (censored: R is a lower
-//   bound).  dL/do_c = dL/dP * softmax(-o/T)_c, so only cells carrying soft-min
-//   weight (> 1e-9 of the total) run the backward pass.
+//   bound).  dL/do_c = dL/dP * softmax(-o/T)_c.
 #include "common.cuh"
 
 namespace pg {
@@ -145,12 +144,24 @@ __global__ void k_softmin_finish(float temperature, float *result) {
 // ---------------------------------------------------------------- backward
 
 // grads (kParams) accumulate over cells and samples; loss accumulates in *loss.
-__global__ void __launch_bounds__(128) k_mlp_backward(const float *params, const float *feat, const float *out,
-                                                      int ncells, const float *result, float target_log,
-                                                      int censored, float inv_t, float *grads, float *loss) {
+// One block walks the sample's cells in chunks of blockDim.x: every thread computes
+// its cell's activations and local gradients (dL/dz2, dL/dz1) into shared memory,
+// then each thread owns a fixed slice of the parameters and sums that slice over the
+// chunk (no atomics on shared data); the block adds each parameter's total to the
+// global gradient once.
+constexpr int kBwdThreads = 128;
+
+__global__ void __launch_bounds__(kBwdThreads) k_mlp_backward(const float *params, const float *feat,
+                                                             const float *out, int ncells, const float *result,
+                                                             float target_log, int censored, float inv_t,
+                                                             float *grads, float *loss) {
     __shared__ float s[kParams];
-    __shared__ float g[kParams];
-    for(int k = threadIdx.x; k < kParams; k += blockDim.x) { g[k] = 0.0f; }
+    extern __shared__ float dyn[];
+    float *H1 = dyn;                              // [kBwdThreads][kH]
+    float *DZ2 = H1 + kBwdThreads * kH;           // [kBwdThreads][kH]
+    float *DZ1 = DZ2 + kBwdThreads * kH;          // [kBwdThreads][kH]
+    float *X = DZ1 + kBwdThreads * kH;            // [kBwdThreads][4]: x0, x1, x2, go
+    float *H2 = X + kBwdThreads * 4;              // [kBwdThreads][kH]
     load_params(params, s);
     const float P = result[0];
     const float m = ordered_to_float(*reinterpret_cast<const int *>(result + 1));
@@ -158,47 +169,92 @@ __global__ void __launch_bounds__(128) k_mlp_backward(const float *params, const
     float e = P - target_log;
     if(censored) { e = fminf(e, 0.0f); }
     const float dP = 2.0f * e;
-    if(blockIdx.x == 0 && threadIdx.x == 0) { atomicAdd(loss, e * e); }
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    float w = 0.0f;
-    if(c < ncells && out[c] < INFINITY) { w = __expf(-(out[c] - m) * inv_t) / Z; }
-    const bool active = w > 1e-9f && dP != 0.0f;
-    if(__syncthreads_or(active)) {
+    if(threadIdx.x == 0) { atomicAdd(loss, e * e); }
+    // parameter slice owned by this thread: W2 entries t, t+T, ...; then the small ones
+    float acc[kH * kH / kBwdThreads];
+    float acc_small[(kParams - kH * kH + kBwdThreads - 1) / kBwdThreads];
+    for(int q = 0; q < kH * kH / kBwdThreads; q++) { acc[q] = 0.0f; }
+    for(int q = 0; q < (int) (sizeof(acc_small) / sizeof(float)); q++) { acc_small[q] = 0.0f; }
+    const int t = threadIdx.x;
+    for(int c0 = 0; c0 < ncells; c0 += kBwdThreads) {
+        const int c = c0 + t;
+        float w = 0.0f;
+        if(c < ncells && out[c] < INFINITY) { w = __expf(-(out[c] - m) * inv_t) / Z; }
+        const float go = dP * w;
+        const bool active = go != 0.0f;
+        if(!__syncthreads_or(active)) { continue; }
+        float *h1 = H1 + t * kH, *dz2 = DZ2 + t * kH, *dz1 = DZ1 + t * kH, *h2 = H2 + t * kH;
+        float x[kIn] = {0.0f, 0.0f, 0.0f};
         if(active) {
             const float *f = feat + (size_t) c * kFeat;
-            const float x[kIn] = {f[0], f[1], f[2]};
-            const float go = dP * w;                 // dL/do_c
-            float h1[kH], dh1[kH];
+            x[0] = f[0]; x[1] = f[1]; x[2] = f[2];
             for(int u = 0; u < kH; u++) {
                 float z = s[kOffB1 + u];
                 for(int k = 0; k < kIn; k++) { z = fmaf(s[kOffW1 + u * kIn + k], x[k], z); }
                 h1[u] = tanhf(z);
-                dh1[u] = 0.0f;
+                dz1[u] = 0.0f;
             }
-            atomicAdd(&g[kOffB3], go);
             for(int u = 0; u < kH; u++) {
                 float z = s[kOffB2 + u];
                 const float *wr = s + kOffW2 + u * kH;
                 for(int k = 0; k < kH; k++) { z = fmaf(wr[k], h1[k], z); }
-                const float h2 = tanhf(z);
-                atomicAdd(&g[kOffW3 + u], go * h2);
-                const float dz2 = go * s[kOffW3 + u] * (1.0f - h2 * h2);
-                atomicAdd(&g[kOffB2 + u], dz2);
-                for(int k = 0; k < kH; k++) {
-                    atomicAdd(&g[kOffW2 + u * kH + k], dz2 * h1[k]);
-                    dh1[k] = fmaf(dz2, wr[k], dh1[k]);
-                }
+                const float hz = tanhf(z);
+                h2[u] = hz;
+                const float d2 = go * s[kOffW3 + u] * (1.0f - hz * hz);
+                dz2[u] = d2;
+                for(int k = 0; k < kH; k++) { dz1[k] = fmaf(d2, wr[k], dz1[k]); }
             }
-            for(int u = 0; u < kH; u++) {
-                const float dz1 = dh1[u] * (1.0f - h1[u] * h1[u]);
-                atomicAdd(&g[kOffB1 + u], dz1);
-                for(int k = 0; k < kIn; k++) { atomicAdd(&g[kOffW1 + u * kIn + k], dz1 * x[k]); }
+            for(int u = 0; u < kH; u++) { dz1[u] *= (1.0f - h1[u] * h1[u]); }
+        } else {
+            for(int u = 0; u < kH; u++) { h1[u] = 0.0f; dz2[u] = 0.0f; dz1[u] = 0.0f; h2[u] = 0.0f; }
+        }
+        X[t * 4 + 0] = x[0]; X[t * 4 + 1] = x[1]; X[t * 4 + 2] = x[2]; X[t * 4 + 3] = go;
+        __syncthreads();
+        // W2[u][k] += sum_c dz2[c][u] h1[c][k]
+        for(int q = 0; q < kH * kH / kBwdThreads; q++) {
+            const int e2 = t + q * kBwdThreads, u = e2 / kH, k = e2 % kH;
+            float a = 0.0f;
+            for(int cc = 0; cc < kBwdThreads; cc++) { a = fmaf(DZ2[cc * kH + u], H1[cc * kH + k], a); }
+            acc[q] += a;
+        }
+        // the rest: W1[u][k] (dz1 x), b1 (dz1), b2 (dz2), W3 (go h2), b3 (go)
+        for(int q = 0; q < (int) (sizeof(acc_small) / sizeof(float)); q++) {
+            const int r = t + q * kBwdThreads;
+            float a = 0.0f;
+            if(r < kH * kIn) {
+                const int u = r / kIn, k = r % kIn;
+                for(int cc = 0; cc < kBwdThreads; cc++) { a = fmaf(DZ1[cc * kH + u], X[cc * 4 + k], a); }
+            } else if(r < kH * kIn + kH) {
+                const int u = r - kH * kIn;
+                for(int cc = 0; cc < kBwdThreads; cc++) { a += DZ1[cc * kH + u]; }
+            } else if(r < kH * kIn + 2 * kH) {
+                const int u = r - kH * kIn - kH;
+                for(int cc = 0; cc < kBwdThreads; cc++) { a += DZ2[cc * kH + u]; }
+            } else if(r < kH * kIn + 3 * kH) {
+                const int u = r - kH * kIn - 2 * kH;
+                for(int cc = 0; cc < kBwdThreads; cc++) { a = fmaf(X[cc * 4 + 3], H2[cc * kH + u], a); }
+            } else if(r == kH * kIn + 3 * kH) {
+                for(int cc = 0; cc < kBwdThreads; cc++) { a += X[cc * 4 + 3]; }
             }
+            acc_small[q] += a;
         }
         __syncthreads();
-        for(int k = threadIdx.x; k < kParams; k += blockDim.x) {
-            if(g[k] != 0.0f) { atomicAdd(&grads[k], g[k]); }
-        }
+    }
+    for(int q = 0; q < kH * kH / kBwdThreads; q++) {
+        const int e2 = t + q * kBwdThreads;
+        if(acc[q] != 0.0f) { atomicAdd(&grads[kOffW2 + e2], acc[q]); }
+    }
+    for(int q = 0; q < (int) (sizeof(acc_small) / sizeof(float)); q++) {
+        const int r = t + q * kBwdThreads;
+        if(acc_small[q] == 0.0f) { continue; }
+        int dst;
+        if(r < kH * kIn) { dst = kOffW1 + r; }
+        else if(r < kH * kIn + kH) { dst = kOffB1 + (r - kH * kIn); }
+        else if(r < kH * kIn + 2 * kH) { dst = kOffB2 + (r - kH * kIn - kH); }
+        else if(r < kH * kIn + 3 * kH) { dst = kOffW3 + (r - kH * kIn - 2 * kH); }
+        else if(r == kH * kIn + 3 * kH) { dst = kOffB3; }
+        else { continue; }
+        atomicAdd(&grads[dst], acc_small[q]);
     }
 }
 
@@ -248,8 +304,12 @@ int mlp_softmin(const float *out, int32_t ncells, float temperature, float *resu
 int mlp_backward(const float *params, const float *feat, const float *out, int32_t ncells, const float *result,
                  float target_log, int censored, float temperature, float *grads, float *loss, cudaStream_t st) {
     if(!params || !feat || !out || !result || !grads || !loss || ncells <= 0) { return PG_ERR_ARGUMENT; }
-    k_mlp_backward<<<blocks_for(ncells, 128), 128, 0, st>>>(params, feat, out, ncells, result, target_log,
-                                                             censored, 1.0f / temperature, grads, loss);
+    const size_t smem = (size_t) kBwdThreads * (4 * kH + 4) * sizeof(float);
+    if(cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem) != cudaSuccess) {
+        return PG_ERR_CUDA;
+    }
+    k_mlp_backward<<<1, kBwdThreads, smem, st>>>(params, feat, out, ncells, result, target_log, censored,
+                                                   1.0f / temperature, grads, loss);
     note_launch();
     return launch_status();
 }

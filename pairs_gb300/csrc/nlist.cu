@@ -113,9 +113,13 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
     }
 }
 
+int tile_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
+               double r_list2, pg_status *status, cudaStream_t st);
+
 int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                          pg_neighbor_list *list, double r_list2, pg_status *status, cudaStream_t st) {
     if(!box || !p || !cells || !list || !status) { return PG_ERR_ARGUMENT; }
+    if(list->nbr16 != nullptr) { return tile_build(box, p, cells, list, r_list2, status, st); }
     if(!p->pos || !p->pos_hi || !p->pos_lo || !p->pos_ref || !list->nbr || !list->count) { return PG_ERR_ARGUMENT; }
     if(list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS)) { return PG_ERR_ARGUMENT; }
     for(int d = 0; d < 3; d++) {

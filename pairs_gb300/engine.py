@@ -43,7 +43,7 @@ class LJEngine:
     def __init__(self, state, *, lo=None, hi=None, periodic=(True, True, True), cutoff=2.5, skin=0.3,
                  dt=0.005, ntypes=1, epsilon=None, sigma6=None, precision="fp64", half=False,
                  sync="exact", every=20, neighbor_capacity=100, policy="fixed", device="cuda",
-                 capacity=None, fused=True):
+                 capacity=None, fused=True, tiles=None):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -151,10 +151,18 @@ class LJEngine:
         self.cells.cell_count = t["cell_count"].data_ptr()
         self.cells.particle_cell = t["particle_cell"].data_ptr()
 
-        # ---- neighbour list
+        # ---- neighbour list: 16-bit tile lists on the mixed path (shared-memory
+        # neighbourhoods), 32-bit global lists otherwise
         self.list = A.PgNeighborList()
         self.list.stride = cap
         self.list.half = int(bool(half))
+        self.tiles = (self.precision == A.PG_MIXED) if tiles is None else bool(tiles)
+        if self.tiles:
+            if self.precision != A.PG_MIXED:
+                raise ValueError("tile lists are implemented for the mixed-precision path")
+            mean = max(n / ncells, 1.0)
+            self.list.tile_z = max(1, min(self.cells.dims[2], int(round(224.0 / mean))))
+            self._set_tile_capacity(int(9 * (self.list.tile_z + 2) * mean * 1.4) + 64)
         self._alloc_list(int(neighbor_capacity))
 
         # ---- LJ parameters
@@ -198,11 +206,28 @@ class LJEngine:
                      "pos_ref", "ref_hi", "ref_lo", "mass", "type", "uid", "flags"):
             setattr(p, name, t[name].data_ptr() if name in t else None)
 
+    # shared memory per tile block: 32 B per staged particle (+16 B force sums for
+    # half lists), below the 227 KB a block may use
+    SMEM_LIMIT = 220 * 1024
+
+    def _set_tile_capacity(self, c):
+        per = 48 if self.list.half else 32
+        self.list.tile_capacity = int(min(c, self.SMEM_LIMIT // per, 65535))
+        return c <= self.list.tile_capacity
+
     def _alloc_list(self, max_nb):
         self.list.max_neighbors = max_nb
-        self.t["nbr"] = torch.zeros((max_nb, self.cap), dtype=torch.int32, device=self.dev)
+        self.t.pop("nbr", None)
+        self.t.pop("nbr16", None)
+        if self.tiles:
+            self.t["nbr16"] = torch.zeros((max_nb, self.cap), dtype=torch.int16, device=self.dev)
+            self.list.nbr16 = self.t["nbr16"].data_ptr()
+            self.list.nbr = None
+        else:
+            self.t["nbr"] = torch.zeros((max_nb, self.cap), dtype=torch.int32, device=self.dev)
+            self.list.nbr = self.t["nbr"].data_ptr()
+            self.list.nbr16 = None
         self.t["count"] = torch.zeros((self.cap,), dtype=torch.int32, device=self.dev)
-        self.list.nbr = self.t["nbr"].data_ptr()
         self.list.count = self.t["count"].data_ptr()
 
     def _rotate_ring(self):
@@ -235,6 +260,19 @@ class LJEngine:
             guard = st.guard_tripped if guard is None else guard
             if st.nonfinite:
                 raise A.PairsError("non-finite particle position met while binning")
+            if st.overflow & 4:
+                # a tile neighbourhood did not fit the shared-memory capacity: grow it,
+                # or make tiles shorter, or give up tiles for this system
+                need = int(st.max_tile_staged * 1.15) + 32
+                if not self._set_tile_capacity(need):
+                    if self.list.tile_z > 1:
+                        self.list.tile_z = max(1, self.list.tile_z // 2)
+                        self._set_tile_capacity(need)
+                    else:
+                        self.tiles = False
+                        self._alloc_list(self.list.max_neighbors)
+                self.t["status"][6] = 0
+                continue
             if st.overflow & 2:
                 self._alloc_list(int(st.max_neighbors * 1.2) + 8)
                 continue
@@ -247,7 +285,8 @@ class LJEngine:
 
     def force(self, energy=False):
         e = C.c_void_p(self.t["energy"].data_ptr()) if energy else None
-        A.call("pg_lj_force", C.byref(self.box), C.byref(self.p), C.byref(self.list), C.byref(self.lj),
+        A.call("pg_lj_force", C.byref(self.box), C.byref(self.p), C.byref(self.cells), C.byref(self.list),
+               C.byref(self.lj),
                self.precision, self.sync, e, self.ws, self.sh)
 
     def advance(self, kicks):
@@ -471,10 +510,80 @@ class LJEngine:
     def flags(self):
         return self.t["flags"][: self.n].cpu().numpy()[self._uid_order()]
 
+    def _tile_slot_tables(self):
+        """Host restatement of the tile layout (tile.cu tile_layout): for every particle
+        the global index and image code of each shared-memory slot of its tile."""
+        dims = [self.cells.dims[d] for d in range(3)]
+        per = [bool(self.box.periodic[d]) for d in range(3)]
+        start = self.t["cell_start"].cpu().numpy()
+        count = self.t["cell_count"].cpu().numpy()
+        tz = self.list.tile_z
+        ntz = (dims[2] + tz - 1) // tz
+        dx, dy, dz = dims
+        enc = lambda s: 1 if s > 0 else (2 if s < 0 else 0)
+        tables = {}
+        for cx in range(dx):
+            for cy in range(dy):
+                for zt in range(ntz):
+                    z0, z1 = zt * tz, min(zt * tz + tz, dz)
+                    segs = []
+                    for pas in (0, 1):
+                        for ox in (-1, 0, 1):
+                            nx, sx = cx + ox, 0
+                            if nx < 0 or nx >= dx:
+                                if not per[0]:
+                                    continue
+                                sx = -1 if nx < 0 else 1
+                                nx %= dx
+                            for oy in (-1, 0, 1):
+                                ny, sy = cy + oy, 0
+                                if ny < 0 or ny >= dy:
+                                    if not per[1]:
+                                        continue
+                                    sy = -1 if ny < 0 else 1
+                                    ny %= dy
+                                cell0 = (nx * dy + ny) * dz
+                                parts = [(max(z0 - 1, 0), min(z1, dz - 1), 0)]
+                                if z0 - 1 < 0 and per[2]:
+                                    parts.append((dz - 1, dz - 1, -1))
+                                if z1 >= dz and per[2]:
+                                    parts.append((0, 0, 1))
+                                for za, zb, sz in parts:
+                                    code = enc(sx) | (enc(sy) << 2) | (enc(sz) << 4)
+                                    if (code == 0) != (pas == 0):
+                                        continue
+                                    b = start[cell0 + za]
+                                    e = start[cell0 + zb] + count[cell0 + zb]
+                                    segs.append((b, e - b, code))
+                    gj = np.concatenate([np.arange(b, b + c) for b, c, _ in segs]) if segs else np.zeros(0, int)
+                    gc = np.concatenate([np.full(c, code) for b, c, code in segs]) if segs else np.zeros(0, int)
+                    c_first = (cx * dy + cy) * dz
+                    ib = start[c_first + z0]
+                    ie = start[c_first + z1 - 1] + count[c_first + z1 - 1]
+                    for i in range(ib, ie):
+                        tables[i] = (gj, gc)
+        return tables
+
     def pairs(self):
         """Verlet entries as (uid_i, uid_j, sx, sy, sz) rows (list order per particle)."""
         n = self.n
         cnt = self.t["count"][:n].cpu().numpy()
+        if self.tiles:
+            tab = self._tile_slot_tables()
+            slots = self.t["nbr16"][:, :n].cpu().numpy().astype(np.int64) & 0xFFFF
+            uid = self.t["uid"][:n].cpu().numpy()
+            rows = []
+            dec = lambda c: np.where(c == 1, 1, np.where(c == 2, -1, 0))
+            for i in range(n):
+                k = cnt[i]
+                if k == 0:
+                    continue
+                gj, gc = tab[i]
+                sl = slots[:k, i]
+                j, code = gj[sl], gc[sl]
+                rows.append(np.stack([np.full(k, uid[i]), uid[j], dec(code & 3), dec((code >> 2) & 3),
+                                      dec((code >> 4) & 3)], axis=1))
+            return np.concatenate(rows).astype(np.int32) if rows else np.zeros((0, 5), np.int32)
         nbr = self.t["nbr"][:, :n].cpu().numpy().astype(np.uint32)
         uid = self.t["uid"][:n].cpu().numpy()
         rows = []

@@ -29,7 +29,8 @@ from . import _capi as A
 
 class LearnedSchedule:
     def __init__(self, engine, warmup_cycles=6, samples_per_cycle=4, margin=1.3, temperature=0.05, lr=3e-3,
-                 train_steps=300, seed=0, max_samples=64, top_cells=256, online_every=16, online_steps=2):
+                 train_steps=300, seed=0, max_samples=64, top_cells=256, online_every=32, online_steps=1,
+                 online_recent=16):
         self.e = engine
         lib = A.load()
         self.np = lib.pg_mlp_param_count()
@@ -37,6 +38,7 @@ class LearnedSchedule:
         self.ncells = min(top_cells, self.ncells_all)       # cells per sample: the fastest ones
         self.online_every = online_every
         self.online_steps = online_steps
+        self.online_recent = online_recent
         self.warmup_cycles = warmup_cycles
         self.samples_per_cycle = samples_per_cycle
         self.margin = margin
@@ -122,18 +124,20 @@ class LearnedSchedule:
         self.pending = []
         self.cycles += 1
         if self.trained and self.online_every and self.cycles % self.online_every == 0:
-            self.train(self.online_steps)
+            self.train(self.online_steps, recent=self.online_recent)
 
     # ---------------------------------------------------------------- training
-    def train(self, steps=None):
+    def train(self, steps=None, recent=None):
+        """Adam steps on the stored samples (the `recent` newest ones if given)."""
         e = self.e
         steps = self.train_steps if steps is None else steps
         if not self.labels:
             return None
-        ns = len(self.labels)
+        batch = self.labels if recent is None else self.labels[-recent:]
+        ns = len(batch)
         for _ in range(steps):
             self.loss.zero_()
-            for slot, target, cens in self.labels:
+            for slot, target, cens in batch:
                 self.predict_log(slot)
                 A.call("pg_mlp_backward", self._ptr(self.params), self._ptr(self.feat[slot]), self._ptr(self.out),
                        self.ncells, self._ptr(self.result), float(target), int(cens), self.temperature,

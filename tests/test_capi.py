@@ -55,5 +55,5 @@ def test_workspace_size_positive(lib):
 def test_argument_errors_without_gpu(lib):
     # null descriptors are rejected before any CUDA call
     assert lib.pg_build_neighbor_lists(None, None, None, None, 7.84, None, None) == _capi.PG_ERR_ARGUMENT
-    assert lib.pg_lj_force(None, None, None, None, 0, 0, None, _capi.PgWorkspace(), None) == _capi.PG_ERR_ARGUMENT
+    assert lib.pg_lj_force(None, None, None, None, None, 0, 0, None, _capi.PgWorkspace(), None) == _capi.PG_ERR_ARGUMENT
     assert lib.pg_permute(-1, None, None, None, 4, None) == _capi.PG_ERR_ARGUMENT
