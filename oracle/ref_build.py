@@ -44,12 +44,24 @@ CONFIGS = {
     "lj4_t4": dict(kind="md", n=[4, 4, 4], timesteps=100, ntypes=4, reneighbor_every=20, thermo_every=100),
     "lj8": dict(kind="md", n=[8, 8, 8], timesteps=100, ntypes=1, reneighbor_every=20, thermo_every=100),
     "lj6x5x4": dict(kind="md", n=[6, 5, 4], timesteps=60, ntypes=1, reneighbor_every=10, thermo_every=20),
+    # DEM example program (spheres on a simple-cubic grid falling on a bottom wall);
+    # "dem_dense" packs the grid tighter so sphere-sphere contacts start early
+    "dem_small": dict(kind="dem", timesteps=300, domain_size=[0.03, 0.03, 0.05], spacing=0.005,
+                      planes=[[100000, 0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 13]]),
+    "dem_dense": dict(kind="dem", timesteps=300, domain_size=[0.02, 0.02, 0.03], spacing=0.0034,
+                      initial_velocity=0.3,
+                      planes=[[100000, 0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 13]]),
 }
 
 
 def generate(name, cfg):
     wd = os.path.join(OUT, name)
     os.makedirs(wd, exist_ok=True)
+    if cfg["kind"] == "dem":
+        with open(os.path.join(wd, "planes.input"), "w") as f:
+            for p in cfg["planes"]:
+                f.write(",".join(repr(x) if isinstance(x, float) else str(x) for x in p) + "\n")
+        cfg = dict(cfg, planes="planes.input")
     env = dict(os.environ)
     env["PYTHONPATH"] = os.path.join(REF, "src")
     full = dict(cfg)
@@ -65,6 +77,8 @@ def patch(src_path, cfg):
     """Insert the two hook calls into the generated main()."""
     with open(src_path) as f:
         lines = f.read().split("\n")
+    if cfg["kind"] == "dem":
+        return patch_dem(src_path, lines)
 
     # The time loop follows the start of the "all" timer (sim/timestep.py:63-72).
     t0 = next(k for k, l in enumerate(lines) if "pairs::start_timer(pairs, 0);" in l)
@@ -92,10 +106,29 @@ def patch(src_path, cfg):
         f.write("\n".join(lines))
 
 
+def patch_dem(src_path, lines):
+    t0 = next(k for k, l in enumerate(lines) if "pairs::start_timer(pairs, 0);" in l)
+    m = re.match(r"\s*for\(int (i\d+) = 0; \1 < (\d+); \1\+\+\) \{", lines[t0 + 1])
+    assert m, "time loop not found after the all-timer start"
+    ts_var = m.group(1)
+    cu = next(k for k, l in enumerate(lines) if "clear_unused_contact_history(pairs" in l and k > t0)
+    while "stop_timer" in lines[cu + 1]:
+        cu += 1
+    lines.insert(cu + 1, "        oracle_hook_step_dem(%s, nlocal, uid, position, linear_velocity, angular_velocity, "
+                         "force, torque, rotation_quat, num_contacts, contact_lists, is_sticking, "
+                         "tangential_spring_displacement, impact_velocity_magnitude, neighbor_capacity);" % ts_var)
+    lines.insert(t0, "    oracle_hook_init_dem(nlocal, uid, type, flags, shape, mass, radius, position, "
+                     "linear_velocity, normal);")
+    with open(src_path, "w") as f:
+        f.write("\n".join(lines))
+
+
 def box_of(cfg):
     if "domain" in cfg:
         lo, hi = cfg["domain"]
         return [hi[d] - lo[d] for d in range(3)]
+    if cfg["kind"] == "dem":
+        return list(cfg["domain_size"])
     a = pow(4.0 / cfg.get("rho", 0.8442), 1.0 / 3.0)   # sim/copper_fcc_lattice.py:19-22
     return [cfg["n"][d] * a for d in range(3)]
 

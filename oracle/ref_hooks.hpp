@@ -138,3 +138,59 @@ static void oracle_hook_step(
     }
     fclose(f);
 }
+
+/* DEM dumps (examples/dem.py program): initial state after the setup kernel, and
+ * per step the local particles' state plus every contact-history record. */
+static void oracle_hook_init_dem(int nlocal, const int *uid, const int *type, const int *flags, const int *shape,
+                                 const double *mass, const double *radius, const double *position,
+                                 const double *linear_velocity, const double *normal) {
+    using namespace oracle_dump;
+    const char *dir = dump_dir();
+    if(dir == nullptr) { return; }
+    std::string path = std::string(dir) + "/init.bin";
+    FILE *f = fopen(path.c_str(), "wb");
+    if(f == nullptr) { perror("oracle_hook_init_dem"); std::exit(3); }
+    put_i32(f, nlocal);
+    put_arr(f, uid, nlocal); put_arr(f, type, nlocal); put_arr(f, flags, nlocal); put_arr(f, shape, nlocal);
+    put_arr(f, mass, nlocal); put_arr(f, radius, nlocal);
+    put_arr(f, position, (size_t) nlocal * 3); put_arr(f, linear_velocity, (size_t) nlocal * 3);
+    put_arr(f, normal, (size_t) nlocal * 3);
+    fclose(f);
+}
+
+static void oracle_hook_step_dem(int ts, int nlocal, const int *uid, const double *position,
+                                 const double *linear_velocity, const double *angular_velocity,
+                                 const double *force, const double *torque, const double *rotation_quat,
+                                 const int *num_contacts, const int *contact_lists, const int *is_sticking,
+                                 const double *tsd, const double *ivm, int neighbor_capacity) {
+    using namespace oracle_dump;
+    const char *dir = dump_dir();
+    if(dir == nullptr) { return; }
+    const int every = env_int("PAIRS_ORACLE_DUMP_EVERY", 1);
+    if(every > 1 && (ts % every) != 0) { return; }
+    char name[64];
+    snprintf(name, sizeof(name), "/step_%05d.bin", ts);
+    std::string path = std::string(dir) + name;
+    FILE *f = fopen(path.c_str(), "wb");
+    if(f == nullptr) { perror("oracle_hook_step_dem"); std::exit(3); }
+    put_i32(f, ts); put_i32(f, nlocal);
+    put_arr(f, uid, nlocal);
+    put_arr(f, position, (size_t) nlocal * 3); put_arr(f, linear_velocity, (size_t) nlocal * 3);
+    put_arr(f, angular_velocity, (size_t) nlocal * 3);
+    put_arr(f, force, (size_t) nlocal * 3); put_arr(f, torque, (size_t) nlocal * 3);
+    put_arr(f, rotation_quat, (size_t) nlocal * 4);
+    std::vector<int32_t> ids;
+    std::vector<double> vals;
+    for(int i = 0; i < nlocal; i++) {
+        for(int k = 0; k < num_contacts[i]; k++) {
+            const size_t a = (size_t) i * neighbor_capacity + k;
+            ids.push_back(uid[i]); ids.push_back(contact_lists[a]); ids.push_back(is_sticking[a]);
+            vals.push_back(tsd[a * 3]); vals.push_back(tsd[a * 3 + 1]); vals.push_back(tsd[a * 3 + 2]);
+            vals.push_back(ivm[a]);
+        }
+    }
+    put_i32(f, (int32_t) (ids.size() / 3));
+    put_arr(f, ids.data(), ids.size());
+    put_arr(f, vals.data(), vals.size());
+    fclose(f);
+}

@@ -87,6 +87,34 @@ def make(name):
     print(name, os.path.getsize(path), "bytes")
 
 
+DEM_KEEP = {
+    "dem_small": [0, 1, 100, 150, 300],
+    "dem_dense": [0, 1, 50, 150, 300],
+}
+
+
+def make_dem(name):
+    exe, cfg = ref_build.build(name)
+    dump = os.path.join(ref_build.OUT, name, "dump")
+    ref_build.run(exe, dump)
+    init, steps = ref_dump.read_dem_all(dump)
+    rec = {"cfg": np.array(json.dumps({k: v for k, v in cfg.items() if not k.startswith("_")}))}
+    for k in ("uid", "type", "flags", "shape", "mass", "radius", "pos", "vel", "normal"):
+        rec["init_" + k] = init[k]
+    for ts in DEM_KEEP[name]:
+        s = ref_dump.dem_by_uid(steps[ts])
+        for k in ("uid", "pos", "vel", "angvel", "force", "torque", "quat"):
+            rec[f"step{ts}_{k}"] = s[k]
+        ids, vals = s["contact_ids"], s["contact_vals"]
+        order = np.lexsort((ids[:, 1], ids[:, 0]))
+        rec[f"step{ts}_contact_ids"] = ids[order]
+        rec[f"step{ts}_contact_vals"] = vals[order]
+    rec["ncontacts"] = np.array([len(steps[t]["contact_ids"]) for t in sorted(steps)])
+    path = os.path.join(OUT, name + ".npz")
+    np.savez_compressed(path, **rec)
+    print(name, os.path.getsize(path), "bytes")
+
+
 def unpack_pairs(packed):
     """Inverse of the compact pair encoding used above."""
     ij = packed[:, :4].copy().view(np.int16).astype(np.int32)
@@ -94,5 +122,5 @@ def unpack_pairs(packed):
 
 
 if __name__ == "__main__":
-    for n in (sys.argv[1:] or list(KEEP)):
-        make(n)
+    for n in (sys.argv[1:] or list(KEEP) + list(DEM_KEEP)):
+        (make_dem if n in DEM_KEEP else make)(n)

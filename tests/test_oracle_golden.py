@@ -75,3 +75,30 @@ def test_exact_sync_differs_only_off_rebuild():
     assert np.array_equal(ref.state()[2], exact.state()[2])
     ref.step(); exact.step()
     assert not np.array_equal(ref.state()[2], exact.state()[2])
+
+
+DEM_NAMES = ["dem_small", "dem_dense"]
+
+
+@pytest.mark.parametrize("name", DEM_NAMES)
+def test_dem_oracle_matches_reference_bit_exact(name):
+    from oracle import dem
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    cfg = json.loads(str(g["cfg"]))
+    p = dem.example_params(spacing=cfg["spacing"], v0=cfg.get("initial_velocity", 1.0))
+    sim = dem.Sim(cfg["domain_size"], cfg["planes"], p)
+    ini = sim.initial()
+    for k in ("uid", "type", "flags", "shape", "mass", "radius", "pos", "vel", "normal"):
+        assert np.array_equal(ini[k], g["init_" + k]), k
+    keep = sorted(int(k[4:].split("_")[0]) for k in g.files if k.startswith("step") and k.endswith("_pos"))
+    for ts in range(max(keep) + 1):
+        sim.step()
+        if ts in keep:
+            uid = g[f"step{ts}_uid"]
+            st = sim.state(uid)
+            for k in ("pos", "vel", "angvel", "force", "torque", "quat"):
+                assert np.array_equal(st[k], g[f"step{ts}_{k}"]), (ts, k)
+            ids, vals = sim.contacts()
+            order = np.lexsort((ids[:, 1], ids[:, 0]))
+            assert np.array_equal(ids[order], g[f"step{ts}_contact_ids"]), ts
+            assert np.array_equal(vals[order], g[f"step{ts}_contact_vals"]), ts
