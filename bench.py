@@ -132,9 +132,11 @@ def run_ours(args, rank, world, dist):
     n = len(st["mass"])
     lib = A.load()
 
+    tiles = {"auto": None, "on": True, "off": False}[args.tiles]
+
     def make(precision, half, policy):
         return LJEngine(st, precision=precision, half=half, sync="exact", every=20, policy=policy,
-                        device=str(dev))
+                        device=str(dev), tiles=tiles if precision == "mixed" else None)
 
     def kernel_times(eng, k):
         stream = eng.stream
@@ -214,16 +216,19 @@ def run_ours(args, rank, world, dist):
     fms = kernel_times(eng, 20)
     pairs_total = int(eng.t["count"][:n].sum().item())
     # algorithmic bytes of one force launch: own position (32: FP32 hi+lo, or FP64
-    # x,y,z,pad), neighbour count (4), force write (16 FP32 / 32 FP64), 4 bytes per
-    # Verlet entry; a half list adds one reaction write per particle (b_F)
+    # x,y,z,pad), neighbour count (4), force write (16 FP32 / 32 FP64), one Verlet
+    # entry per pair (4 bytes global, 2 bytes tile-local); a half list adds one
+    # reaction write per particle (b_F)
     b_f = 16 if prec == "mixed" else 32
-    b_force = n * (32 + 4 + b_f) + 4 * pairs_total + (n * b_f if eng.list.half else 0)
+    b_entry = 2 if eng.list.nbr16 else 4
+    b_force = n * (32 + 4 + b_f) + b_entry * pairs_total + (n * b_f if eng.list.half else 0)
+    kname = ("k_tile_lj" if eng.list.nbr16 else ("k_lj_mixed" if prec == "mixed" else "k_lj_fp64"))
     f_avg = statistics.mean(fms) if fms else float("nan")
     pk, pk_kind = peaks()
     achieved = b_force / (f_avg / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_kind": pk_kind,
-                "traffic": traffic_from_profiles("k_lj_" + prec), "kernel": "k_lj_%s" % args.variant,
+                "traffic": traffic_from_profiles(kname), "kernel": "%s (%s)" % (kname, args.variant),
                 "kernel_ms": round(f_avg, 4), "algorithmic_bytes": b_force, "list_entries": pairs_total}
     schedule = dict(counters, policy=args.policy, calibration_steps=calib_steps,
                     calibration_s=round(calib_s, 3),
@@ -398,6 +403,8 @@ def main():
                     default="mixed-half")
     ap.add_argument("--policy", default="learned", help="rebuild policy: learned | guard | fixed | interval:k")
     ap.add_argument("--drift-steps", type=int, default=1000)
+    ap.add_argument("--tiles", choices=["auto", "on", "off"], default="auto",
+                    help="mixed path: 16-bit shared-memory tile lists (auto = on) or global lists")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline arm only (profiling runs)")
     args = ap.parse_args()

@@ -154,6 +154,66 @@ typedef struct {
     int64_t bytes;
 } pg_workspace;
 
+/* DEM particle state, sorted order (the properties of examples/dem.py:144-162).
+ * Spheres (shape 0) and half spaces (shape 1, flags infinite|fixed) share the
+ * arrays; binning puts half spaces in the trailing bucket of the cell grid.  The
+ * reference's rotation matrix is not stored: it is always the matrix of rotation_quat
+ * (mapping/keywords.py:241-259), recomputed where needed with the same arithmetic.
+ * The reference's 3x3 inverse inertia is diag(inv_inertia) for both shapes. */
+typedef struct {
+    int32_t n;
+    int32_t capacity;
+    double *pos;                 /* double4[capacity] */
+    double *vel;                 /* double4[capacity] linear velocity */
+    double *angvel;              /* double4[capacity] angular velocity */
+    double *force;               /* double4[capacity] */
+    double *torque;              /* double4[capacity] */
+    double *quat;                /* double4[capacity] rotation quaternion (w, x, y, z) */
+    double *normal;              /* double4[capacity] half-space normal */
+    double *pos_ref;             /* double4[capacity] positions at the last list build */
+    double *mass;                /* [capacity] (+inf for half spaces after setup) */
+    double *radius;              /* [capacity] */
+    double *inv_inertia;         /* [capacity] diagonal of the inverse inertia tensor */
+    int32_t *uid;                /* [capacity] */
+    int32_t *type;               /* [capacity] */
+    int32_t *flags;              /* [capacity] 1 infinite, 4 fixed, 8 global */
+    int32_t *shape;              /* [capacity] 0 sphere, 1 half space */
+    const int32_t *guard;        /* speculative stepping, as pg_particles.guard */
+    int32_t step;
+    int32_t pad_;
+} pg_dem_particles;
+
+/* Per-particle contact history (sim/contact_history.py:12-17): up to `capacity`
+ * records per particle, column-major [slot * stride + particle], keyed by the
+ * partner's uid, in creation order (the reference's contact_lists / num_contacts
+ * with the properties is_sticking, tangential_spring_displacement and
+ * impact_velocity_magnitude of examples/dem.py:159-161). */
+typedef struct {
+    int32_t capacity;            /* records per particle, <= 64 */
+    int32_t stride;              /* >= particle capacity */
+    int32_t *count;              /* [stride] records in use */
+    int32_t *partner;            /* [capacity * stride] partner uid */
+    int32_t *sticking;           /* [capacity * stride] */
+    double  *history;            /* double4[capacity * stride]: tangential spring
+                                    displacement (x, y, z), impact velocity magnitude */
+} pg_contacts;
+
+/* Constants of the DEM program (symbols of examples/dem.py:180-211). */
+typedef struct {
+    double dt;
+    double pi;                   /* the program's `pi` symbol */
+    double kappa;                /* tangential / normal stiffness ratio */
+    double ln_e;                 /* log of the dry restitution coefficient */
+    double tc;                   /* collision time */
+    double drho;                 /* densityParticle - densityFluid, in the symbols' type */
+    double gravity;
+    double skin;                 /* Verlet list skin (list radius r_i + r_j + skin) */
+    int32_t ntypes;              /* <= 4 */
+    int32_t pad_;
+    double friction_static[16];  /* [ti * ntypes + tj] */
+    double friction_dynamic[16];
+} pg_dem_params;
+
 /* ---------------------------------------------------------------------------- */
 
 /* Library version and the size of each struct, so a binding can check layouts. */
@@ -265,6 +325,47 @@ int pg_mlp_backward(const float *params, const float *features, const float *out
 /* One Adam step on params with grads * grad_scale; zeroes grads. t counts from 1. */
 int pg_mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float beta1, float beta2,
                 float eps, int32_t t, float grad_scale, void *stream);
+
+/* ---- DEM (examples/dem.py) ------------------------------------------------ */
+
+/* Setup kernel update_mass_and_inertia (examples/dem.py:6-15): identity rotation,
+ * inv_inertia = the (0,0) entry of inversed(diagonal_matrix(0.4 m r^2)) for spheres
+ * (mapping/keywords.py:129-146 arithmetic), mass = +inf and inv_inertia = 0 for half
+ * spaces. */
+int pg_dem_setup(pg_dem_particles *d, void *stream);
+
+/* Wrap, bin and sort the DEM particles like pg_bin_particles.  pos, uid, flags and
+ * cells->particle_cell are permuted in place; every other per-particle array of d
+ * and the contact history c are gathered into `spare` / `spare_c` (same capacities),
+ * which the caller then swaps with d / c.  force and torque are not carried (each
+ * step recomputes them).  ws: pg_workspace_bytes(n, ncells). */
+int pg_dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
+               const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, void *stream);
+
+/* Sphere-sphere candidate list: partners j (with periodic image) whose centre lies
+ * within r_i + r_j + skin, over the 27 cells around the sphere (cell_len must be at
+ * least 2 r_max + skin).  Records pos_ref.  The reference scans the 27 cells every
+ * step instead (build_cell_lists only, examples/dem.py:193); the exact contact test
+ * below runs every step, so the contacts are the same while no sphere moved more
+ * than skin/2 since the build. */
+int pg_dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *cells, pg_neighbor_list *list,
+                      const pg_dem_params *prm, pg_status *status, void *stream);
+
+/* Gravity with buoyancy (examples/dem.py:90-92) and the linear spring-dashpot
+ * contact (examples/dem.py:18-74) against spheres (list) and half spaces (trailing
+ * bucket), with contact-history lookup/creation by partner uid
+ * (mapping/funcs.py:230-265) and removal of the records not used this step
+ * (sim/contact_history.py:91-127).  Writes force and torque (FP64, the generated
+ * operation order).  Overflow bit 3: a particle needed more than c->capacity records. */
+int pg_dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cells,
+                 const pg_neighbor_list *list, const pg_contacts *c, const pg_dem_params *prm,
+                 pg_status *status, void *stream);
+
+/* Explicit Euler with rotation (examples/dem.py:77-87), skipping fixed particles,
+ * plus the FP64 displacement guard against pos_ref (first step with a displacement
+ * above sqrt(half_skin2) kept in status->guard_tripped). */
+int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step,
+                 pg_status *status, void *stream);
 
 /* cudaStreamSynchronize, returning PG_OK or PG_ERR_CUDA. */
 int pg_stream_sync(void *stream);

@@ -67,7 +67,29 @@ class PgWorkspace(C.Structure):
     _fields_ = [("ptr", C.c_void_p), ("bytes", C.c_int64)]
 
 
-STRUCTS = [PgStatus, PgBox, PgParticles, PgCells, PgNeighborList, PgLJParams, PgWorkspace]
+class PgDemParticles(C.Structure):
+    _fields_ = [("n", C.c_int32), ("capacity", C.c_int32),
+                ("pos", C.c_void_p), ("vel", C.c_void_p), ("angvel", C.c_void_p), ("force", C.c_void_p),
+                ("torque", C.c_void_p), ("quat", C.c_void_p), ("normal", C.c_void_p), ("pos_ref", C.c_void_p),
+                ("mass", C.c_void_p), ("radius", C.c_void_p), ("inv_inertia", C.c_void_p),
+                ("uid", C.c_void_p), ("type", C.c_void_p), ("flags", C.c_void_p), ("shape", C.c_void_p),
+                ("guard", C.c_void_p), ("step", C.c_int32), ("pad_", C.c_int32)]
+
+
+class PgContacts(C.Structure):
+    _fields_ = [("capacity", C.c_int32), ("stride", C.c_int32), ("count", C.c_void_p),
+                ("partner", C.c_void_p), ("sticking", C.c_void_p), ("history", C.c_void_p)]
+
+
+class PgDemParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("pi", C.c_double), ("kappa", C.c_double), ("ln_e", C.c_double),
+                ("tc", C.c_double), ("drho", C.c_double), ("gravity", C.c_double), ("skin", C.c_double),
+                ("ntypes", C.c_int32), ("pad_", C.c_int32),
+                ("friction_static", C.c_double * 16), ("friction_dynamic", C.c_double * 16)]
+
+
+STRUCTS = [PgStatus, PgBox, PgParticles, PgCells, PgNeighborList, PgLJParams, PgWorkspace, PgDemParticles,
+           PgContacts, PgDemParams]
 
 P = C.POINTER
 # name -> (restype, argtypes)
@@ -101,6 +123,15 @@ SIGNATURES = {
                                   C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
     "pg_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_float,
                               C.c_float, C.c_int32, C.c_float, C.c_void_p]),
+    "pg_dem_setup": (C.c_int, [P(PgDemParticles), C.c_void_p]),
+    "pg_dem_bin": (C.c_int, [P(PgBox), P(PgDemParticles), P(PgDemParticles), P(PgContacts), P(PgContacts),
+                             P(PgCells), PgWorkspace, C.c_void_p, C.c_void_p]),
+    "pg_dem_build_list": (C.c_int, [P(PgBox), P(PgDemParticles), P(PgCells), P(PgNeighborList), P(PgDemParams),
+                                    C.c_void_p, C.c_void_p]),
+    "pg_dem_force": (C.c_int, [P(PgBox), P(PgDemParticles), P(PgCells), P(PgNeighborList), P(PgContacts),
+                               P(PgDemParams), C.c_void_p, C.c_void_p]),
+    "pg_dem_euler": (C.c_int, [P(PgDemParticles), P(PgDemParams), C.c_double, C.c_int32, C.c_void_p,
+                               C.c_void_p]),
 }
 
 _lib = None

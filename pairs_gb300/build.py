@@ -21,6 +21,9 @@ LIB = os.path.join(LIBDIR, "libpairs_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I", INCLUDE, "-I", CSRC]
+# per-file flags: the FP64 DEM kernels follow the reference's operation order with
+# every multiply and add separately rounded
+FILE_FLAGS = {"dem.cu": ["-fmad=false"]}
 
 
 def nvcc():
@@ -39,7 +42,7 @@ def _digest(paths):
     for p in paths:
         with open(p, "rb") as f:
             h.update(p.encode() + b"\0" + f.read())
-    h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    h.update(" ".join(ARCH + NVCC_FLAGS + sorted(str(FILE_FLAGS).split())).encode())
     return h.hexdigest()
 
 
@@ -60,7 +63,8 @@ def build(force=False, verbose=False, extra_flags=()):
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        cmd = [cc, "-c", src, "-o", obj] + ARCH + NVCC_FLAGS + list(extra_flags)
+        cmd = [cc, "-c", src, "-o", obj] + ARCH + NVCC_FLAGS + FILE_FLAGS.get(os.path.basename(src), []) + \
+            list(extra_flags)
         if verbose:
             cmd += ["-Xptxas", "-v"]
         res = subprocess.run(cmd, capture_output=True, text=True)

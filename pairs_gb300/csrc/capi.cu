@@ -31,6 +31,15 @@ int mlp_backward(const float *params, const float *feat, const float *out, int32
 int mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float b1, float b2, float eps,
              int32_t t, float scale, cudaStream_t st);
 int mlp_param_count();
+int dem_setup(pg_dem_particles *d, cudaStream_t st);
+int dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
+            const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, cudaStream_t st);
+int dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *cells, pg_neighbor_list *list,
+                   const pg_dem_params *prm, pg_status *status, cudaStream_t st);
+int dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cells, const pg_neighbor_list *list,
+              const pg_contacts *c, const pg_dem_params *prm, pg_status *status, cudaStream_t st);
+int dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step, pg_status *status,
+              cudaStream_t st);
 }  // namespace pg
 
 unsigned long long pg::g_kernel_launches = 0;
@@ -47,7 +56,8 @@ int pg_struct_sizes(int64_t *out, int n) {
     const int64_t sizes[] = {
         (int64_t) sizeof(pg_status), (int64_t) sizeof(pg_box), (int64_t) sizeof(pg_particles),
         (int64_t) sizeof(pg_cells), (int64_t) sizeof(pg_neighbor_list), (int64_t) sizeof(pg_lj_params),
-        (int64_t) sizeof(pg_workspace),
+        (int64_t) sizeof(pg_workspace), (int64_t) sizeof(pg_dem_particles), (int64_t) sizeof(pg_contacts),
+        (int64_t) sizeof(pg_dem_params),
     };
     const int m = (int) (sizeof(sizes) / sizeof(sizes[0]));
     if(out == nullptr) { return m; }
@@ -117,6 +127,29 @@ int pg_permute(int32_t n, const int32_t *perm, const void *src, void *dst, int e
 }
 
 int pg_mlp_param_count(void) { return pg::mlp_param_count(); }
+
+int pg_dem_setup(pg_dem_particles *d, void *stream) { return pg::dem_setup(d, S(stream)); }
+
+int pg_dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
+               const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, void *stream) {
+    return pg::dem_bin(box, d, spare, c, spare_c, cells, ws, status, S(stream));
+}
+
+int pg_dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *cells, pg_neighbor_list *list,
+                      const pg_dem_params *prm, pg_status *status, void *stream) {
+    return pg::dem_build_list(box, d, cells, list, prm, status, S(stream));
+}
+
+int pg_dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cells,
+                 const pg_neighbor_list *list, const pg_contacts *c, const pg_dem_params *prm,
+                 pg_status *status, void *stream) {
+    return pg::dem_force(box, d, cells, list, c, prm, status, S(stream));
+}
+
+int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step,
+                 pg_status *status, void *stream) {
+    return pg::dem_euler(d, prm, half_skin2, step, status, S(stream));
+}
 
 int pg_cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t steps_since_build,
                      double dt, double half_skin, float *features, void *stream) {

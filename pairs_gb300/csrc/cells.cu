@@ -21,9 +21,10 @@ __global__ void k_bin_count(pg_box box, pg_particles p, pg_cells cells, int32_t 
     double c3[3] = {x.x, x.y, x.z};
     bool moved = false;
     bool finite = true;
+    const bool infinite = p.flags != nullptr && (p.flags[i] & kFlagInfinite);   // half spaces stay put
     for(int d = 0; d < 3; d++) {
         if(!isfinite(c3[d])) { finite = false; }
-        if(box.periodic[d]) {
+        if(box.periodic[d] && !infinite) {
             if(c3[d] < box.lo[d]) { c3[d] = __dadd_rn(c3[d], box.len[d]); moved = true; }
             else if(c3[d] > box.hi[d]) { c3[d] = __dadd_rn(c3[d], -box.len[d]); moved = true; }
         }
@@ -36,7 +37,7 @@ __global__ void k_bin_count(pg_box box, pg_particles p, pg_cells cells, int32_t 
     if(!finite) {
         atomicExch(&status->nonfinite, 1);
         cell = cells.ncells;                       // parked in the extra bucket
-    } else if(p.flags != nullptr && (p.flags[i] & kFlagInfinite)) {
+    } else if(infinite) {
         cell = cells.ncells;                       // infinite shapes (half spaces) last
     } else {
         int idx = 0;

@@ -54,8 +54,9 @@ struct TileArgs {
 };
 
 // Enumerate the neighbourhood of tile t into shared tables (one thread), unshifted
-// segments first; returns the number of staged particles.
-__device__ int tile_layout(const TileArgs &a, int t, Seg *segs, Col *cols, int &nsegs, int &n_unshifted,
+// segments first; returns the number of staged particles.  unshifted_slots = the
+// shared-memory slots of the unshifted segments (slots [0, unshifted_slots)).
+__device__ int tile_layout(const TileArgs &a, int t, Seg *segs, Col *cols, int &nsegs, int &unshifted_slots,
                            int &i_begin, int &i_end, int &cx, int &cy, int &z0, int &z1) {
     const int dx = a.cells.dims[0], dy = a.cells.dims[1], dz = a.cells.dims[2];
     const int zt = t % a.ntz, col = t / a.ntz;
@@ -65,7 +66,7 @@ __device__ int tile_layout(const TileArgs &a, int t, Seg *segs, Col *cols, int &
     i_begin = a.cells.cell_start[c_first + z0];
     i_end = a.cells.cell_start[c_first + z1 - 1] + a.cells.cell_count[c_first + z1 - 1];
     Seg tmp[kMaxSegs];
-    int n = 0;
+    int n = 0, n_unshifted_segs = 0;
     for(int k = 0; k < 9; k++) {
         cols[k].cell0 = 0; cols[k].za = 0; cols[k].zb = -1;
         cols[k].main_seg = cols[k].low_seg = cols[k].high_seg = -1;
@@ -110,14 +111,17 @@ __device__ int tile_layout(const TileArgs &a, int t, Seg *segs, Col *cols, int &
                 }
             }
         }
-        if(pass == 0) { n_unshifted = n; }
+        if(pass == 0) { n_unshifted_segs = n; }
     }
     int base = 0;
+    unshifted_slots = 0;
     for(int s = 0; s < n; s++) {
+        if(s == n_unshifted_segs) { unshifted_slots = base; }
         tmp[s].base = base;
         base += tmp[s].count;
         segs[s] = tmp[s];
     }
+    if(n_unshifted_segs == n) { unshifted_slots = base; }
     nsegs = n;
     return base;
 }

@@ -67,7 +67,11 @@ def read_particle_data(sim, filename, prop_names, shape_id):
             return out[name]
         prop = sim.property(name)
         val = prop.value if prop is not None else default
-        return np.full((m,) if not isinstance(val, (list, tuple)) else (m, len(val)), val, dtype=np.float64)
+        if isinstance(val, (list, tuple)):
+            return np.tile(np.asarray(val, dtype=np.float64), (m, 1))
+        width = _WIDTH.get(prop.type, 1) if prop is not None else 1
+        # a scalar default of a vector/matrix property fills every component
+        return np.full((m,) if width == 1 else (m, width), val, dtype=np.float64)
 
     vel_name = "linear_velocity"
     state = dict(pos=out[pos_name].reshape(m, 3).astype(np.float64),
@@ -107,7 +111,10 @@ def format_vtk(pos, mass, flags=None):
 
 
 def write_vtk(sim, engine, timestep):
-    pos, _, _ = engine.state()
-    mass = engine.masses()
+    st = engine.state()
+    if isinstance(st, dict):                      # DEM engine: arrays by name
+        pos, mass, flags = st["pos"], st["mass"], st["flags"]
+    else:
+        pos, mass, flags = st[0], engine.masses(), engine.flags()
     with open(f"{sim.vtk_file}_{timestep}.vtk", "w") as f:
-        f.write(format_vtk(pos, mass, engine.flags()))
+        f.write(format_vtk(pos, mass, flags))

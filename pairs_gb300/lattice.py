@@ -15,6 +15,8 @@ additive lagged-Fibonacci generator (r[i] = r[i-3] + r[i-31] mod 2^32, 34 seeded
 words from the minimal-standard LCG, first 310 outputs discarded, result r >> 1),
 restated here so the type stream matches.
 """
+import math
+
 import numpy as np
 
 _IA, _IM, _IQ, _IR = 16807, 2147483647, 127773, 2836
@@ -119,3 +121,109 @@ def adjust_thermo(mass, vel, box, temp):
         vel[:, c] -= _seq_sum(vel[:, c]) / n
     t = temperature(mass, vel)
     vel *= np.sqrt(temp / t)
+
+
+# ---------------------------------------------------------------------------- DEM grid
+
+def _mt19937_words(count, seed=5489):
+    """First `count` 32-bit outputs of std::mt19937(seed) (tempered), as uint64."""
+    mt = np.zeros(624, dtype=np.uint64)
+    mt[0] = seed
+    for i in range(1, 624):
+        prev = int(mt[i - 1])
+        mt[i] = (1812433253 * (prev ^ (prev >> 30)) + i) & 0xFFFFFFFF
+    upper, lower, mag = np.uint64(0x80000000), np.uint64(0x7FFFFFFF), np.uint64(0x9908B0DF)
+    out = []
+    produced = 0
+
+    def twist(lo, hi):
+        # mt[i] for i in [lo, hi): reads mt[i+1] (old unless i+1 == 624 -> new mt[0])
+        # and mt[(i+397) % 624] (already new when it wrapped below i)
+        i = np.arange(lo, hi)
+        nxt = mt[(i + 1) % 624]
+        y = (mt[i] & upper) | (nxt & lower)
+        v = mt[(i + 397) % 624] ^ (y >> np.uint64(1))
+        v = np.where((y & np.uint64(1)) != 0, v ^ mag, v)
+        mt[lo:hi] = v
+
+    while produced < count:
+        twist(0, 227)          # reads old mt[397..623]
+        twist(227, 454)        # reads new mt[0..226]
+        twist(454, 623)        # reads new mt[227..395]
+        twist(623, 624)        # reads new mt[0] and mt[396]
+        y = mt.copy()
+        y ^= y >> np.uint64(11)
+        y ^= (y << np.uint64(7)) & np.uint64(0x9D2C5680)
+        y ^= (y << np.uint64(15)) & np.uint64(0xEFC60000)
+        y ^= y >> np.uint64(18)
+        out.append(y & np.uint64(0xFFFFFFFF))
+        produced += 624
+    return np.concatenate(out)[:count] if out else np.zeros(0, dtype=np.uint64)
+
+
+def _canonical(words):
+    """libstdc++ generate_canonical<double, 53> over pairs of 32-bit draws (low word
+    first): (a + b * 2^32) / 2^64, rounded once in the sum, clamped below 1."""
+    a = words[0::2].astype(np.float64)
+    b = words[1::2].astype(np.float64)
+    r = (a + b * 4294967296.0) / 18446744073709551616.0
+    return np.where(r >= 1.0, np.nextafter(1.0, 0.0), r)
+
+
+def dem_sc_grid(xmax, ymax, zmax, spacing, diameter, min_diameter, max_diameter, initial_velocity, density,
+                ntypes, lo=(0.0, 0.0, 0.0), hi=None):
+    """Spheres on a simple-cubic grid, the reference's dem_sc_grid
+    (runtime/dem_sc_grid.hpp:62-172) on one rank, vectorised and bit-identical.
+
+    Grid points ref + idx*spacing (ref = spacing/2) inside [0, xmax) x [0, ymax) x
+    [diameter, zmax), visited x fastest.  Every visited point draws a diameter from a
+    default-seeded mt19937 (uniform in [min_diameter, max_diameter)); a point inside
+    the domain [lo, hi - 1e-5) becomes a sphere with uid = its visit number + 1, mass
+    4/3 pi r^3 density, velocity (0.1 U(-v0, v0), 0.1 U(-v0, v0), -v0) from the same
+    engine and type rand() % ntypes."""
+    hi = (xmax, ymax, zmax) if hi is None else hi
+    gen_lo = (0.0, 0.0, float(diameter))
+    gen_hi = (float(xmax), float(ymax), float(zmax))
+    ref = spacing * 0.5
+    axes = []
+    for d in range(3):
+        start = int(math.ceil((gen_lo[d] - ref) / spacing))
+        idx = []
+        k = start
+        while True:
+            x = ref + k * spacing
+            if not (x >= gen_lo[d] and x < gen_hi[d]):
+                break
+            idx.append(x)
+            k += 1
+        axes.append(np.array(idx, dtype=np.float64))
+    if any(len(a) == 0 for a in axes):
+        return dict(pos=np.zeros((0, 3)), vel=np.zeros((0, 3)), mass=np.zeros(0), radius=np.zeros(0),
+                    type=np.zeros(0, np.int32), uid=np.zeros(0, np.int32), flags=np.zeros(0, np.int32),
+                    shape=np.zeros(0, np.int32))
+    zz, yy, xx = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    pts = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
+    npts = len(pts)
+    small = 0.00001
+    inside = np.ones(npts, dtype=bool)
+    for d in range(3):
+        inside &= (pts[:, d] >= lo[d]) & (pts[:, d] < hi[d] - small)
+    # uniform draws in visiting order: one per point, two more per kept sphere
+    per_point = 1 + 2 * inside.astype(np.int64)
+    first = np.concatenate([[0], np.cumsum(per_point)[:-1]])
+    ndraws = int(per_point.sum())
+    u = _canonical(_mt19937_words(2 * ndraws))
+    diam = u[first] * (max_diameter - min_diameter) + min_diameter
+    v0 = float(initial_velocity)
+    keep = np.nonzero(inside)[0]
+    vx = 0.1 * (u[first[keep] + 1] * (v0 - (-v0)) + (-v0))
+    vy = 0.1 * (u[first[keep] + 2] * (v0 - (-v0)) + (-v0))
+    n = len(keep)
+    rad = diam[keep] * 0.5
+    pi = 3.141592653589793
+    mass = ((4.0 / 3.0) * pi) * rad * rad * rad * float(density)
+    vel = np.stack([vx, vy, np.full(n, -v0)], axis=1)
+    typ = (glibc_rand(n) % ntypes).astype(np.int32) if n else np.zeros(0, np.int32)
+    return dict(pos=pts[keep].copy(), vel=vel, mass=mass, radius=rad, type=typ,
+                uid=(keep + 1).astype(np.int32), flags=np.zeros(n, np.int32), shape=np.zeros(n, np.int32))
+

@@ -299,6 +299,8 @@ class Simulation:
         self.engine = self.build_engine()
         eng = self.engine
         nsteps = (self.ntimesteps if timesteps is None else timesteps) + 1
+        if self.plan["program"] == "dem":
+            return self._run_dem(eng, nsteps)
         every = self._compute_thermo
         for _ in range(nsteps):
             ts = eng.ts
@@ -312,4 +314,15 @@ class Simulation:
             if self.vtk_file is not None and (self.vtk_frequency == 0 or ts % self.vtk_frequency == 0):
                 from .io import write_vtk
                 write_vtk(self, eng, ts)
+        return eng
+
+    def _run_dem(self, eng, nsteps):
+        """DEM time loop: the engine advances in chunks between VTK frames."""
+        from .io import write_vtk
+        freq = self.vtk_frequency if self.vtk_file is not None else 0
+        while eng.ts < nsteps:
+            if self.vtk_file is not None and (freq == 0 or eng.ts % freq == 0):
+                write_vtk(self, eng, eng.ts)
+            nxt = nsteps if not freq else min(nsteps, (eng.ts // freq + 1) * freq)
+            eng.run(nxt - eng.ts)
         return eng
