@@ -10,7 +10,8 @@
  *
  * Memory: the caller owns every buffer (the Python front end allocates them as
  * torch tensors).  The library allocates nothing; kernels that need scratch take it
- * from pg_workspace.
+ * from pg_workspace (pg_bin_particles_noalloc instead uses a fixed array inside the
+ * library).
  *
  * Errors: every entry point returns an int status (PG_OK, or a PG_ERR_* code, or
  * PG_OVERFLOW when a capacity was too small).  On PG_OVERFLOW the needed size is in
@@ -46,6 +47,7 @@ extern "C" {
 #define PG_ERR_ARGUMENT   -1     /* invalid argument (sizes, null pointers, alignment) */
 #define PG_ERR_CUDA       -2     /* a CUDA call failed (launch or runtime error) */
 #define PG_ERR_NONFINITE  -3     /* a non-finite position/velocity/force was found */
+#define PG_ERR_LIMIT      -4     /* the input is larger than a fixed-scratch entry point takes */
 
 #define PG_FP64   0              /* FP64 force, FP64 everything */
 #define PG_MIXED  1              /* FP32 force on compensated FP32 positions, FP64 integration */
@@ -233,6 +235,30 @@ int64_t pg_workspace_bytes(int32_t n, int32_t ncells);
  * (sim/cell_lists.py:90-171) and the exchange half of the halo code. */
 int pg_bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells,
                      pg_workspace ws, pg_status *status, void *stream);
+
+/* pg_bin_particles for callers that cannot allocate device memory.  No counterpart
+ * in the reference (its generated code allocates its own arrays).
+ *
+ * Who needs it: a host program that gives this library a fixed device-memory
+ * budget at start-up and allows no allocation afterwards, or one that must not
+ * stall on (or fail in) a device allocation inside its time loop, cannot make the
+ * workspace pg_bin_particles takes.  This entry point takes the same inputs and
+ * outputs and no workspace: its scratch is a fixed array inside the library's own
+ * device image, which every GPU that loads the library holds until the process
+ * exits (about 5.3 MB).  It calls no allocator.
+ *
+ * Limit: at most PG_NOALLOC_MAX_PARTICLES particles and PG_NOALLOC_MAX_CELLS cells;
+ * larger inputs return PG_ERR_LIMIT before any work is queued.
+ * The first call on a device looks up the scratch array's device address (once
+ * per device, on the calling thread's current device); make that first call
+ * before any stream capture begins.
+ * Every call shares the one scratch array and leaves its contents behind (the
+ * call clears what it needs zeroed itself); calls whose GPU work overlaps, on
+ * different streams or from different host threads, race on it: serialise them. */
+#define PG_NOALLOC_MAX_PARTICLES 131072
+#define PG_NOALLOC_MAX_CELLS     65536
+int pg_bin_particles_noalloc(const pg_box *box, pg_particles *p, pg_cells *cells, pg_status *status,
+                             void *stream);
 
 /* Build the Verlet list within r_list (the reference's build_neighbor_lists,
  * sim/neighbor_lists.py:21-48 with interaction.py:90-120).  The acceptance test

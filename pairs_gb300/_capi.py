@@ -15,6 +15,9 @@ PG_OVERFLOW = 1
 PG_ERR_ARGUMENT = -1
 PG_ERR_CUDA = -2
 PG_ERR_NONFINITE = -3
+PG_ERR_LIMIT = -4
+NOALLOC_MAX_PARTICLES = 131072
+NOALLOC_MAX_CELLS = 65536
 
 PG_FP64 = 0
 PG_MIXED = 1
@@ -99,6 +102,7 @@ SIGNATURES = {
     "pg_struct_sizes": (C.c_int, [P(C.c_int64), C.c_int]),
     "pg_workspace_bytes": (C.c_int64, [C.c_int32, C.c_int32]),
     "pg_bin_particles": (C.c_int, [P(PgBox), P(PgParticles), P(PgCells), PgWorkspace, C.c_void_p, C.c_void_p]),
+    "pg_bin_particles_noalloc": (C.c_int, [P(PgBox), P(PgParticles), P(PgCells), C.c_void_p, C.c_void_p]),
     "pg_build_neighbor_lists": (C.c_int, [P(PgBox), P(PgParticles), P(PgCells), P(PgNeighborList), C.c_double,
                                           C.c_void_p, C.c_void_p]),
     "pg_lj_force": (C.c_int, [P(PgBox), P(PgParticles), P(PgCells), P(PgNeighborList), P(PgLJParams), C.c_int,
@@ -173,7 +177,9 @@ def check_layout(lib):
             raise PairsError(f"struct layout mismatch for {s.__name__}: python {C.sizeof(s)} vs C {size}")
 
 
-_ERR = {PG_ERR_ARGUMENT: "invalid argument", PG_ERR_CUDA: "CUDA error", PG_ERR_NONFINITE: "non-finite state"}
+_ERR = {PG_ERR_ARGUMENT: "invalid argument", PG_ERR_CUDA: "CUDA error", PG_ERR_NONFINITE: "non-finite state",
+        PG_ERR_LIMIT: f"input too large for the fixed scratch (at most {NOALLOC_MAX_PARTICLES} particles and "
+                      f"{NOALLOC_MAX_CELLS} cells)"}
 
 
 def call(name, *args):
