@@ -132,11 +132,11 @@ def run_ours(args, rank, world, dist):
     n = len(st["mass"])
     lib = A.load()
 
-    tiles = {"auto": None, "on": True, "off": False}[args.tiles]
+    tiles = {"auto": None, "on": True, "off": False}[args.tiles]   # auto: the engine's default (global lists)
 
     def make(precision, half, policy):
         return LJEngine(st, precision=precision, half=half, sync="exact", every=20, policy=policy,
-                        device=str(dev), tiles=tiles if precision == "mixed" else None)
+                        device=str(dev), tiles=tiles if precision == "mixed" else None, tile_tpa=args.tile_tpa)
 
     def kernel_times(eng, k):
         stream = eng.stream
@@ -350,6 +350,73 @@ def cpu_baseline(st, steps):
                       f"with oracle/lj_oracle.c, OpenMP {nth} threads"}
 
 
+# ------------------------------------------------------------------------------ ensemble
+
+def run_ensemble(args, rank, world, dist):
+    """Batched ensemble (512 replicas, 500..32000 atoms each, rho U[0.6,0.9],
+    T U[0.7,1.5], mixed precision): aggregate atom-steps/s of the batched path (one
+    launch per phase, CUDA-graph chunks, autotuned layout) against the same replicas
+    advanced one by one with the single-system engine."""
+    import torch
+    from pairs_gb300 import _capi as A
+    from pairs_gb300 import lattice
+    from pairs_gb300.engine import LJEngine
+    from pairs_gb300.ensemble import Ensemble, autotune
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    cfgs = lattice.ensemble_configs(count=args.replicas)
+    reps = [lattice.trimmed_fcc(**c) for c in cfgs]
+    natoms = sum(len(r["mass"]) for r in reps)
+    steps = args.steps
+    (tpa, block, reach), table = autotune(reps)
+    ens = Ensemble(reps, tpa=tpa, block=block, reach=reach)
+    ens.run(args.warmup)
+    ens.synchronize()
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    lib = A.load()
+    l0 = lib.pg_kernel_launches()
+    b0, s0 = ens.nbuilds, ens.host_syncs
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ens.stream)
+    ens.run(steps)
+    e1.record(ens.stream)
+    ens.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    launches = lib.pg_kernel_launches() - l0
+    value = natoms * steps / (ms / 1e3)
+    # one by one: every replica with the single-system mixed engine (guard policy)
+    one_steps = args.one_by_one_steps
+    t0 = time.perf_counter()
+    for st in reps:
+        eng = LJEngine(st, precision="mixed", half=False, tiles=False, policy="guard", sync="exact")
+        eng.run(one_steps + 1)
+        del eng
+    torch.cuda.synchronize()
+    one_s = time.perf_counter() - t0
+    one_value = natoms * one_steps / one_s
+    line = {
+        "metric": "aggregate atom-steps/s of a batched LJ ensemble on 1 GB300", "value": value,
+        "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 force / f64 integrate",
+        "data": "synthetic (trimmed fcc lattices, reference velocity rule, seed 2024)",
+        "config": {"workload": f"{len(reps)} LJ replicas, {natoms} atoms total, sizes log-uniform 500..32000, "
+                               "rho U[0.6,0.9], T U[0.7,1.5], rc 2.5, skin 0.3, dt 0.005, mixed, full lists, "
+                               "guard rebuilds, CUDA-graph chunks",
+                   "replicas": len(reps), "atoms": natoms,
+                   "autotuned": {"tpa": tpa, "block": block, "reach": reach}},
+        "autotune_table": table,
+        "one_by_one": {"value": one_value, "steps": one_steps, "seconds": one_s,
+                       "definition": "each replica alone through LJEngine (mixed, full list, guard), "
+                                     "wall time including its setup"},
+        "speedup_vs_one_by_one": value / one_value,
+        "schedule": {"rebuilds": ens.nbuilds - b0, "host_syncs": ens.host_syncs - s0},
+        "gpu_launches": launches, "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
 # ------------------------------------------------------------------------------ reference arm
 
 def run_reference(args, rank, world, dist):
@@ -395,7 +462,10 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="lj64")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble"], default="lj64")
+    ap.add_argument("--replicas", type=int, default=512, help="ensemble workload: number of replicas")
+    ap.add_argument("--one-by-one-steps", type=int, default=100,
+                    help="ensemble workload: steps per replica of the one-by-one comparison")
     ap.add_argument("--cpu-steps", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
@@ -404,7 +474,9 @@ def main():
     ap.add_argument("--policy", default="learned", help="rebuild policy: learned | guard | fixed | interval:k")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--tiles", choices=["auto", "on", "off"], default="auto",
-                    help="mixed path: 16-bit shared-memory tile lists (auto = on) or global lists")
+                    help="mixed path, full lists: 16-bit shared-memory tile lists or global lists (auto = off)")
+    ap.add_argument("--tile-tpa", type=int, default=2, choices=[1, 2, 4],
+                    help="threads per atom of the tile force kernel")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline arm only (profiling runs)")
     args = ap.parse_args()
@@ -412,6 +484,8 @@ def main():
     dist, rank, world, _ = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world, dist)
+    elif args.workload == "ensemble":
+        run_ensemble(args, rank, world, dist)
     else:
         run_ours(args, rank, world, dist)
     if dist:

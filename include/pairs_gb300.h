@@ -127,9 +127,12 @@ typedef struct {
 /* Verlet list, column-major ELL.  Two entry formats:
  *   nbr   32-bit global partner index + image code (any precision);
  *   nbr16 16-bit slot in the shared-memory neighbourhood of the particle's tile
- *         (mixed precision; used when not NULL): a tile is tile_z cells of one
- *         z column, its neighbourhood the 3x3 columns around it, staged with the
- *         periodic images applied, at most tile_capacity particles. */
+ *         (mixed precision, full lists; used when not NULL): a tile is tile_z
+ *         cells of one z column, its neighbourhood the 3x3 columns around it,
+ *         staged with the periodic images applied.  The build writes each tile's
+ *         layout (segments of the neighbourhood) to tile_table and the largest
+ *         neighbourhood to pg_status.max_tile_staged. */
+#define PG_TILE_RECORD_WORDS 180     /* int32 words per tile in tile_table */
 typedef struct {
     int32_t stride;              /* >= capacity of particles */
     int32_t max_neighbors;       /* entries per particle */
@@ -139,7 +142,12 @@ typedef struct {
     int32_t steps_since_build;   /* host-maintained, for PG_SYNC_REFERENCE */
     uint16_t *nbr16;             /* [max_neighbors * stride] or NULL */
     int32_t tile_z;              /* cells per tile along z (nbr16 lists) */
-    int32_t tile_capacity;       /* shared-memory particles per tile (<= 65535) */
+    int32_t tile_capacity;       /* build: largest neighbourhood allowed (overflow bit 2
+                                    above it); force: slots each block stages (at least
+                                    the build's max_tile_staged) */
+    int32_t *tile_table;         /* [ntiles * PG_TILE_RECORD_WORDS] */
+    int32_t tile_tpa;            /* threads per particle in the tile force kernel: 1, 2, 4 */
+    int32_t pad_;
 } pg_neighbor_list;
 
 /* Lennard-Jones parameters per type pair (examples/md.py:5-8, feature tables). */
@@ -155,6 +163,37 @@ typedef struct {
     void   *ptr;
     int64_t bytes;
 } pg_workspace;
+
+/* One replica of a batched ensemble: its slice of the concatenated particle arrays
+ * and of the shared cell arrays, and its own periodic box and cell grid.  Replicas
+ * are independent systems; no pair crosses replicas. */
+typedef struct {
+    int32_t first;               /* particles [first, first + n) */
+    int32_t n;
+    int32_t cell0;               /* cells [cell0, cell0 + ncells) of the shared cell arrays */
+    int32_t ncells;
+    int32_t dims[3];
+    int32_t reach;               /* stencil reach in cells (cell_len >= r_list / reach) */
+    double  lo[3];
+    double  len[3];
+    double  cell_len[3];
+    double  quantum;             /* grid step of this replica's pos_hi */
+    float   len_hi[3];
+    float   len_lo[3];
+} pg_replica;
+
+/* A batched ensemble (config: hundreds of independent periodic LJ replicas run by
+ * one launch per phase).  The list layout interleaves `tpa` entries per particle:
+ * entry k of particle i is at ((k / tpa) * stride + i) * tpa + k % tpa, so the tpa
+ * threads that share a particle read consecutive words. */
+typedef struct {
+    int32_t nreplicas;
+    int32_t ncells;              /* cells of all replicas */
+    const pg_replica *replicas;  /* device [nreplicas] */
+    const int32_t *replica_of;   /* device [capacity]: replica of each particle */
+    int32_t tpa;                 /* threads per particle in the force kernel: 1, 2, 4 or 8 */
+    int32_t block;               /* threads per block of the force kernel: 64..512 */
+} pg_ensemble;
 
 /* DEM particle state, sorted order (the properties of examples/dem.py:144-162).
  * Spheres (shape 0) and half spaces (shape 1, flags infinite|fixed) share the
@@ -351,6 +390,37 @@ int pg_mlp_backward(const float *params, const float *features, const float *out
 /* One Adam step on params with grads * grad_scale; zeroes grads. t counts from 1. */
 int pg_mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float beta1, float beta2,
                 float eps, int32_t t, float grad_scale, void *stream);
+
+/* ---- batched ensemble of LJ replicas (no counterpart in the reference, which runs
+ * one system per generated program; each replica follows the same modules) ---- */
+
+/* Wrap each particle into its replica's box and bin it into the replica's cells
+ * (global cell = cell0 + local cell), sort, permute, and split positions on each
+ * replica's grid; pg_bin_particles for every replica at once.  cells->ncells = total
+ * cells, cell_start/cell_count sized as for pg_bin_particles.  ws:
+ * pg_workspace_bytes(n, total cells). */
+int pg_ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_workspace ws, pg_status *status,
+                    void *stream);
+
+/* Full Verlet lists within r_list for every replica (27- or 125-cell stencil per
+ * the replica's reach), exact FP64 acceptance as pg_build_neighbor_lists, in the
+ * tpa-interleaved layout; records pos_ref / ref_hi / ref_lo. */
+int pg_ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
+                            double r_list2, pg_status *status, void *stream);
+
+/* Mixed-precision LJ forces (FP32 on compensated positions) for every replica,
+ * tpa threads per particle, full lists. */
+int pg_ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list,
+                      const pg_lj_params *lj, void *stream);
+
+/* pg_integrate_mixed for every replica (each re-splits on its own grid); the guard
+ * word takes the first step at which any replica's particle moved > skin/2. */
+int pg_ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift,
+                          double half_skin2, int32_t step, pg_status *status, void *stream);
+
+/* Per-replica thermo: out[2r] = T_r = sum/(3 n_r - 3), out[2r+1] = sum m v^2 (FP64,
+ * one block per replica, fixed order).  out: device double[2 * nreplicas]. */
+int pg_ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, void *stream);
 
 /* ---- DEM (examples/dem.py) ------------------------------------------------ */
 

@@ -58,7 +58,11 @@ class PgCells(C.Structure):
 class PgNeighborList(C.Structure):
     _fields_ = [("stride", C.c_int32), ("max_neighbors", C.c_int32), ("half", C.c_int32),
                 ("nbr", C.c_void_p), ("count", C.c_void_p), ("steps_since_build", C.c_int32),
-                ("nbr16", C.c_void_p), ("tile_z", C.c_int32), ("tile_capacity", C.c_int32)]
+                ("nbr16", C.c_void_p), ("tile_z", C.c_int32), ("tile_capacity", C.c_int32),
+                ("tile_table", C.c_void_p), ("tile_tpa", C.c_int32), ("pad_", C.c_int32)]
+
+
+TILE_RECORD_WORDS = 180
 
 
 class PgLJParams(C.Structure):
@@ -91,8 +95,20 @@ class PgDemParams(C.Structure):
                 ("friction_static", C.c_double * 16), ("friction_dynamic", C.c_double * 16)]
 
 
+class PgReplica(C.Structure):
+    _fields_ = [("first", C.c_int32), ("n", C.c_int32), ("cell0", C.c_int32), ("ncells", C.c_int32),
+                ("dims", C.c_int32 * 3), ("reach", C.c_int32), ("lo", C.c_double * 3), ("len", C.c_double * 3),
+                ("cell_len", C.c_double * 3), ("quantum", C.c_double), ("len_hi", C.c_float * 3),
+                ("len_lo", C.c_float * 3)]
+
+
+class PgEnsemble(C.Structure):
+    _fields_ = [("nreplicas", C.c_int32), ("ncells", C.c_int32), ("replicas", C.c_void_p),
+                ("replica_of", C.c_void_p), ("tpa", C.c_int32), ("block", C.c_int32)]
+
+
 STRUCTS = [PgStatus, PgBox, PgParticles, PgCells, PgNeighborList, PgLJParams, PgWorkspace, PgDemParticles,
-           PgContacts, PgDemParams]
+           PgContacts, PgDemParams, PgReplica, PgEnsemble]
 
 P = C.POINTER
 # name -> (restype, argtypes)
@@ -127,6 +143,15 @@ SIGNATURES = {
                                   C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
     "pg_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_float,
                               C.c_float, C.c_int32, C.c_float, C.c_void_p]),
+    "pg_ensemble_bin": (C.c_int, [P(PgEnsemble), P(PgParticles), P(PgCells), PgWorkspace, C.c_void_p,
+                                  C.c_void_p]),
+    "pg_ensemble_build_lists": (C.c_int, [P(PgEnsemble), P(PgParticles), P(PgCells), P(PgNeighborList),
+                                          C.c_double, C.c_void_p, C.c_void_p]),
+    "pg_ensemble_force": (C.c_int, [P(PgEnsemble), P(PgParticles), P(PgNeighborList), P(PgLJParams),
+                                    C.c_void_p]),
+    "pg_ensemble_integrate": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_double, C.c_int, C.c_int, C.c_double,
+                                        C.c_int32, C.c_void_p, C.c_void_p]),
+    "pg_ensemble_thermo": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_void_p, C.c_void_p]),
     "pg_dem_setup": (C.c_int, [P(PgDemParticles), C.c_void_p]),
     "pg_dem_bin": (C.c_int, [P(PgBox), P(PgDemParticles), P(PgDemParticles), P(PgContacts), P(PgContacts),
                              P(PgCells), PgWorkspace, C.c_void_p, C.c_void_p]),

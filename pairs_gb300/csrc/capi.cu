@@ -31,6 +31,15 @@ int mlp_backward(const float *params, const float *feat, const float *out, int32
 int mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float b1, float b2, float eps,
              int32_t t, float scale, cudaStream_t st);
 int mlp_param_count();
+int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_workspace ws, pg_status *status,
+                 cudaStream_t st);
+int ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
+                         double r_list2, pg_status *status, cudaStream_t st);
+int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
+                   cudaStream_t st);
+int ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift, double half_skin2,
+                       int32_t step, pg_status *status, cudaStream_t st);
+int ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, cudaStream_t st);
 int dem_setup(pg_dem_particles *d, cudaStream_t st);
 int dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
             const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, cudaStream_t st);
@@ -57,7 +66,7 @@ int pg_struct_sizes(int64_t *out, int n) {
         (int64_t) sizeof(pg_status), (int64_t) sizeof(pg_box), (int64_t) sizeof(pg_particles),
         (int64_t) sizeof(pg_cells), (int64_t) sizeof(pg_neighbor_list), (int64_t) sizeof(pg_lj_params),
         (int64_t) sizeof(pg_workspace), (int64_t) sizeof(pg_dem_particles), (int64_t) sizeof(pg_contacts),
-        (int64_t) sizeof(pg_dem_params),
+        (int64_t) sizeof(pg_dem_params), (int64_t) sizeof(pg_replica), (int64_t) sizeof(pg_ensemble),
     };
     const int m = (int) (sizeof(sizes) / sizeof(sizes[0]));
     if(out == nullptr) { return m; }
@@ -127,6 +136,30 @@ int pg_permute(int32_t n, const int32_t *perm, const void *src, void *dst, int e
 }
 
 int pg_mlp_param_count(void) { return pg::mlp_param_count(); }
+
+int pg_ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_workspace ws, pg_status *status,
+                    void *stream) {
+    return pg::ensemble_bin(e, p, cells, ws, status, S(stream));
+}
+
+int pg_ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
+                            double r_list2, pg_status *status, void *stream) {
+    return pg::ensemble_build_lists(e, p, cells, list, r_list2, status, S(stream));
+}
+
+int pg_ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list,
+                      const pg_lj_params *lj, void *stream) {
+    return pg::ensemble_force(e, p, list, lj, S(stream));
+}
+
+int pg_ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift,
+                          double half_skin2, int32_t step, pg_status *status, void *stream) {
+    return pg::ensemble_integrate(e, p, dt, kicks, drift, half_skin2, step, status, S(stream));
+}
+
+int pg_ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, void *stream) {
+    return pg::ensemble_thermo(e, p, out, S(stream));
+}
 
 int pg_dem_setup(pg_dem_particles *d, void *stream) { return pg::dem_setup(d, S(stream)); }
 

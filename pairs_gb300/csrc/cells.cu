@@ -214,22 +214,25 @@ int64_t bin_workspace_bytes(int32_t n, int32_t ncells) {
     return (int64_t) bin_ws_layout(n, ncells, nullptr, nullptr);
 }
 
-int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_workspace ws,
-                  pg_status *status, cudaStream_t st, int32_t **perm_out) {
-    if(box == nullptr || p == nullptr || cells == nullptr || status == nullptr) { return PG_ERR_ARGUMENT; }
-    if(p->n < 0 || p->n > p->capacity || p->pos == nullptr) { return PG_ERR_ARGUMENT; }
-    if(cells->ncells != cells->dims[0] * cells->dims[1] * cells->dims[2]) { return PG_ERR_ARGUMENT; }
-    const int n = p->n;
-    const int ntot = cells->ncells + 1;           // + the infinite-shape bucket
-    if(ws.ptr == nullptr || ws.bytes < bin_workspace_bytes(n, cells->ncells)) { return PG_ERR_ARGUMENT; }
+// Zero the cell counters of the workspace (the count pass adds into them).
+int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cudaStream_t st) {
+    if(ws.ptr == nullptr || ws.bytes < bin_workspace_bytes(n, ncells)) { return PG_ERR_ARGUMENT; }
     BinWs w;
-    bin_ws_layout(n, cells->ncells, (char *) ws.ptr, &w);
-    if(perm_out) { *perm_out = w.perm; }
+    bin_ws_layout(n, ncells, (char *) ws.ptr, &w);
+    cudaMemsetAsync(w.count, 0, (size_t) (ncells + 1) * 4, st);
+    *count = w.count;
+    return PG_OK;
+}
 
-    cudaMemsetAsync(w.count, 0, (size_t) ntot * 4, st);
-    if(n > 0) {
-        k_bin_count<<<blocks_for(n), kBlock, 0, st>>>(*box, *p, *cells, w.count, status); note_launch();
-    }
+// Everything after the count pass: exclusive scan of the counts (ncells cells plus
+// the trailing bucket), scatter, per-cell order by uid, gather of every per-particle
+// array of p and of cells->particle_cell, and the cell bookkeeping.
+int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_cells *cells, pg_status *status,
+               cudaStream_t st, int32_t **perm_out) {
+    BinWs w;
+    bin_ws_layout(n, ncells, (char *) ws.ptr, &w);
+    if(perm_out) { *perm_out = w.perm; }
+    const int ntot = ncells + 1;
     const int nb = (ntot + kScanBlock - 1) / kScanBlock;
     k_scan_block_sums<<<nb, kScanBlock, 0, st>>>(w.count, ntot, w.block_sums); note_launch();
     k_scan_sums<<<1, kScanBlock, 0, st>>>(w.block_sums, nb); note_launch();
@@ -253,6 +256,23 @@ int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_worksp
     // cell bookkeeping for the sorted order
     cudaMemcpyAsync(cells->cell_start, w.start, (size_t) (ntot + 1) * 4, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(cells->cell_count, w.count, (size_t) ntot * 4, cudaMemcpyDeviceToDevice, st);
+    return launch_status();
+}
+
+int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_workspace ws,
+                  pg_status *status, cudaStream_t st, int32_t **perm_out) {
+    if(box == nullptr || p == nullptr || cells == nullptr || status == nullptr) { return PG_ERR_ARGUMENT; }
+    if(p->n < 0 || p->n > p->capacity || p->pos == nullptr) { return PG_ERR_ARGUMENT; }
+    if(cells->ncells != cells->dims[0] * cells->dims[1] * cells->dims[2]) { return PG_ERR_ARGUMENT; }
+    const int n = p->n;
+    int32_t *count = nullptr;
+    int rc = bin_prepare(n, cells->ncells, ws, &count, st);
+    if(rc) { return rc; }
+    if(n > 0) {
+        k_bin_count<<<blocks_for(n), kBlock, 0, st>>>(*box, *p, *cells, count, status); note_launch();
+    }
+    rc = bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out);
+    if(rc || n == 0) { return rc; }
     if(p->pos_hi != nullptr && p->pos_lo != nullptr) {
         k_split_positions<<<blocks_for(n), kBlock, 0, st>>>(*box, *p); note_launch();
     }

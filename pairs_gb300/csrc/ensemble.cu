@@ -1,0 +1,423 @@
+// Batched ensemble: hundreds of independent periodic LJ replicas of uneven size,
+// advanced by one launch per phase (bin, list, force, integrate, thermo) for all of
+// them.
+//
+// The reference runs one system per generated program; every replica here follows
+// the same modules as the single-system path (cells.cu, nlist.cu, lj.cu,
+// integrate.cu), with the box, cell grid and FP32 position grid looked up per
+// particle from the replica table.  Particles of replica r occupy [first, first+n)
+// of the concatenated arrays and its cells [cell0, cell0+ncells) of the shared cell
+// arrays; binning sorts by global cell, so replica ranges never mix.
+//
+// Small replicas would leave most SMs idle as separate launches (a 500-atom replica
+// is two blocks); batched, every phase is one grid over all ~4M particles.  The
+// force kernel can give each particle tpa threads (1, 2, 4 or 8) that split its
+// list and combine with shuffles; the list layout interleaves tpa entries per
+// particle so those threads read consecutive words.  The host-side autotuner picks
+// tpa, the block size and the stencil reach (27 cells of >= r_list or 125 cells of
+// >= r_list/2) by timing them on the ensemble itself.
+#include "common.cuh"
+
+namespace pg {
+
+int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cudaStream_t st);
+int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_cells *cells, pg_status *status,
+               cudaStream_t st, int32_t **perm_out);
+
+constexpr float kEnsBand = 1.0e-4f;
+
+struct EnsArgs {
+    pg_ensemble e;
+    pg_particles p;
+    pg_cells cells;
+    pg_neighbor_list list;
+    double r_list2;
+    float r2_lo, r2_hi;
+    int ntypes;
+    float cutoff2;
+    float eps[64];
+    float sig6[64];
+    // integration
+    double dt, kick, half_skin2;
+    float half_skin2_lo, half_skin2_hi;
+    int32_t step;
+    int drift;
+    pg_status *status;
+};
+
+// ------------------------------------------------------------------ binning
+
+__global__ void __launch_bounds__(kBlock) k_ens_count(EnsArgs a, int32_t *count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= a.p.n) { return; }
+    const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
+    D4 x = ld_d4_plain(a.p.pos, i);
+    double c3[3] = {x.x, x.y, x.z};
+    bool moved = false, finite = true;
+    for(int d = 0; d < 3; d++) {
+        if(!isfinite(c3[d])) { finite = false; }
+        const double lo = R.lo[d], hi = __dadd_rn(R.lo[d], R.len[d]);
+        if(c3[d] < lo) { c3[d] = __dadd_rn(c3[d], R.len[d]); moved = true; }
+        else if(c3[d] > hi) { c3[d] = __dadd_rn(c3[d], -R.len[d]); moved = true; }
+    }
+    if(moved) {
+        x.x = c3[0]; x.y = c3[1]; x.z = c3[2];
+        st_d4(a.p.pos, i, x);
+    }
+    int cell;
+    if(!finite) {
+        atomicExch(&a.status->nonfinite, 1);
+        cell = a.e.ncells;
+    } else {
+        int idx = 0;
+        for(int d = 0; d < 3; d++) {
+            int c = (int) floor((c3[d] - R.lo[d]) / R.cell_len[d]);
+            c = c < 0 ? 0 : (c >= R.dims[d] ? R.dims[d] - 1 : c);
+            idx = idx * R.dims[d] + c;
+        }
+        cell = R.cell0 + idx;
+    }
+    a.cells.particle_cell[i] = cell;
+    atomicAdd(&count[cell], 1);
+}
+
+// hi/lo split on each replica's own grid
+__global__ void __launch_bounds__(kBlock) k_ens_split(EnsArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= a.p.n) { return; }
+    const double q = a.e.replicas[a.e.replica_of[i]].quantum, iq = 1.0 / q;
+    const D4 x = ld_d4_plain(a.p.pos, i);
+    float4 h, l;
+    split_pos(x.x, iq, q, h.x, l.x);
+    split_pos(x.y, iq, q, h.y, l.y);
+    split_pos(x.z, iq, q, h.z, l.z);
+    h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);
+    l.w = 0.0f;
+    st_f4(a.p.pos_hi, i, h);
+    st_f4(a.p.pos_lo, i, l);
+}
+
+// ------------------------------------------------------------------ list build
+
+__device__ __forceinline__ float ens_delta(float hi_i, float lo_i, float hi_j, float lo_j, int s, float len_hi,
+                                           float len_lo) {
+    const float sh = s == 0 ? 0.0f : (s > 0 ? len_hi : -len_hi);
+    const float sl = s == 0 ? 0.0f : (s > 0 ? len_lo : -len_lo);
+    return __fadd_rn(__fsub_rn(__fsub_rn(hi_i, hi_j), sh), __fsub_rn(__fsub_rn(lo_i, lo_j), sl));
+}
+
+__device__ __forceinline__ size_t ens_slot(int k, int i, int stride, int tpa) {
+    return ((size_t) (k / tpa) * stride + i) * tpa + (k % tpa);
+}
+
+// a periodic stencil coordinate c in [-dims, 2 dims): neighbour cell and image shift
+// (offsets beyond one box are skipped by the caller; replicas are larger than
+// 2 r_list, so they hold no partner)
+__device__ __forceinline__ void wrap_cell(int c, int dims, int &nc, int &s) {
+    nc = c; s = 0;
+    if(nc < 0) { nc += dims; s = -1; }
+    else if(nc >= dims) { nc -= dims; s = 1; }
+}
+
+__global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= a.p.n) { return; }
+    const D4 xi = ld_d4(a.p.pos, i);
+    st_d4(a.p.pos_ref, i, xi);
+    const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+    st_f4(a.p.ref_hi, i, hi);
+    st_f4(a.p.ref_lo, i, lo);
+    const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
+    const int tpa = a.e.tpa;
+    int cnt = 0;
+    const int ci = a.cells.particle_cell[i] - R.cell0;
+    if(ci >= 0 && ci < R.ncells) {
+        const int dz_ = R.dims[2], dy_ = R.dims[1], dx_ = R.dims[0], rr = R.reach;
+        const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
+        const int stride = a.list.stride, cap = a.list.max_neighbors;
+        for(int ox = -rr; ox <= rr; ox++) {
+            if(ox < -dx_ || ox > dx_) { continue; }
+            int nx, sx;
+            wrap_cell(cx + ox, dx_, nx, sx);
+            for(int oy = -rr; oy <= rr; oy++) {
+                if(oy < -dy_ || oy > dy_) { continue; }
+                int ny, sy;
+                wrap_cell(cy + oy, dy_, ny, sy);
+                for(int oz = -rr; oz <= rr; oz++) {
+                    if(oz < -dz_ || oz > dz_) { continue; }
+                    int nz, sz;
+                    wrap_cell(cz + oz, dz_, nz, sz);
+                    const int c = R.cell0 + (nx * dy_ + ny) * dz_ + nz;
+                    const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
+                    const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
+                    for(int j = b; j < e; j++) {
+                        if(j == i && code == 0u) { continue; }
+                        const float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
+                        const float fx = ens_delta(hi.x, lo.x, hj.x, lj.x, sx, R.len_hi[0], R.len_lo[0]);
+                        const float fy = ens_delta(hi.y, lo.y, hj.y, lj.y, sy, R.len_hi[1], R.len_lo[1]);
+                        const float fz = ens_delta(hi.z, lo.z, hj.z, lj.z, sz, R.len_hi[2], R.len_lo[2]);
+                        const float r2f = fx * fx + fy * fy + fz * fz;
+                        bool keep;
+                        if(r2f < a.r2_lo) { keep = true; }
+                        else if(r2f > a.r2_hi) { keep = false; }
+                        else {
+                            const D4 xj = ld_d4(a.p.pos, j);
+                            const double ddx = __dsub_rn(xi.x, ref_image(xj.x, sx, R.len[0]));
+                            const double ddy = __dsub_rn(xi.y, ref_image(xj.y, sy, R.len[1]));
+                            const double ddz = __dsub_rn(xi.z, ref_image(xj.z, sz, R.len[2]));
+                            keep = ref_rsq(ddx, ddy, ddz) < a.r_list2;
+                        }
+                        if(keep) {
+                            if(cnt < cap) {
+                                a.list.nbr[ens_slot(cnt, i, stride, tpa)] = (int32_t) (code | (uint32_t) j);
+                            }
+                            cnt++;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    a.list.count[i] = cnt < a.list.max_neighbors ? cnt : a.list.max_neighbors;
+    const int wm = warp_max(cnt);
+    if((threadIdx.x & 31) == 0 && wm > 0) {
+        atomicMax(&a.status->max_neighbors, wm);
+        if(wm > a.list.max_neighbors) { atomicOr(&a.status->overflow, 2); }
+    }
+}
+
+// ------------------------------------------------------------------ force
+
+template<int TPA, bool kOneType>
+__global__ void k_ens_force(EnsArgs a) {
+    if(frozen_force(a.p)) { return; }
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = g / TPA, t = g % TPA;
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    if(i < a.p.n) {
+        const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+        const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
+        const float lhx = R.len_hi[0], lhy = R.len_hi[1], lhz = R.len_hi[2];
+        const float llx = R.len_lo[0], lly = R.len_lo[1], llz = R.len_lo[2];
+        const int ti = kOneType ? 0 : __float_as_int(hi.w) * a.ntypes;
+        const int cnt = a.list.count[i];
+        const int32_t *nb = a.list.nbr + (size_t) i * TPA + t;
+        const size_t row = (size_t) a.list.stride * TPA;
+        const float c2 = a.cutoff2;
+        for(int k = t, r = 0; k < cnt; k += TPA, r++) {
+            const uint32_t e = (uint32_t) __ldg(nb + r * row);
+            const int j = (int) (e & PG_NBR_INDEX_MASK);
+            const uint32_t code = e >> PG_NBR_INDEX_BITS;
+            const float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
+            float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
+            float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
+            if(code != 0u) {
+                const int sx = image_shift(code, 0), sy = image_shift(code, 1), sz = image_shift(code, 2);
+                dhx -= sx * lhx; dlx -= sx * llx;
+                dhy -= sy * lhy; dly -= sy * lly;
+                dhz -= sz * lhz; dlz -= sz * llz;
+            }
+            const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
+            const float rsq = dx * dx + dy * dy + dz * dz;
+            if(rsq < c2) {
+                const int tij = kOneType ? 0 : ti + __float_as_int(hj.w);
+                const float sr2 = __frcp_rn(rsq);
+                const float sr6 = sr2 * sr2 * sr2 * a.sig6[tij];
+                const float f = 48.0f * sr6 * (sr6 - 0.5f) * sr2 * a.eps[tij];
+                fx += dx * f; fy += dy * f; fz += dz * f;
+            }
+        }
+    }
+    if(TPA > 1) {
+        for(int o = TPA / 2; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o);
+            fy += __shfl_xor_sync(0xffffffffu, fy, o);
+            fz += __shfl_xor_sync(0xffffffffu, fz, o);
+        }
+    }
+    if(i < a.p.n && t == 0) { st_f4(a.p.force32, i, make_float4(fx, fy, fz, 0.0f)); }
+}
+
+// ------------------------------------------------------------------ integrate
+
+__device__ __forceinline__ void ens_resplit(double x, float q, float iq, float &hi, float &lo) {
+    const float xf = (float) x;
+    const float h = rintf(xf * iq) * q;
+    hi = h;
+    lo = (float) (x - (double) h);
+}
+
+__global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
+    if(a.drift ? frozen_integrate(a.p) : frozen_force(a.p)) { return; }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool tripped = false;
+    if(i < a.p.n) {
+        const float4 f = ld_f4(a.p.force32, i);
+        const double m = a.p.mass[i];
+        const double c = m == 1.0 ? a.kick : a.kick / m;
+        D4 v = ld_d4_plain(a.p.vel, i);
+        v.x = fma(c, (double) f.x, v.x);
+        v.y = fma(c, (double) f.y, v.y);
+        v.z = fma(c, (double) f.z, v.z);
+        st_d4(a.p.vel, i, v);
+        if(a.drift) {
+            D4 x = ld_d4_plain(a.p.pos, i);
+            x.x = fma(a.dt, v.x, x.x);
+            x.y = fma(a.dt, v.y, x.y);
+            x.z = fma(a.dt, v.z, x.z);
+            st_d4(a.p.pos, i, x);
+            const float q = (float) a.e.replicas[a.e.replica_of[i]].quantum, iq = 1.0f / q;
+            float4 h, l;
+            ens_resplit(x.x, q, iq, h.x, l.x);
+            ens_resplit(x.y, q, iq, h.y, l.y);
+            ens_resplit(x.z, q, iq, h.z, l.z);
+            h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);
+            l.w = 0.0f;
+            st_f4(a.p.pos_hi, i, h);
+            st_f4(a.p.pos_lo, i, l);
+            const float4 rh = ld_f4(a.p.ref_hi, i);
+            const float4 rl = ld_f4(a.p.ref_lo, i);
+            const float dx = (h.x - rh.x) + (l.x - rl.x);
+            const float dy = (h.y - rh.y) + (l.y - rl.y);
+            const float dz = (h.z - rh.z) + (l.z - rl.z);
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            if(d2 > a.half_skin2_hi) {
+                tripped = true;
+            } else if(d2 > a.half_skin2_lo) {
+                const D4 r = ld_d4_plain(a.p.pos_ref, i);
+                const double ex = x.x - r.x, ey = x.y - r.y, ez = x.z - r.z;
+                tripped = (ex * ex + ey * ey + ez * ez) > a.half_skin2;
+            }
+        }
+    }
+    if(__any_sync(0xffffffffu, tripped) && (threadIdx.x & 31) == 0) {
+        atomicMin(&a.status->guard_tripped, a.step);
+    }
+}
+
+// ------------------------------------------------------------------ thermo
+
+__global__ void __launch_bounds__(kBlock) k_ens_thermo(EnsArgs a, double *out) {
+    const pg_replica &R = a.e.replicas[blockIdx.x];
+    double acc = 0.0;
+    for(int i = R.first + threadIdx.x; i < R.first + R.n; i += blockDim.x) {
+        const D4 v = ld_d4(a.p.vel, i);
+        const double s = __dadd_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)), __dmul_rn(v.z, v.z));
+        acc += __dmul_rn(a.p.mass[i], s);
+    }
+    __shared__ double red[kBlock / 32];
+    acc = warp_sum(acc);
+    if((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = acc; }
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        double sum = 0.0;
+        for(int w = 0; w < (int) (blockDim.x >> 5); w++) { sum += red[w]; }
+        out[2 * blockIdx.x] = sum * (1.0 / (double) (R.n * 3 - 3));
+        out[2 * blockIdx.x + 1] = sum;
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+static bool ens_ok(const pg_ensemble *e, const pg_particles *p) {
+    return e && p && e->replicas && e->replica_of && e->nreplicas > 0 && p->n >= 0 && p->n <= p->capacity &&
+           (e->tpa == 1 || e->tpa == 2 || e->tpa == 4 || e->tpa == 8) && e->block >= 64 && e->block <= 512 &&
+           e->block % 32 == 0;
+}
+
+int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_workspace ws, pg_status *status,
+                 cudaStream_t st) {
+    if(!ens_ok(e, p) || !cells || !status || !p->pos || !p->pos_hi || !p->pos_lo || cells->ncells != e->ncells) {
+        return PG_ERR_ARGUMENT;
+    }
+    const int n = p->n;
+    int32_t *count = nullptr;
+    int rc = bin_prepare(n, e->ncells, ws, &count, st);
+    if(rc) { return rc; }
+    EnsArgs a = {};
+    a.e = *e; a.p = *p; a.cells = *cells; a.status = status;
+    if(n > 0) { k_ens_count<<<blocks_for(n), kBlock, 0, st>>>(a, count); note_launch(); }
+    rc = bin_finish(n, e->ncells, ws, p, cells, status, st, nullptr);
+    if(rc || n == 0) { return rc; }
+    a.p = *p;
+    k_ens_split<<<blocks_for(n), kBlock, 0, st>>>(a); note_launch();
+    return launch_status();
+}
+
+int ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
+                         double r_list2, pg_status *status, cudaStream_t st) {
+    if(!ens_ok(e, p) || !cells || !list || !list->nbr || !list->count || !status || !p->pos_ref || !p->ref_hi ||
+       !p->ref_lo || list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS) || list->half) {
+        return PG_ERR_ARGUMENT;
+    }
+    EnsArgs a = {};
+    a.e = *e; a.p = *p; a.cells = *cells; a.list = *list; a.status = status;
+    a.r_list2 = r_list2;
+    a.r2_lo = (float) r_list2 * (1.0f - kEnsBand);
+    a.r2_hi = (float) r_list2 * (1.0f + kEnsBand);
+    if(p->n > 0) { k_ens_list<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch(); }
+    return launch_status();
+}
+
+template<int TPA>
+static void launch_force(const EnsArgs &a, int n, int block, bool one, cudaStream_t st) {
+    const int64_t threads = (int64_t) n * TPA;
+    const int grid = (int) ((threads + block - 1) / block);
+    if(one) { k_ens_force<TPA, true><<<grid, block, 0, st>>>(a); }
+    else { k_ens_force<TPA, false><<<grid, block, 0, st>>>(a); }
+    note_launch();
+}
+
+int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
+                   cudaStream_t st) {
+    if(!ens_ok(e, p) || !list || !list->nbr || !list->count || !lj || !p->pos_hi || !p->pos_lo || !p->force32 ||
+       lj->ntypes < 1 || lj->ntypes > 8 || (lj->ntypes > 1 && !p->type)) {
+        return PG_ERR_ARGUMENT;
+    }
+    EnsArgs a = {};
+    a.e = *e; a.p = *p; a.list = *list;
+    a.ntypes = lj->ntypes;
+    a.cutoff2 = (float) lj->cutoff2;
+    for(int k = 0; k < lj->ntypes * lj->ntypes; k++) {
+        a.eps[k] = (float) lj->epsilon[k];
+        a.sig6[k] = (float) lj->sigma6[k];
+    }
+    if(p->n == 0) { return PG_OK; }
+    const bool one = lj->ntypes == 1;
+    switch(e->tpa) {
+        case 1: launch_force<1>(a, p->n, e->block, one, st); break;
+        case 2: launch_force<2>(a, p->n, e->block, one, st); break;
+        case 4: launch_force<4>(a, p->n, e->block, one, st); break;
+        default: launch_force<8>(a, p->n, e->block, one, st); break;
+    }
+    return launch_status();
+}
+
+int ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift, double half_skin2,
+                       int32_t step, pg_status *status, cudaStream_t st) {
+    if(!ens_ok(e, p) || !p->pos || !p->vel || !p->mass || !p->force32 || !p->pos_hi || !p->pos_lo || !status ||
+       (kicks != 1 && kicks != 2) || (drift && (!p->ref_hi || !p->ref_lo || !p->pos_ref))) {
+        return PG_ERR_ARGUMENT;
+    }
+    EnsArgs a = {};
+    a.e = *e; a.p = *p; a.status = status;
+    a.dt = dt;
+    a.kick = kicks * (dt * 0.5);
+    a.half_skin2 = half_skin2;
+    a.half_skin2_lo = (float) (half_skin2 * (1.0 - 1e-3));
+    a.half_skin2_hi = (float) (half_skin2 * (1.0 + 1e-3));
+    a.step = step;
+    a.drift = drift;
+    if(p->n > 0) { k_ens_integrate<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch(); }
+    return launch_status();
+}
+
+int ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, cudaStream_t st) {
+    if(!ens_ok(e, p) || !p->vel || !p->mass || !out) { return PG_ERR_ARGUMENT; }
+    EnsArgs a = {};
+    a.e = *e; a.p = *p;
+    k_ens_thermo<<<e->nreplicas, kBlock, 0, st>>>(a, out); note_launch();
+    return launch_status();
+}
+
+}  // namespace pg

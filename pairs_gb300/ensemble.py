@@ -1,0 +1,353 @@
+"""Batched ensembles: many independent periodic LJ replicas on one GPU.
+
+`Ensemble` concatenates the replicas' particles into one set of device arrays (a
+replica table gives each its slice, box, cell grid and FP32 position grid) and runs
+the mixed-precision LJ time step of `LJEngine` for all of them with one launch per
+phase (pg_ensemble_*).  Between list rebuilds the steps run speculatively in chunks
+captured once as a CUDA graph: a chunk of K steps is 2K kernel nodes (integrate,
+force), replayed without host work; the FP64 displacement guard freezes every later
+pass on the device once any replica's atom moved more than skin/2, the host then
+rebuilds all replicas and continues from the step after the trip.
+
+`autotune()` picks the threads per atom of the force kernel, its block size and the
+cell size (27 cells of >= r_list, or 125 cells of >= r_list/2) by timing the
+candidates on the ensemble itself.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _capi as A
+from .engine import _box_quantum
+
+INT32_MAX = 2 ** 31 - 1
+
+
+class Ensemble:
+    def __init__(self, replicas, *, cutoff=2.5, skin=0.3, dt=0.005, epsilon=1.0, sigma6=1.0, tpa=1, block=256,
+                 reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, device="cuda"):
+        A.load()
+        if not torch.cuda.is_available():
+            raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
+        if policy not in ("guard", "every"):
+            raise ValueError(f"unknown ensemble rebuild policy {policy!r}")
+        self.dev = torch.device(device)
+        self.policy = policy
+        self.graphs = graphs and policy == "guard"
+        self.cutoff, self.skin, self.dt = cutoff, skin, dt
+        self.r_list = cutoff + skin
+        self.r_list2 = self.r_list * self.r_list
+        self.half_skin2 = (0.5 * skin) ** 2
+        self.nrep = len(replicas)
+        sizes = [len(r["pos"]) for r in replicas]
+        self.sizes = np.array(sizes, dtype=np.int64)
+        self.first = np.concatenate([[0], np.cumsum(self.sizes)[:-1]]).astype(np.int64)
+        self.n = int(self.sizes.sum())
+        self.boxes = np.array([np.asarray(r["box"], dtype=np.float64) for r in replicas])
+        for L in self.boxes:
+            if min(L) <= 2.0 * self.r_list:
+                raise ValueError("every replica box must be longer than 2 (cutoff + skin)")
+        self.ts = 0
+        self.nbuilds = 0
+        self.host_syncs = 0
+        self.chunk = chunk
+        self._cycle = 6
+        self._build_ts = 0
+        self._graphs = {}
+        self.stream = torch.cuda.Stream(device=self.dev)
+        self.sh = C.c_void_p(self.stream.cuda_stream)
+
+        f64, f32, i32 = torch.float64, torch.float32, torch.int32
+        n = self.n
+        z = lambda shape, dt: torch.zeros(shape, dtype=dt, device=self.dev)
+        t = self.t = {}
+        for name in ("pos", "vel", "pos_ref"):
+            t[name] = z((n, 4), f64)
+        for name in ("pos_hi", "pos_lo", "ref_hi", "ref_lo", "force32"):
+            t[name] = z((n, 4), f32)
+        t["mass"] = z((n,), f64)
+        t["type"] = z((n,), i32)
+        t["uid"] = z((n,), i32)
+        t["replica_of"] = z((n,), i32)
+        hp = np.zeros((n, 4))
+        hv = np.zeros((n, 4))
+        hp[:, :3] = np.concatenate([np.asarray(r["pos"], dtype=np.float64) for r in replicas])
+        hv[:, :3] = np.concatenate([np.asarray(r["vel"], dtype=np.float64) for r in replicas])
+        t["pos"].copy_(torch.from_numpy(hp))
+        t["vel"].copy_(torch.from_numpy(hv))
+        t["mass"].copy_(torch.from_numpy(np.concatenate([np.asarray(r["mass"], dtype=np.float64) for r in replicas])))
+        t["uid"].copy_(torch.from_numpy(np.arange(n, dtype=np.int32)))
+        t["replica_of"].copy_(torch.from_numpy(np.repeat(np.arange(self.nrep, dtype=np.int32), self.sizes)))
+
+        self.p = A.PgParticles()
+        self.p.n = self.p.capacity = n
+        for name in ("pos", "vel", "pos_ref", "pos_hi", "pos_lo", "ref_hi", "ref_lo", "force32", "mass", "type",
+                     "uid"):
+            setattr(self.p, name, t[name].data_ptr())
+        self.p.guard = None
+
+        self.lj = A.PgLJParams()
+        self.lj.ntypes = 1
+        self.lj.cutoff2 = cutoff * cutoff
+        self.lj.epsilon[0], self.lj.sigma6[0] = epsilon, sigma6
+
+        init = A.PgStatus()
+        init.guard_tripped = INT32_MAX
+        t["status_init"] = torch.tensor(np.frombuffer(bytes(init), dtype=np.int32).copy(), device=self.dev)
+        t["status"] = t["status_init"].clone()
+        self.status_ptr = C.c_void_p(t["status"].data_ptr())
+        t["thermo"] = z((2 * self.nrep,), f64)
+        self.e = A.PgEnsemble()
+        self.e.nreplicas = self.nrep
+        self.e.replica_of = t["replica_of"].data_ptr()
+        self.list = A.PgNeighborList()
+        self.list.stride = n
+        self.list.half = 0
+        # a liquid at rho <= 0.9 has about 4/3 pi 2.8^3 rho ~ 83 partners within r_list
+        self._max_nb = int(neighbor_capacity or 112)
+        self.configure(tpa, block, reach)
+        with torch.cuda.stream(self.stream):
+            self.rebuild()
+            self._force(0)                     # step 0: forces only (the reference's skip_first)
+        self.ts = 1
+        self._pending = False                  # no final half kick is owed for step 0
+
+    # ------------------------------------------------------------------ layout
+
+    def configure(self, tpa, block, reach):
+        """Set the force kernel's threads per atom / block size and the cell size
+        (cells of >= r_list / reach); takes effect at the next rebuild."""
+        self.tpa, self.block, self.reach = int(tpa), int(block), int(reach)
+        self.e.tpa, self.e.block = self.tpa, self.block
+        reps = (A.PgReplica * self.nrep)()
+        cell0 = 0
+        for r in range(self.nrep):
+            R = reps[r]
+            L = self.boxes[r]
+            R.first, R.n = int(self.first[r]), int(self.sizes[r])
+            R.cell0 = cell0
+            nc = 1
+            for d in range(3):
+                dims = max(1, int(math.floor(L[d] * self.reach / self.r_list)))
+                R.dims[d] = dims
+                R.lo[d] = 0.0
+                R.len[d] = L[d]
+                R.cell_len[d] = L[d] / dims
+                nc *= dims
+            R.ncells = nc
+            R.reach = self.reach
+            q = _box_quantum(np.zeros(3), L)
+            R.quantum = q
+            for d in range(3):
+                lh = round(L[d] / q) * q
+                R.len_hi[d] = lh
+                R.len_lo[d] = L[d] - lh
+            cell0 += nc
+        self.ncells = cell0
+        self.e.ncells = cell0
+        t = self.t
+        t["replicas"] = torch.frombuffer(bytearray(bytes(reps)), dtype=torch.uint8).to(self.dev)
+        self.e.replicas = t["replicas"].data_ptr()
+        self.cells = A.PgCells()
+        self.cells.ncells = cell0
+        self.cells.dims[0], self.cells.dims[1], self.cells.dims[2] = cell0, 1, 1
+        t["cell_start"] = torch.zeros(cell0 + 2, dtype=torch.int32, device=self.dev)
+        t["cell_count"] = torch.zeros(cell0 + 1, dtype=torch.int32, device=self.dev)
+        t["particle_cell"] = torch.zeros(self.n, dtype=torch.int32, device=self.dev)
+        self.cells.cell_start = t["cell_start"].data_ptr()
+        self.cells.cell_count = t["cell_count"].data_ptr()
+        self.cells.particle_cell = t["particle_cell"].data_ptr()
+        wsb = A.load().pg_workspace_bytes(self.n, cell0)
+        t["ws"] = torch.empty((int(wsb),), dtype=torch.uint8, device=self.dev)
+        self.ws = A.PgWorkspace(t["ws"].data_ptr(), int(wsb))
+        self._alloc_list(self._max_nb)
+        self._graphs = {}
+        torch.cuda.synchronize(self.dev)       # the new buffers are used on self.stream
+
+    def _alloc_list(self, max_nb):
+        self._max_nb = max_nb
+        self.list.max_neighbors = max_nb
+        rows = -(-max_nb // self.tpa) * self.tpa
+        self.t["nbr"] = torch.zeros((rows * self.n,), dtype=torch.int32, device=self.dev)
+        self.t["count"] = torch.zeros((self.n,), dtype=torch.int32, device=self.dev)
+        self.list.nbr = self.t["nbr"].data_ptr()
+        self.list.count = self.t["count"].data_ptr()
+        self._graphs = {}
+
+    # ------------------------------------------------------------------ modules
+
+    def read_status(self):
+        self.host_syncs += 1
+        s = self.t["status"].cpu().numpy()
+        return A.PgStatus.from_buffer_copy(s.tobytes())
+
+    def rebuild(self):
+        by = C.byref
+        self.p.guard = None
+        A.call("pg_ensemble_bin", by(self.e), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
+        while True:
+            self.t["status"][0] = 0
+            self.t["status"][2] = 0
+            A.call("pg_ensemble_build_lists", by(self.e), by(self.p), by(self.cells), by(self.list), self.r_list2,
+                   self.status_ptr, self.sh)
+            st = self.read_status()
+            if st.nonfinite:
+                raise A.PairsError("non-finite particle position met while binning")
+            if st.overflow & 2:
+                self._alloc_list(int(st.max_neighbors * 1.15) + 8)
+                continue
+            break
+        self.t["status"][4] = INT32_MAX
+        self.nbuilds += 1
+        self._build_ts = self.ts
+
+    def _force(self, step):
+        self.p.step = step
+        A.call("pg_ensemble_force", C.byref(self.e), C.byref(self.p), C.byref(self.list), C.byref(self.lj), self.sh)
+
+    def _integrate(self, step, kicks, drift=1):
+        self.p.step = step
+        A.call("pg_ensemble_integrate", C.byref(self.e), C.byref(self.p), self.dt, kicks, drift, self.half_skin2,
+               step, self.status_ptr, self.sh)
+
+    def _chunk_launches(self, k):
+        """Steps 0..k-1 of a speculative chunk (relative step numbers)."""
+        self.p.guard = self.t["status"].data_ptr() + 4 * 4
+        for s in range(k):
+            self._integrate(s, 2)
+            self._force(s)
+        self.p.guard = None
+
+    def _run_chunk(self, k):
+        if not self.graphs:
+            self._chunk_launches(k)
+            return
+        g = self._graphs.get(k)
+        if g is None:
+            # first use of this length: capture it (the launches of the capture are
+            # not executed; the replay below runs them)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=self.stream):
+                self._chunk_launches(k)
+            self._graphs[k] = g
+        g.replay()
+
+    def run(self, nsteps):
+        """Advance every replica by nsteps time steps."""
+        target = self.ts + nsteps
+        with torch.cuda.stream(self.stream):
+            while self.ts < target:
+                if self.policy == "every" or not self._pending:
+                    # one plain step (every step with policy "every"; the first step
+                    # after step 0 otherwise, which owes no final half kick)
+                    self._integrate(self.ts, 2 if self._pending else 1)
+                    if self.policy == "every" or self.read_status().guard_tripped != INT32_MAX:
+                        self.rebuild()
+                    self._force(self.ts)
+                    self.ts += 1
+                    self._pending = True
+                    continue
+                # run up to one step past the predicted trip (the last cycle's length)
+                k = self.chunk or max(2, self._cycle - (self.ts - self._build_ts) + 1)
+                k = min(k, target - self.ts)
+                start = self.ts
+                self._run_chunk(k)
+                st = self.read_status()
+                g = st.guard_tripped
+                if g != INT32_MAX:
+                    # the device froze after the integration of relative step g: the
+                    # positions are those of step start + g; rebuild, then its force
+                    self.ts = start + g
+                    self._cycle = max(1, self.ts - self._build_ts)
+                    self.rebuild()
+                    self._force(self.ts)
+                    self.ts += 1
+                else:
+                    self.ts = start + k
+                    self._cycle = max(self._cycle, self.ts - self._build_ts)
+        return self
+
+    def synchronize(self):
+        self.stream.synchronize()
+
+    # ------------------------------------------------------------------ readout
+
+    def thermo(self):
+        """Per-replica temperature at the last completed step (the owed final half
+        kick is applied to a copy of the velocities)."""
+        with torch.cuda.stream(self.stream):
+            vel = self.t["vel"].clone()
+            if self._pending:
+                self._integrate(self.ts - 1, 1, drift=0)
+            A.call("pg_ensemble_thermo", C.byref(self.e), C.byref(self.p), C.c_void_p(self.t["thermo"].data_ptr()),
+                   self.sh)
+            out = self.t["thermo"].cpu().numpy().reshape(self.nrep, 2)
+            self.t["vel"].copy_(vel)
+        return out[:, 0].copy()
+
+    def replica_state(self, r):
+        """(pos, vel after the pending final kick is NOT applied, force) of replica r
+        in uid order."""
+        a, b = int(self.first[r]), int(self.first[r] + self.sizes[r])
+        uid = self.t["uid"][a:b].cpu().numpy()
+        order = np.argsort(uid, kind="stable")
+        pos = self.t["pos"][a:b, :3].cpu().numpy()[order]
+        vel = self.t["vel"][a:b, :3].cpu().numpy()[order]
+        frc = self.t["force32"][a:b, :3].cpu().numpy().astype(np.float64)[order]
+        return pos, vel, frc
+
+    def replica_pairs(self, r):
+        """Verlet entries (uid_i, uid_j, sx, sy, sz) of replica r, uids counted from the
+        replica's first particle."""
+        a, b = int(self.first[r]), int(self.first[r] + self.sizes[r])
+        cnt = self.t["count"].cpu().numpy()[a:b]
+        nbr = self.t["nbr"].cpu().numpy().astype(np.int64) & 0xFFFFFFFF
+        uid = self.t["uid"].cpu().numpy()
+        tpa, stride = self.tpa, self.n
+        kmax = int(cnt.max()) if len(cnt) else 0
+        k = np.arange(kmax)[:, None]
+        i = np.arange(a, b)[None, :]
+        mask = k < cnt[None, :]
+        idx = ((k // tpa) * stride + i) * tpa + k % tpa
+        e = nbr[idx[mask]]
+        ii = np.broadcast_to(i, mask.shape)[mask]
+        j = e & ((1 << A.NBR_INDEX_BITS) - 1)
+        code = e >> A.NBR_INDEX_BITS
+        dec = lambda c: np.where(c == 1, 1, np.where(c == 2, -1, 0))
+        return np.stack([uid[ii] - a, uid[j] - a, dec(code & 3), dec((code >> 2) & 3), dec((code >> 4) & 3)],
+                        axis=1).astype(np.int32)
+
+
+def autotune(replicas, candidates=None, steps=6, **kw):
+    """Time (tpa, block, reach) candidates on this ensemble: per candidate one list
+    build and `steps` force passes (CUDA events); score = force time + build time /
+    expected steps between rebuilds.  Returns (best, table)."""
+    if candidates is None:
+        candidates = [(t, b, r) for r in (1, 2) for t in (1, 2, 4, 8) for b in (128, 256)]
+    ens = Ensemble(replicas, graphs=False, **kw)
+    table = []
+    for tpa, block, reach in candidates:
+        ens.configure(tpa, block, reach)
+        with torch.cuda.stream(ens.stream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ens.stream)
+            ens.rebuild()
+            e1.record(ens.stream)
+            f = []
+            for _ in range(steps + 1):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(ens.stream)
+                ens._force(0)
+                b.record(ens.stream)
+                f.append((a, b))
+        ens.synchronize()
+        build = e0.elapsed_time(e1)
+        force = float(np.median([a.elapsed_time(b) for a, b in f[1:]]))
+        score = force + build / 8.0
+        table.append(dict(tpa=tpa, block=block, reach=reach, force_ms=force, build_ms=build, score=score))
+    best = min(table, key=lambda r: r["score"])
+    del ens
+    torch.cuda.empty_cache()
+    return (best["tpa"], best["block"], best["reach"]), table

@@ -227,3 +227,41 @@ def dem_sc_grid(xmax, ymax, zmax, spacing, diameter, min_diameter, max_diameter,
     return dict(pos=pts[keep].copy(), vel=vel, mass=mass, radius=rad, type=typ,
                 uid=(keep + 1).astype(np.int32), flags=np.zeros(n, np.int32), shape=np.zeros(n, np.int32))
 
+
+# ---------------------------------------------------------------------------- ensembles
+
+def trimmed_fcc(natoms, rho, temperature, uid0=0):
+    """One replica of the batched ensemble: the smallest n^3 fcc lattice with
+    4 n^3 >= natoms, its first `natoms` sites in the reference's visiting order,
+    rescaled into the cubic box L = (natoms / rho)^(1/3); reference velocity rule
+    (Park-Miller per site, zero momentum, rescaled to `temperature` over the kept
+    atoms), mass 1, one type."""
+    n = 1
+    while 4 * n ** 3 < natoms:
+        n += 1
+    i, j, k, _ = fcc_sites(n, n, n, 0.8442)
+    i, j, k = i[:natoms], j[:natoms], k[:natoms]
+    L = (natoms / rho) ** (1.0 / 3.0)
+    half = L / (2 * n)
+    pos = np.stack([half * i, half * j, half * k], axis=1)
+    seed = k * (2 * n) * (2 * n) + j * (2 * n) + i + 1
+    vel = np.empty_like(pos)
+    for c in range(3):
+        for _ in range(5):
+            seed, _v = _park_miller(seed)
+        seed, vel[:, c] = _park_miller(seed)
+    mass = np.ones(natoms)
+    box = np.array([L, L, L])
+    adjust_thermo(mass, vel, box, temperature)
+    return dict(pos=pos, vel=vel, mass=mass, type=np.zeros(natoms, np.int32),
+                uid=np.arange(uid0, uid0 + natoms, dtype=np.int32), box=box)
+
+
+def ensemble_configs(count=512, nmin=500, nmax=32000, rho=(0.6, 0.9), temperature=(0.7, 1.5), seed=2024):
+    """Replica sizes log-uniform in [nmin, nmax], densities and temperatures uniform,
+    from numpy's PCG64 with `seed`."""
+    g = np.random.default_rng(seed)
+    sizes = np.exp(g.uniform(np.log(nmin), np.log(nmax), count)).astype(np.int64)
+    rhos = g.uniform(rho[0], rho[1], count)
+    temps = g.uniform(temperature[0], temperature[1], count)
+    return [dict(natoms=int(s), rho=float(r), temperature=float(t)) for s, r, t in zip(sizes, rhos, temps)]
