@@ -95,12 +95,8 @@ class ClockSampler:
 
 
 def dist_setup():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-        return dist, int(os.environ["RANK"]), ws, int(os.environ.get("LOCAL_RANK", "0"))
-    return None, 0, 1, 0
+    from pairs_gb300.replicas import init_from_env
+    return init_from_env(os.environ)
 
 
 def traffic_from_profiles(kernel):
@@ -184,10 +180,12 @@ def run_ours(args, rank, world, dist):
         l0 = lib.pg_kernel_launches()
         c0 = dict(builds=eng.nbuilds, syncs=eng.host_syncs, rewinds=eng.rewinds, skipped=eng.skipped_steps)
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("timed")        # ncu --nvtx-include "timed/" selects these launches
         s0.record(stream)
         eng.run(steps)
         s1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         launches = lib.pg_kernel_launches() - l0
         eng.force = orig_force
         ms = s0.elapsed_time(s1)
@@ -204,11 +202,9 @@ def run_ours(args, rank, world, dist):
     clocks.start()
     ms, _, launches, counters = timed(eng, args.steps, args.warmup, force_events=False)
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n * args.steps * world / (ms / 1e3)
+    # whole job: the atoms all replicas advanced over the slowest rank's time
+    from pairs_gb300.replicas import job_throughput
+    value, ms = job_throughput(n * args.steps, ms, dist, device=dev)
     # force-kernel time for the roofline: a speculative policy issues passes that the
     # device skips after a guard trip, so time the kernel on its own on the settled
     # state (same stream, CUDA events around each launch)
@@ -417,6 +413,101 @@ def run_ensemble(args, rank, world, dist):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------------------------ DEM
+
+def granular_workload(count, seed=7):
+    """The granular DEM workload: `count` spheres, radii U[0.4, 0.6] mm, 2500 kg/m^3,
+    random non-overlapping positions (jittered lattice of spacing 1.2615 mm) in a
+    1:1:4 box periodic in x and y over a rigid plane at z = 0 (82 x 82 x 328 mm for
+    1M spheres, ~25% solid fraction), at rest under gravity."""
+    import math
+    from pairs_gb300 import lattice
+    s = 0.082 / 65
+    nx = 65 if count == 1000000 else int(math.ceil((count / 4.0) ** (1.0 / 3.0))) + 1
+    a = nx * s
+    box = (a, a, 4 * a)
+    st = lattice.dem_random_packing(count, box, 4e-4, 6e-4, 2500, seed=seed, spacing=s)
+    plane = dict(pos=np.zeros((1, 3)), vel=np.zeros((1, 3)), mass=np.ones(1), radius=np.zeros(1),
+                 type=np.zeros(1, np.int32), uid=np.array([count + 1], np.int32), flags=np.array([13], np.int32),
+                 shape=np.ones(1, np.int32), normal=np.array([[0.0, 0.0, 1.0]]))
+    state = {k: np.concatenate([st[k] if k in st else np.zeros((count, 3)), plane[k]]) for k in plane}
+    e, nu = 0.7, 0.22
+    consts = dict(dt=1e-6, kappa=2.0 * (1.0 - nu) / (2.0 - nu), ln_e=math.log(e), tc=5e-4, drho=2500.0,
+                  gravity=9.81, mu=0.5, kn=1e5)
+    return box, state, consts
+
+
+def run_dem(args, rank, world, dist):
+    """Granular DEM workload on one GB300: mixed precision (FP64 contact geometry,
+    FP32 contact model, FP64 integration) against the FP64 path, particle-steps/s."""
+    import torch
+    from pairs_gb300 import _capi as A
+    from pairs_gb300.dem import DEMEngine, dem_params
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    count = args.dem_spheres
+    box, state, c = granular_workload(count)
+    prm = lambda: dem_params(c["dt"], c["kappa"], c["ln_e"], c["tc"], c["drho"], c["gravity"], [0.0], [c["mu"]],
+                             kn=c["kn"])
+    lib = A.load()
+
+    def timed(precision, steps):
+        eng = DEMEngine(state, lo=[0, 0, 0], hi=box, periodic=(True, True, False), params=prm(),
+                        precision=precision, skin=1e-4)
+        eng.run(args.warmup)
+        torch.cuda.synchronize()
+        l0, b0 = lib.pg_kernel_launches(), eng.nbuilds
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        eng.run(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        ncont = int(eng.sets[0]["ccount"][:eng.n].sum().item())
+        out = dict(value=(count + 1) * steps / (ms / 1e3), ms_per_step=ms / steps, steps=steps,
+                   rebuilds=eng.nbuilds - b0, launches=lib.pg_kernel_launches() - l0, contacts_at_end=ncont)
+        del eng
+        torch.cuda.empty_cache()
+        return out
+
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    mixed = timed("mixed", args.steps)
+    clk = clocks.stop()
+    fp64 = timed("fp64", max(10, args.steps // 5))
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import dem as odem
+        n_cpu = 20000
+        cbox, cstate, _ = granular_workload(n_cpu)
+        spheres = {k: cstate[k][:n_cpu] for k in ("uid", "type", "mass", "radius", "pos", "vel")}
+        p = dict(dt=c["dt"], kappa=c["kappa"], ln_e=c["ln_e"], tc=c["tc"], rho_p=2500, rho_f=0,
+                 gravity=c["gravity"], mu=c["mu"], cell=1.01 * 1.2e-3)
+        sim = odem.Sim(cbox, [[n_cpu + 1, 0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 13]], p, spheres=spheres, kn=c["kn"])
+        sim.run(5)
+        k = 100
+        t0 = time.perf_counter()
+        sim.run(k)
+        el = time.perf_counter() - t0
+        cpu = {"value": (n_cpu + 1) * k / el, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+               "sample": f"{k} steps of a {n_cpu}-sphere version of the workload with oracle/dem_oracle.c "
+                         "(the reference's DEM program restated: every step rebins and scans 27 cells)"}
+    line = {
+        "metric": "particle-steps/s of the granular DEM workload on 1 GB300", "value": mixed["value"],
+        "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mixed["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 geometry + f32 contact model / f64 integrate",
+        "data": "synthetic (seeded random non-overlapping spheres, at rest)",
+        "config": {"workload": f"{count} spheres r U[0.4,0.6] mm, 2500 kg/m^3, box {box[0]*1e3:.1f} x "
+                               f"{box[1]*1e3:.1f} x {box[2]*1e3:.1f} mm periodic x,y, plane z=0, gravity, kn 1e5 N/m, "
+                               "e 0.7, kt = kappa kn (nu 0.22), Coulomb mu 0.5 with history, dt 1e-6 s",
+                   "spheres": count},
+        "mixed": mixed, "fp64": fp64, "speedup_mixed_vs_fp64": mixed["value"] / fp64["value"],
+        "gpu_launches": mixed["launches"], "clocks": clk, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
 # ------------------------------------------------------------------------------ reference arm
 
 def run_reference(args, rank, world, dist):
@@ -462,7 +553,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble"], default="lj64")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble", "dem"], default="lj64")
+    ap.add_argument("--dem-spheres", type=int, default=1000000, help="dem workload: number of spheres")
     ap.add_argument("--replicas", type=int, default=512, help="ensemble workload: number of replicas")
     ap.add_argument("--one-by-one-steps", type=int, default=100,
                     help="ensemble workload: steps per replica of the one-by-one comparison")
@@ -486,6 +578,8 @@ def main():
         run_reference(args, rank, world, dist)
     elif args.workload == "ensemble":
         run_ensemble(args, rank, world, dist)
+    elif args.workload == "dem":
+        run_dem(args, rank, world, dist)
     else:
         run_ours(args, rank, world, dist)
     if dist:

@@ -111,14 +111,19 @@ typedef struct {
      * step < `step`.  The host later rebuilds at the tripped step and resumes. */
     const int32_t *guard;
     int32_t step;
-    int32_t pad_;
+    int32_t hilo_stride;         /* 0 or 1: pos_hi and pos_lo are separate float4 arrays;
+                                    2: one interleaved array (hi, lo of a particle in one
+                                    32-byte record), pos_lo = pos_hi + 4 floats */
 } pg_particles;
 
 /* Cell grid over the box, counting-sort layout (cell_start/cell_count). */
 typedef struct {
     int32_t dims[3];
     int32_t ncells;
-    double  cell_len[3];         /* len[d] / dims[d] >= list radius */
+    int32_t reach;               /* Verlet build stencil: cells within `reach` per axis (27 cells
+                                    for 1, 125 for 2); 0 is taken as 1 */
+    int32_t pad_;
+    double  cell_len[3];         /* len[d] / dims[d] >= list radius / reach */
     int32_t *cell_start;         /* [ncells + 2]: cells, then the bucket of infinite shapes */
     int32_t *cell_count;         /* [ncells + 1] */
     int32_t *particle_cell;      /* [capacity] */
@@ -219,6 +224,9 @@ typedef struct {
     int32_t *type;               /* [capacity] */
     int32_t *flags;              /* [capacity] 1 infinite, 4 fixed, 8 global */
     int32_t *shape;              /* [capacity] 0 sphere, 1 half space */
+    float   *pos32;              /* float4[capacity] (x, y, z, radius) in FP32, or NULL; kept
+                                    by the list build and Euler for the mixed-precision
+                                    contact kernel's candidate screen */
     const int32_t *guard;        /* speculative stepping, as pg_particles.guard */
     int32_t step;
     int32_t pad_;
@@ -249,6 +257,9 @@ typedef struct {
     double drho;                 /* densityParticle - densityFluid, in the symbols' type */
     double gravity;
     double skin;                 /* Verlet list skin (list radius r_i + r_j + skin) */
+    double kn;                   /* 0: normal stiffness from the collision time tc, as the
+                                    example; > 0: this fixed stiffness, damping
+                                    -2 ln_e sqrt(meff kn) / sqrt(pi^2 + ln_e^2) */
     int32_t ntypes;              /* <= 4 */
     int32_t pad_;
     double friction_static[16];  /* [ti * ntypes + tj] */
@@ -451,11 +462,12 @@ int pg_dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *ce
  * contact (examples/dem.py:18-74) against spheres (list) and half spaces (trailing
  * bucket), with contact-history lookup/creation by partner uid
  * (mapping/funcs.py:230-265) and removal of the records not used this step
- * (sim/contact_history.py:91-127).  Writes force and torque (FP64, the generated
- * operation order).  Overflow bit 3: a particle needed more than c->capacity records. */
+ * (sim/contact_history.py:91-127).  Writes force and torque.  precision PG_FP64:
+ * the generated operation order; PG_MIXED: FP64 contact geometry, FP32 contact
+ * model and sums.  Overflow bit 3: a particle needed more than c->capacity records. */
 int pg_dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cells,
                  const pg_neighbor_list *list, const pg_contacts *c, const pg_dem_params *prm,
-                 pg_status *status, void *stream);
+                 int precision, pg_status *status, void *stream);
 
 /* Explicit Euler with rotation (examples/dem.py:77-87), skipping fixed particles,
  * plus the FP64 displacement guard against pos_ref (first step with a displacement

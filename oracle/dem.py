@@ -36,6 +36,7 @@ def lib():
         L.dem_nlocal.argtypes = [C.c_void_p]
         L.dem_get.argtypes = [C.c_void_p, C.c_int, _ip] + [C.c_void_p] * 7
         L.dem_get_initial.argtypes = [C.c_void_p] + [C.c_void_p] * 9
+        L.dem_set_normal_stiffness.argtypes = [C.c_void_p, C.c_double]
         L.dem_contacts.restype = C.c_long
         L.dem_contacts.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long]
         _lib = L
@@ -58,18 +59,33 @@ def example_params(**over):
 class Sim:
     """The reference's DEM time loop on one rank (see dem_oracle.c header)."""
 
-    def __init__(self, domain_size, planes, params=None, cap=None, history_fixed=False, ccap=20):
+    def __init__(self, domain_size, planes, params=None, cap=None, history_fixed=False, ccap=20, spheres=None,
+                 kn=0.0):
+        """spheres: None for the example's dem_sc_grid, else a dict of arrays (uid,
+        type, mass, radius, pos, vel) added in that order.  kn > 0: fixed normal
+        stiffness (damping from the restitution coefficient)."""
         p = params or example_params()
         self.p = p
         lo = np.zeros(3)
         hi = np.asarray(domain_size, dtype=np.float64)
-        cap = cap or 200000
+        cap = cap or max(200000, 2 * (len(spheres["pos"]) if spheres is not None else 0) + 1000)
         fs = np.zeros(1); fd = np.array([p["mu"]])
         self._h = lib().dem_create(cap, lo, hi, np.array([1, 1, 0], dtype=np.int32), p["cell"], p["dt"], math.pi,
                                    p["kappa"], p["ln_e"], p["tc"], p["rho_p"], p["rho_f"], p["gravity"], 1, fs, fd,
                                    ccap, int(history_fixed))
-        d = p["diameter"]
-        lib().dem_sc_grid(self._h, hi[0], hi[1], hi[2], p["spacing"], d, d * 0.9, d * 1.1, p["v0"], p["rho_p"], 1)
+        if kn:
+            lib().dem_set_normal_stiffness(self._h, float(kn))
+        if spheres is None:
+            d = p["diameter"]
+            lib().dem_sc_grid(self._h, hi[0], hi[1], hi[2], p["spacing"], d, d * 0.9, d * 1.1, p["v0"], p["rho_p"],
+                              1)
+        else:
+            for k in range(len(spheres["pos"])):
+                pos = np.ascontiguousarray(spheres["pos"][k], dtype=np.float64)
+                vel = np.ascontiguousarray(spheres["vel"][k], dtype=np.float64)
+                lib().dem_add_particle(self._h, int(spheres["uid"][k]), int(spheres["type"][k]),
+                                       float(spheres["mass"][k]), float(spheres["radius"][k]), pos, vel.ctypes.data,
+                                       None, 0, 0)
         for pl in planes:
             uid, typ, mass = int(pl[0]), int(pl[1]), float(pl[2])
             pos = np.array(pl[3:6], dtype=np.float64)

@@ -104,6 +104,7 @@ typedef struct {
     int pbc[3];
     double spacing;              /* cell size (linkedCellWidth) */
     double dt, pi, kappa, ln_e, tc;
+    double kn_fixed;             /* > 0: fixed normal stiffness (see dem_set_normal_stiffness) */
     double rho_p, rho_f, g;
     int ntypes;
     double fs[16], fd[16];       /* friction_static / friction_dynamic feature tables */
@@ -188,6 +189,10 @@ dem_sim *dem_create(int cap, const double *lo, const double *hi, const int *pbc,
     s->cell_particles = dcalloc((size_t) s->ncells * s->cell_cap, sizeof(int));
     return s;
 }
+
+/* Fixed normal stiffness (the batched DEM workload's contact model: k_n given
+ * directly instead of through the collision time; 0 restores the example's model). */
+void dem_set_normal_stiffness(dem_sim *s, double kn) { s->kn_fixed = kn; }
 
 /* ---- initial state ---------------------------------------------------------- */
 
@@ -535,7 +540,12 @@ static void spring_dashpot(dem_sim *s, int i, int j, int cid, const double *n, c
     const double lrt = sqrt(relt[0] * relt[0] + relt[1] * relt[1] + relt[2] * relt[2]);
     const int cond1a = (sticking == 1) && (lrt < 1e-08);
     const double meff = 1.0 / (inv_mi + (1.0 / s->mass[j]));
-    const double kn = (meff * ((s->pi * s->pi) + (s->ln_e * s->ln_e))) / (s->tc * s->tc);
+    double kn;
+    if(s->kn_fixed > 0.0) {
+        kn = s->kn_fixed;
+    } else {
+        kn = (meff * ((s->pi * s->pi) + (s->ln_e * s->ln_e))) / (s->tc * s->tc);
+    }
     const double kt = s->kappa * kn;
     double tsd0[3], rot[3], sel1[3], nts[3], fTLS[3], fN[3], t[3];
     for(int e = 0; e < 3; e++) { tsd0[e] = s->tsd[a * 3 + e]; }
@@ -548,7 +558,12 @@ static void spring_dashpot(dem_sim *s, int i, int j, int cid, const double *n, c
         sel1[e] = (rl2 <= 0.0) ? 0.0 : rot[e] * sc;
         nts[e] = s->dt * relt[e] + sel1[e];
     }
-    const double dn = ((-(2.0)) * meff) * s->ln_e / s->tc;
+    /* normal damping: from the collision time (examples/dem.py:26), or with a fixed
+     * stiffness the same restitution relation solved for the damping,
+     * -2 ln(e) sqrt(meff kn) / sqrt(pi^2 + ln(e)^2) */
+    const double dn = s->kn_fixed > 0.0
+        ? (((-(2.0)) * s->ln_e) * sqrt(meff * kn)) / sqrt((s->pi * s->pi) + (s->ln_e * s->ln_e))
+        : ((-(2.0)) * meff) * s->ln_e / s->tc;
     const double dtn = sqrt(s->kappa) * dn;
     for(int e = 0; e < 3; e++) { fTLS[e] = kt * nts[e] + dtn * relt[e]; }
     const double fTLS_len = sqrt(fTLS[0] * fTLS[0] + fTLS[1] * fTLS[1] + fTLS[2] * fTLS[2]);

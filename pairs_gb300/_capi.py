@@ -46,11 +46,12 @@ class PgParticles(C.Structure):
                 ("pos_hi", C.c_void_p), ("pos_lo", C.c_void_p), ("pos_ref", C.c_void_p),
                 ("ref_hi", C.c_void_p), ("ref_lo", C.c_void_p),
                 ("mass", C.c_void_p), ("type", C.c_void_p), ("uid", C.c_void_p),
-                ("flags", C.c_void_p), ("guard", C.c_void_p), ("step", C.c_int32), ("pad_", C.c_int32)]
+                ("flags", C.c_void_p), ("guard", C.c_void_p), ("step", C.c_int32), ("hilo_stride", C.c_int32)]
 
 
 class PgCells(C.Structure):
-    _fields_ = [("dims", C.c_int32 * 3), ("ncells", C.c_int32), ("cell_len", C.c_double * 3),
+    _fields_ = [("dims", C.c_int32 * 3), ("ncells", C.c_int32), ("reach", C.c_int32), ("pad_", C.c_int32),
+                ("cell_len", C.c_double * 3),
                 ("cell_start", C.c_void_p), ("cell_count", C.c_void_p),
                 ("particle_cell", C.c_void_p)]
 
@@ -80,7 +81,7 @@ class PgDemParticles(C.Structure):
                 ("torque", C.c_void_p), ("quat", C.c_void_p), ("normal", C.c_void_p), ("pos_ref", C.c_void_p),
                 ("mass", C.c_void_p), ("radius", C.c_void_p), ("inv_inertia", C.c_void_p),
                 ("uid", C.c_void_p), ("type", C.c_void_p), ("flags", C.c_void_p), ("shape", C.c_void_p),
-                ("guard", C.c_void_p), ("step", C.c_int32), ("pad_", C.c_int32)]
+                ("pos32", C.c_void_p), ("guard", C.c_void_p), ("step", C.c_int32), ("pad_", C.c_int32)]
 
 
 class PgContacts(C.Structure):
@@ -91,6 +92,7 @@ class PgContacts(C.Structure):
 class PgDemParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("pi", C.c_double), ("kappa", C.c_double), ("ln_e", C.c_double),
                 ("tc", C.c_double), ("drho", C.c_double), ("gravity", C.c_double), ("skin", C.c_double),
+                ("kn", C.c_double),
                 ("ntypes", C.c_int32), ("pad_", C.c_int32),
                 ("friction_static", C.c_double * 16), ("friction_dynamic", C.c_double * 16)]
 
@@ -158,7 +160,7 @@ SIGNATURES = {
     "pg_dem_build_list": (C.c_int, [P(PgBox), P(PgDemParticles), P(PgCells), P(PgNeighborList), P(PgDemParams),
                                     C.c_void_p, C.c_void_p]),
     "pg_dem_force": (C.c_int, [P(PgBox), P(PgDemParticles), P(PgCells), P(PgNeighborList), P(PgContacts),
-                               P(PgDemParams), C.c_void_p, C.c_void_p]),
+                               P(PgDemParams), C.c_int, C.c_void_p, C.c_void_p]),
     "pg_dem_euler": (C.c_int, [P(PgDemParticles), P(PgDemParams), C.c_double, C.c_int32, C.c_void_p,
                                C.c_void_p]),
 }

@@ -46,7 +46,7 @@ int dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spar
 int dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *cells, pg_neighbor_list *list,
                    const pg_dem_params *prm, pg_status *status, cudaStream_t st);
 int dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cells, const pg_neighbor_list *list,
-              const pg_contacts *c, const pg_dem_params *prm, pg_status *status, cudaStream_t st);
+              const pg_contacts *c, const pg_dem_params *prm, int precision, pg_status *status, cudaStream_t st);
 int dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step, pg_status *status,
               cudaStream_t st);
 }  // namespace pg
@@ -175,8 +175,8 @@ int pg_dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *ce
 
 int pg_dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cells,
                  const pg_neighbor_list *list, const pg_contacts *c, const pg_dem_params *prm,
-                 pg_status *status, void *stream) {
-    return pg::dem_force(box, d, cells, list, c, prm, status, S(stream));
+                 int precision, pg_status *status, void *stream) {
+    return pg::dem_force(box, d, cells, list, c, prm, precision, status, S(stream));
 }
 
 int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step,

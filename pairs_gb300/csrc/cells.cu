@@ -182,8 +182,8 @@ __global__ void k_split_positions(pg_box box, pg_particles p) {
     split_pos(x.z, iq, q, h.z, l.z);
     h.w = __int_as_float(p.type != nullptr ? p.type[i] : 0);
     l.w = 0.0f;
-    st_f4(p.pos_hi, i, h);
-    st_f4(p.pos_lo, i, l);
+    st_f4(p.pos_hi, hl(p, i), h);
+    st_f4(p.pos_lo, hl(p, i), l);
 }
 
 // workspace layout for pg_bin_particles (all offsets 256-byte aligned)

@@ -92,6 +92,9 @@ __device__ __forceinline__ double ref_rsq(double dx, double dy, double dz) {
 // |hi| < 2^24 q): differences of hi values and of hi and len_hi are exact in FP32.
 // lo = x - hi in FP32 (|lo| <= q/2).
 
+// float4 index of particle i in pos_hi / pos_lo (interleaved records: stride 2)
+__device__ __forceinline__ int hl(const pg_particles &p, int i) { return p.hilo_stride == 2 ? 2 * i : i; }
+
 __device__ __forceinline__ void split_pos(double x, double inv_q, double q, float &hi, float &lo) {
     const double h = rint(x * inv_q) * q;
     hi = (float) h;

@@ -10,7 +10,9 @@
 //   euler                    examples/dem.py:77-87 with the quaternion keywords of
 //                            mapping/keywords.py:208-259
 // with the generated operation order.  This file is compiled with -fmad=false so
-// every FP64 operation is separately rounded, as in the reference's C code.
+// every FP64 operation is separately rounded, as in the reference's C code.  A
+// mixed-precision contact kernel (FP64 geometry, FP32 contact model) serves large
+// granular workloads.
 //
 // GPU organisation: one thread per particle.  Each particle owns its contact
 // records (partner uid, sticking flag, tangential spring displacement, impact
@@ -39,6 +41,7 @@ struct DemArgs {
     pg_status *status;
     double half_skin2;
     int32_t step;
+    float screen;                // FP32 candidate screen margin (metres), mixed kernel
 };
 
 __device__ __forceinline__ D4 ldd(const double *b, int i) { return ld_d4_plain(b, i); }
@@ -104,6 +107,9 @@ __global__ void __launch_bounds__(kBlock) k_dem_list(DemArgs a) {
     if(i >= a.d.n) { return; }
     const D4 xi = ldd(a.d.pos, i);
     st_d4(a.d.pos_ref, i, xi);
+    if(a.d.pos32 != nullptr) {
+        st_f4(a.d.pos32, i, make_float4((float) xi.x, (float) xi.y, (float) xi.z, (float) a.d.radius[i]));
+    }
     int cnt = 0;
     const int ci = a.cells.particle_cell[i];
     if(ci < a.cells.ncells && a.d.shape[i] == 0) {
@@ -155,69 +161,79 @@ __global__ void __launch_bounds__(kBlock) k_dem_list(DemArgs a) {
 
 // ------------------------------------------------------------------ contact model
 
-// One contact's spring-dashpot update, examples/dem.py:18-74 once the geometry
-// (normal n, contact point cp, overlap delta) is known.  h is the contact's record
-// (tangential spring displacement in x, y, z; impact velocity magnitude in w).
-__device__ void spring_dashpot(const pg_dem_params &p, double inv_mi, double mj, int tij, const D4 &xi,
-                               const D4 &xj, const D4 &vi, const D4 &vj, const D4 &wi, const D4 &wj,
-                               const double n[3], const double cp[3], double delta, int &sticking, D4 &h,
-                               double facc[3], double tacc[3]) {
-    const double ri[3] = {cp[0] - xi.x, cp[1] - xi.y, cp[2] - xi.z};
-    const double rj[3] = {cp[0] - xj.x, cp[1] - xj.y, cp[2] - xj.z};
-    double vwi[3], vwj[3], rel[3], reln[3], relt[3];
-    vwi[0] = vi.x + (wi.y * ri[2] - wi.z * ri[1]);
-    vwi[1] = vi.y + (wi.z * ri[0] - wi.x * ri[2]);
-    vwi[2] = vi.z + (wi.x * ri[1] - wi.y * ri[0]);
-    vwj[0] = vj.x + (wj.y * rj[2] - wj.z * rj[1]);
-    vwj[1] = vj.y + (wj.z * rj[0] - wj.x * rj[2]);
-    vwj[2] = vj.z + (wj.x * rj[1] - wj.y * rj[0]);
+// One contact's spring-dashpot update, examples/dem.py:18-74 once the geometry is
+// known: normal n, overlap delta, and the contact point relative to both centres
+// (ri = cp - x_i, rj = cp - x_j).  h is the contact's record (tangential spring
+// displacement in x, y, z; impact velocity magnitude in w).  T = double follows the
+// generated operation order; T = float is the mixed-precision contact model (the
+// overlap itself comes from FP64 geometry, see k_dem_force_mixed).
+template<typename T>
+__device__ void spring_dashpot(const pg_dem_params &p, T inv_mi, T mj, int tij, const T vi[3], const T vj[3],
+                               const T wi[3], const T wj[3], const T n[3], const T ri[3], const T rj[3], T delta,
+                               int &sticking, T h[4], T facc[3], T tacc[3]) {
+    T vwi[3], vwj[3], rel[3], reln[3], relt[3];
+    vwi[0] = vi[0] + (wi[1] * ri[2] - wi[2] * ri[1]);
+    vwi[1] = vi[1] + (wi[2] * ri[0] - wi[0] * ri[2]);
+    vwi[2] = vi[2] + (wi[0] * ri[1] - wi[1] * ri[0]);
+    vwj[0] = vj[0] + (wj[1] * rj[2] - wj[2] * rj[1]);
+    vwj[1] = vj[1] + (wj[2] * rj[0] - wj[0] * rj[2]);
+    vwj[2] = vj[2] + (wj[0] * rj[1] - wj[1] * rj[0]);
     for(int e = 0; e < 3; e++) { rel[e] = -(vwi[e] - vwj[e]); }
-    const double vn = rel[0] * n[0] + rel[1] * n[1] + rel[2] * n[2];
+    const T vn = rel[0] * n[0] + rel[1] * n[1] + rel[2] * n[2];
     for(int e = 0; e < 3; e++) { reln[e] = vn * n[e]; relt[e] = rel[e] - reln[e]; }
-    const double lrt = sqrt(relt[0] * relt[0] + relt[1] * relt[1] + relt[2] * relt[2]);
-    const bool cond1a = (sticking == 1) && (lrt < 1e-08);
-    const double meff = 1.0 / (inv_mi + (1.0 / mj));
-    const double kn = (meff * ((p.pi * p.pi) + (p.ln_e * p.ln_e))) / (p.tc * p.tc);
-    const double kt = p.kappa * kn;
-    const double tsd0[3] = {h.x, h.y, h.z};
-    const double proj = tsd0[0] * n[0] + tsd0[1] * n[1] + tsd0[2] * n[2];
-    double rot[3], nts[3], fTLS[3], fN[3], t[3];
-    for(int e = 0; e < 3; e++) { rot[e] = tsd0[e] - n[e] * proj; }
-    const double rl2 = rot[0] * rot[0] + rot[1] * rot[1] + rot[2] * rot[2];
-    const double tl2 = tsd0[0] * tsd0[0] + tsd0[1] * tsd0[1] + tsd0[2] * tsd0[2];
-    const double sc = sqrt(tl2 / rl2);
-    for(int e = 0; e < 3; e++) {
-        const double sel = (rl2 <= 0.0) ? 0.0 : rot[e] * sc;
-        nts[e] = p.dt * relt[e] + sel;
+    const T lrt = sqrt(relt[0] * relt[0] + relt[1] * relt[1] + relt[2] * relt[2]);
+    const bool cond1a = (sticking == 1) && (lrt < T(1e-08));
+    const T meff = T(1.0) / (inv_mi + (T(1.0) / mj));
+    const T pi = T(p.pi), ln_e = T(p.ln_e), kappa = T(p.kappa), dt = T(p.dt);
+    T kn, dn;
+    if(p.kn > 0.0) {
+        // fixed normal stiffness; damping from the restitution relation
+        kn = T(p.kn);
+        dn = (((-(T(2.0))) * ln_e) * sqrt(meff * kn)) / sqrt((pi * pi) + (ln_e * ln_e));
+    } else {
+        const T tc = T(p.tc);
+        kn = (meff * ((pi * pi) + (ln_e * ln_e))) / (tc * tc);
+        dn = ((-(T(2.0))) * meff) * ln_e / tc;
     }
-    const double dn = ((-(2.0)) * meff) * p.ln_e / p.tc;
-    const double dtn = sqrt(p.kappa) * dn;
+    const T kt = kappa * kn;
+    const T tsd0[3] = {h[0], h[1], h[2]};
+    const T proj = tsd0[0] * n[0] + tsd0[1] * n[1] + tsd0[2] * n[2];
+    T rot[3], nts[3], fTLS[3], fN[3], t[3];
+    for(int e = 0; e < 3; e++) { rot[e] = tsd0[e] - n[e] * proj; }
+    const T rl2 = rot[0] * rot[0] + rot[1] * rot[1] + rot[2] * rot[2];
+    const T tl2 = tsd0[0] * tsd0[0] + tsd0[1] * tsd0[1] + tsd0[2] * tsd0[2];
+    const T sc = sqrt(tl2 / rl2);
+    for(int e = 0; e < 3; e++) {
+        const T sel = (rl2 <= T(0.0)) ? T(0.0) : rot[e] * sc;
+        nts[e] = dt * relt[e] + sel;
+    }
+    const T dtn = sqrt(kappa) * dn;
     for(int e = 0; e < 3; e++) { fTLS[e] = kt * nts[e] + dtn * relt[e]; }
-    const double fTLS_len = sqrt(fTLS[0] * fTLS[0] + fTLS[1] * fTLS[1] + fTLS[2] * fTLS[2]);
-    const double kd = kn * delta;
+    const T fTLS_len = sqrt(fTLS[0] * fTLS[0] + fTLS[1] * fTLS[1] + fTLS[2] * fTLS[2]);
+    const T kd = kn * delta;
     for(int e = 0; e < 3; e++) { fN[e] = kd * n[e] + dn * reln[e]; }
-    const double fNl = sqrt(fN[0] * fN[0] + fN[1] * fN[1] + fN[2] * fN[2]);
-    const double fstat = p.friction_static[tij] * fNl;
+    const T fNl = sqrt(fN[0] * fN[0] + fN[1] * fN[1] + fN[2] * fN[2]);
+    const T fstat = T(p.friction_static[tij]) * fNl;
     const bool cond1 = cond1a && (fTLS_len < fstat);
-    const double fdyn = p.friction_dynamic[tij] * fNl;
+    const T fdyn = T(p.friction_dynamic[tij]) * fNl;
     const bool cond2 = (sticking == 1) && (fTLS_len < fdyn);
-    const bool slide = (!cond1 && !cond2) && (kt > 0.0);
-    const double ffa = cond1 ? fstat : fdyn;
-    const double tl = sqrt(fTLS[0] * fTLS[0] + fTLS[1] * fTLS[1] + fTLS[2] * fTLS[2]);
-    const double itl = 1.0 / tl;
-    for(int e = 0; e < 3; e++) { t[e] = (tl > 0.0) ? fTLS[e] * itl : 0.0; }
-    double nt[3];
+    const bool slide = (!cond1 && !cond2) && (kt > T(0.0));
+    const T ffa = cond1 ? fstat : fdyn;
+    const T tl = sqrt(fTLS[0] * fTLS[0] + fTLS[1] * fTLS[1] + fTLS[2] * fTLS[2]);
+    const T itl = T(1.0) / tl;
+    for(int e = 0; e < 3; e++) { t[e] = (tl > T(0.0)) ? fTLS[e] * itl : T(0.0); }
+    T nt[3];
     for(int e = 0; e < 3; e++) { nt[e] = slide ? ((ffa * t[e]) - (dtn * relt[e])) / kt : nts[e]; }
-    const double lrel = sqrt(rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2]);
-    const double ivm = (h.w > 0.0) ? h.w : lrel;
-    h = make_d4(nt[0], nt[1], nt[2], ivm);
+    const T lrel = sqrt(rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2]);
+    const T ivm = (h[3] > T(0.0)) ? h[3] : lrel;
+    h[0] = nt[0]; h[1] = nt[1]; h[2] = nt[2]; h[3] = ivm;
     sticking = ((cond1 || cond2) || (fTLS_len < fdyn)) ? 1 : 0;
-    const double fTabs = (ffa < fTLS_len) ? ffa : fTLS_len;
-    double pf[3];
+    const T fTabs = (ffa < fTLS_len) ? ffa : fTLS_len;
+    T pf[3];
     for(int e = 0; e < 3; e++) { pf[e] = fN[e] + fTabs * t[e]; facc[e] = facc[e] + pf[e]; }
-    const double c0 = (cp[1] - xi.y) * pf[2] - (cp[2] - xi.z) * pf[1];
-    const double c1 = (cp[2] - xi.z) * pf[0] - (cp[0] - xi.x) * pf[2];
-    const double c2 = (cp[0] - xi.x) * pf[1] - (cp[1] - xi.y) * pf[0];
+    const T c0 = ri[1] * pf[2] - ri[2] * pf[1];
+    const T c1 = ri[2] * pf[0] - ri[0] * pf[2];
+    const T c2 = ri[0] * pf[1] - ri[1] * pf[0];
     tacc[0] = tacc[0] + c0;
     tacc[1] = tacc[1] + c1;
     tacc[2] = tacc[2] + c2;
@@ -243,84 +259,29 @@ __device__ __forceinline__ int dem_slot(const pg_contacts &c, int i, int uj, int
     return id;
 }
 
-__device__ __forceinline__ void dem_contact(const DemArgs &a, int i, int j, const D4 &xi, const D4 &xj,
-                                            const D4 &vi, const D4 &wi, double inv_mi, int ti, const double n[3],
-                                            const double cp[3], double delta, int &nc, uint32_t used[2],
-                                            bool &overflow, double f[3], double t[3]) {
+// Look up / create the contact record of partner j, run the model in precision T,
+// store the record back.
+template<typename T>
+__device__ __forceinline__ void dem_contact(const DemArgs &a, int i, int j, const T vi[3], const T wi[3],
+                                            T inv_mi, int ti, const T n[3], const T ri[3], const T rj[3], T delta,
+                                            int &nc, uint32_t used[2], bool &overflow, T f[3], T t[3]) {
     const int slot = dem_slot(a.c, i, a.d.uid[j], nc, used);
     if(slot < 0) { overflow = true; return; }
     const size_t s = (size_t) slot * a.c.stride + i;
     int sticking = a.c.sticking[s];
-    D4 h = ldd(a.c.history, (int) s);
+    const D4 hd = ldd(a.c.history, (int) s);
+    T h[4] = {T(hd.x), T(hd.y), T(hd.z), T(hd.w)};
     const int tij = ti * a.prm.ntypes + (a.d.type ? a.d.type[j] : 0);
-    spring_dashpot(a.prm, inv_mi, a.d.mass[j], tij, xi, xj, vi, ldd(a.d.vel, j), wi, ldd(a.d.angvel, j), n, cp,
-                   delta, sticking, h, f, t);
+    const D4 vj4 = ldd(a.d.vel, j), wj4 = ldd(a.d.angvel, j);
+    const T vj[3] = {T(vj4.x), T(vj4.y), T(vj4.z)}, wj[3] = {T(wj4.x), T(wj4.y), T(wj4.z)};
+    spring_dashpot<T>(a.prm, inv_mi, T(a.d.mass[j]), tij, vi, vj, wi, wj, n, ri, rj, delta, sticking, h, f, t);
     a.c.sticking[s] = sticking;
-    st_d4(a.c.history, (int) s, h);
+    st_d4(a.c.history, (int) s, make_d4(h[0], h[1], h[2], h[3]));
 }
 
-__global__ void __launch_bounds__(kDemBlock) k_dem_force(DemArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= a.d.n || dem_frozen(a.d, false)) { return; }
-    if(a.d.flags != nullptr && (a.d.flags[i] & kFlagFixed)) {
-        st_d4(a.d.force, i, make_d4(0.0, 0.0, 0.0, 0.0));
-        st_d4(a.d.torque, i, make_d4(0.0, 0.0, 0.0, 0.0));
-        a.c.count[i] = 0;
-        return;
-    }
-    const D4 xi = ldd(a.d.pos, i), vi = ldd(a.d.vel, i), wi = ldd(a.d.angvel, i);
-    const double ri = a.d.radius[i];
-    const double inv_mi = 1.0 / a.d.mass[i];
-    const int ti = a.d.type ? a.d.type[i] : 0;
-    int nc = a.c.count[i];
-    uint32_t used[2] = {0u, 0u};
-    double fs[3] = {0, 0, 0}, ts[3] = {0, 0, 0}, fh[3] = {0, 0, 0}, th[3] = {0, 0, 0};
-    bool overflow = false;
-    // sphere-sphere (sim/interaction.py:234-246)
-    const int cnt = a.list.count[i];
-    for(int k = 0; k < cnt; k++) {
-        const uint32_t e = (uint32_t) a.list.nbr[(size_t) k * a.list.stride + i];
-        const int j = (int) (e & PG_NBR_INDEX_MASK);
-        const uint32_t code = e >> PG_NBR_INDEX_BITS;
-        D4 xj = ldd(a.d.pos, j);
-        if(code != 0u) {
-            xj.x = ref_image(xj.x, image_shift(code, 0), a.box.len[0]);
-            xj.y = ref_image(xj.y, image_shift(code, 1), a.box.len[1]);
-            xj.z = ref_image(xj.z, image_shift(code, 2), a.box.len[2]);
-        }
-        const double d0 = xi.x - xj.x, d1 = xi.y - xj.y, d2 = xi.z - xj.z;
-        const double rsq = d0 * d0 + d1 * d1 + d2 * d2;
-        const double rj = a.d.radius[j];
-        const double sep = ri + rj;
-        if(!(rsq < sep * (sep + 0.0))) { continue; }
-        const double dist = sqrt(rsq);
-        const double pd = (dist - ri) - rj;
-        const double delta = -pd;
-        if(delta < 0.0) { continue; }
-        const double inv = 1.0 / dist;
-        const double n[3] = {d0 * inv, d1 * inv, d2 * inv};
-        const double kk = rj + 0.5 * pd;
-        const double cp[3] = {xj.x + n[0] * kk, xj.y + n[1] * kk, xj.z + n[2] * kk};
-        dem_contact(a, i, j, xi, xj, vi, wi, inv_mi, ti, n, cp, delta, nc, used, overflow, fs, ts);
-    }
-    // sphere-half-space (sim/interaction.py:248-264)
-    const int wb = a.cells.cell_start[a.cells.ncells], we = wb + a.cells.cell_count[a.cells.ncells];
-    for(int j = wb; j < we; j++) {
-        if(a.d.shape[j] != kShapeHalfspace) { continue; }
-        const D4 nj = ldd(a.d.normal, j), xj = ldd(a.d.pos, j);
-        const double kx = (nj.x * xi.x + nj.y * xi.y) + nj.z * xi.z;
-        const double dd = (nj.x * xj.x + nj.y * xj.y) + nj.z * xj.z;
-        const double pd = (kx - ri) - dd;
-        if(!(pd < 0.0)) { continue; }
-        const double delta = -pd;
-        if(delta < 0.0) { continue; }
-        const double tmp = ri + pd;
-        const double n[3] = {nj.x, nj.y, nj.z};
-        const double cp[3] = {xi.x - tmp * nj.x, xi.y - tmp * nj.y, xi.z - tmp * nj.z};
-        dem_contact(a, i, j, xi, xj, vi, wi, inv_mi, ti, n, cp, delta, nc, used, overflow, fh, th);
-    }
-    // drop the records not used this step: the last record moves into the hole and
-    // is examined in turn (sim/contact_history.py:103-120)
+// drop the records not used this step: the last record moves into the hole and is
+// examined in turn (sim/contact_history.py:103-120)
+__device__ __forceinline__ void clear_unused(const DemArgs &a, int i, int &nc, uint32_t used[2]) {
     int k = 0;
     while(k < nc) {
         if(!((used[k >> 5] >> (k & 31)) & 1u)) {
@@ -338,6 +299,78 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force(DemArgs a) {
             k++;
         }
     }
+}
+
+__device__ __forceinline__ D4 image_of(const DemArgs &a, int j, uint32_t code) {
+    D4 xj = ldd(a.d.pos, j);
+    if(code != 0u) {
+        xj.x = ref_image(xj.x, image_shift(code, 0), a.box.len[0]);
+        xj.y = ref_image(xj.y, image_shift(code, 1), a.box.len[1]);
+        xj.z = ref_image(xj.z, image_shift(code, 2), a.box.len[2]);
+    }
+    return xj;
+}
+
+__global__ void __launch_bounds__(kDemBlock) k_dem_force(DemArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= a.d.n || dem_frozen(a.d, false)) { return; }
+    if(a.d.flags != nullptr && (a.d.flags[i] & kFlagFixed)) {
+        st_d4(a.d.force, i, make_d4(0.0, 0.0, 0.0, 0.0));
+        st_d4(a.d.torque, i, make_d4(0.0, 0.0, 0.0, 0.0));
+        a.c.count[i] = 0;
+        return;
+    }
+    const D4 xi = ldd(a.d.pos, i), v4 = ldd(a.d.vel, i), w4 = ldd(a.d.angvel, i);
+    const double vi[3] = {v4.x, v4.y, v4.z}, wi[3] = {w4.x, w4.y, w4.z};
+    const double ri = a.d.radius[i];
+    const double inv_mi = 1.0 / a.d.mass[i];
+    const int ti = a.d.type ? a.d.type[i] : 0;
+    int nc = a.c.count[i];
+    uint32_t used[2] = {0u, 0u};
+    double fs[3] = {0, 0, 0}, ts[3] = {0, 0, 0}, fh[3] = {0, 0, 0}, th[3] = {0, 0, 0};
+    bool overflow = false;
+    // sphere-sphere (sim/interaction.py:234-246)
+    const int cnt = a.list.count[i];
+    for(int k = 0; k < cnt; k++) {
+        const uint32_t e = (uint32_t) a.list.nbr[(size_t) k * a.list.stride + i];
+        const int j = (int) (e & PG_NBR_INDEX_MASK);
+        const D4 xj = image_of(a, j, e >> PG_NBR_INDEX_BITS);
+        const double d0 = xi.x - xj.x, d1 = xi.y - xj.y, d2 = xi.z - xj.z;
+        const double rsq = d0 * d0 + d1 * d1 + d2 * d2;
+        const double rj = a.d.radius[j];
+        const double sep = ri + rj;
+        if(!(rsq < sep * (sep + 0.0))) { continue; }
+        const double dist = sqrt(rsq);
+        const double pd = (dist - ri) - rj;
+        const double delta = -pd;
+        if(delta < 0.0) { continue; }
+        const double inv = 1.0 / dist;
+        const double n[3] = {d0 * inv, d1 * inv, d2 * inv};
+        const double kk = rj + 0.5 * pd;
+        const double cp[3] = {xj.x + n[0] * kk, xj.y + n[1] * kk, xj.z + n[2] * kk};
+        const double rvi[3] = {cp[0] - xi.x, cp[1] - xi.y, cp[2] - xi.z};
+        const double rvj[3] = {cp[0] - xj.x, cp[1] - xj.y, cp[2] - xj.z};
+        dem_contact<double>(a, i, j, vi, wi, inv_mi, ti, n, rvi, rvj, delta, nc, used, overflow, fs, ts);
+    }
+    // sphere-half-space (sim/interaction.py:248-264)
+    const int wb = a.cells.cell_start[a.cells.ncells], we = wb + a.cells.cell_count[a.cells.ncells];
+    for(int j = wb; j < we; j++) {
+        if(a.d.shape[j] != kShapeHalfspace) { continue; }
+        const D4 nj = ldd(a.d.normal, j), xj = ldd(a.d.pos, j);
+        const double kx = (nj.x * xi.x + nj.y * xi.y) + nj.z * xi.z;
+        const double dd = (nj.x * xj.x + nj.y * xj.y) + nj.z * xj.z;
+        const double pd = (kx - ri) - dd;
+        if(!(pd < 0.0)) { continue; }
+        const double delta = -pd;
+        if(delta < 0.0) { continue; }
+        const double tmp = ri + pd;
+        const double n[3] = {nj.x, nj.y, nj.z};
+        const double cp[3] = {xi.x - tmp * nj.x, xi.y - tmp * nj.y, xi.z - tmp * nj.z};
+        const double rvi[3] = {cp[0] - xi.x, cp[1] - xi.y, cp[2] - xi.z};
+        const double rvj[3] = {cp[0] - xj.x, cp[1] - xj.y, cp[2] - xj.z};
+        dem_contact<double>(a, i, j, vi, wi, inv_mi, ti, n, rvi, rvj, delta, nc, used, overflow, fh, th);
+    }
+    clear_unused(a, i, nc, used);
     a.c.count[i] = nc;
     if(overflow) {
         atomicOr(&a.status->overflow, 8);
@@ -348,6 +381,98 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force(DemArgs a) {
     const double gz = 0.0 - (a.prm.drho * vol) * a.prm.gravity;
     st_d4(a.d.force, i, make_d4(0.0 + (fs[0] + fh[0]), 0.0 + (fs[1] + fh[1]), gz + (fs[2] + fh[2]), 0.0));
     st_d4(a.d.torque, i, make_d4(0.0 + (ts[0] + th[0]), 0.0 + (ts[1] + th[1]), 0.0 + (ts[2] + th[2]), 0.0));
+}
+
+// Mixed precision: the contact geometry in FP64 (overlaps are ~1e-7 of the
+// separation, far below FP32 resolution of a distance), everything after it in
+// FP32: normal from the FP32 difference vector, overlap from the FP64 numerator
+// sep^2 - |d|^2 divided by sep + |d| (no cancellation), contact-point offsets
+// relative to the two centres, the spring-dashpot model, friction and the force /
+// torque sums.  The integrator stays FP64.
+__global__ void __launch_bounds__(kDemBlock) k_dem_force_mixed(DemArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= a.d.n || dem_frozen(a.d, false)) { return; }
+    if(a.d.flags != nullptr && (a.d.flags[i] & kFlagFixed)) {
+        st_d4(a.d.force, i, make_d4(0.0, 0.0, 0.0, 0.0));
+        st_d4(a.d.torque, i, make_d4(0.0, 0.0, 0.0, 0.0));
+        a.c.count[i] = 0;
+        return;
+    }
+    const D4 xi = ldd(a.d.pos, i), v4 = ldd(a.d.vel, i), w4 = ldd(a.d.angvel, i);
+    const float vi[3] = {(float) v4.x, (float) v4.y, (float) v4.z};
+    const float wi[3] = {(float) w4.x, (float) w4.y, (float) w4.z};
+    const double ri = a.d.radius[i];
+    const float inv_mi = 1.0f / (float) a.d.mass[i];
+    // FP32 screen: a candidate whose FP32 distance exceeds the contact distance by more
+    // than the FP32 rounding of the coordinates (a.screen) cannot touch
+    const float4 pi32 = ld_f4(a.d.pos32, i);
+    const float lx = (float) a.box.len[0], ly = (float) a.box.len[1], lz = (float) a.box.len[2];
+    const int ti = a.d.type ? a.d.type[i] : 0;
+    int nc = a.c.count[i];
+    uint32_t used[2] = {0u, 0u};
+    float fs[3] = {0, 0, 0}, ts[3] = {0, 0, 0}, fh[3] = {0, 0, 0}, th[3] = {0, 0, 0};
+    bool overflow = false;
+    const int cnt = a.list.count[i];
+    for(int k = 0; k < cnt; k++) {
+        const uint32_t e = (uint32_t) a.list.nbr[(size_t) k * a.list.stride + i];
+        const int j = (int) (e & PG_NBR_INDEX_MASK);
+        const uint32_t code = e >> PG_NBR_INDEX_BITS;
+        {
+            const float4 pj = ld_f4(a.d.pos32, j);
+            const float fx = pi32.x - (pj.x + image_shift(code, 0) * lx);
+            const float fy = pi32.y - (pj.y + image_shift(code, 1) * ly);
+            const float fz = pi32.z - (pj.z + image_shift(code, 2) * lz);
+            const float lim = pi32.w + pj.w + a.screen;
+            if(fx * fx + fy * fy + fz * fz > lim * lim) { continue; }
+        }
+        const D4 xj = image_of(a, j, code);
+        const double d0 = xi.x - xj.x, d1 = xi.y - xj.y, d2 = xi.z - xj.z;
+        const double rsq = d0 * d0 + d1 * d1 + d2 * d2;
+        const double rj = a.d.radius[j];
+        const double sep = ri + rj;
+        if(!(rsq < sep * sep)) { continue; }
+        const float dist = sqrtf((float) rsq);
+        const float delta = (float) (sep * sep - rsq) / ((float) sep + dist);
+        const float inv = 1.0f / dist;
+        const float df[3] = {(float) d0, (float) d1, (float) d2};
+        const float n[3] = {df[0] * inv, df[1] * inv, df[2] * inv};
+        const float kk = (float) rj - 0.5f * delta;
+        const float rvj[3] = {n[0] * kk, n[1] * kk, n[2] * kk};
+        const float rvi[3] = {rvj[0] - df[0], rvj[1] - df[1], rvj[2] - df[2]};
+        dem_contact<float>(a, i, j, vi, wi, inv_mi, ti, n, rvi, rvj, delta, nc, used, overflow, fs, ts);
+    }
+    const int wb = a.cells.cell_start[a.cells.ncells], we = wb + a.cells.cell_count[a.cells.ncells];
+    for(int j = wb; j < we; j++) {
+        if(a.d.shape[j] != kShapeHalfspace) { continue; }
+        const D4 nj = ldd(a.d.normal, j), xj = ldd(a.d.pos, j);
+        {
+            const float pdf = ((float) nj.x * (pi32.x - (float) xj.x) + (float) nj.y * (pi32.y - (float) xj.y)) +
+                              (float) nj.z * (pi32.z - (float) xj.z) - pi32.w;
+            if(pdf > a.screen) { continue; }
+        }
+        const double kx = (nj.x * xi.x + nj.y * xi.y) + nj.z * xi.z;
+        const double dd = (nj.x * xj.x + nj.y * xj.y) + nj.z * xj.z;
+        const double pd = (kx - ri) - dd;
+        if(!(pd < 0.0)) { continue; }
+        const float delta = (float) (-pd);
+        const float tmp = (float) (ri + pd);
+        const float n[3] = {(float) nj.x, (float) nj.y, (float) nj.z};
+        const float rvi[3] = {-tmp * n[0], -tmp * n[1], -tmp * n[2]};
+        const float rvj[3] = {(float) (xi.x - xj.x) + rvi[0], (float) (xi.y - xj.y) + rvi[1],
+                              (float) (xi.z - xj.z) + rvi[2]};
+        dem_contact<float>(a, i, j, vi, wi, inv_mi, ti, n, rvi, rvj, delta, nc, used, overflow, fh, th);
+    }
+    clear_unused(a, i, nc, used);
+    a.c.count[i] = nc;
+    if(overflow) {
+        atomicOr(&a.status->overflow, 8);
+        atomicMax(&a.status->max_contacts, a.c.capacity + 1);
+    }
+    const double vol = (((4.0 / 3.0) * a.prm.pi) * ri) * ri * ri;
+    const double gz = 0.0 - (a.prm.drho * vol) * a.prm.gravity;
+    st_d4(a.d.force, i, make_d4((double) (fs[0] + fh[0]), (double) (fs[1] + fh[1]), gz + (double) (fs[2] + fh[2]),
+                                0.0));
+    st_d4(a.d.torque, i, make_d4((double) (ts[0] + th[0]), (double) (ts[1] + th[1]), (double) (ts[2] + th[2]), 0.0));
 }
 
 // ------------------------------------------------------------------ Euler with rotation
@@ -373,42 +498,53 @@ __global__ void __launch_bounds__(kBlock) k_dem_euler(DemArgs a) {
         const D4 X = ldd(a.d.pos, i), V = ldd(a.d.vel, i), W = ldd(a.d.angvel, i);
         const D4 F = ldd(a.d.force, i), T = ldd(a.d.torque, i), Qd = ldd(a.d.quat, i);
         const double Qo[4] = {Qd.x, Qd.y, Qd.z, Qd.w};
-        double R[9];
-        quat_matrix(Qo, R);                      // the rotation matrix of the last step
-        const double iI = a.d.inv_inertia[i];
         const double im = 1.0 / a.d.mass[i];
         const double h = 0.5 * im;
         const double f3[3] = {F.x, F.y, F.z}, t3[3] = {T.x, T.y, T.z};
         double x3[3] = {X.x, X.y, X.z}, v3[3] = {V.x, V.y, V.z}, w3[3] = {W.x, W.y, W.z};
         for(int e = 0; e < 3; e++) { x3[e] = x3[e] + (((h * f3[e]) * dt) * dt + v3[e] * dt); }
         for(int e = 0; e < 3; e++) { v3[e] = v3[e] + (im * f3[e]) * dt; }
-        // inv_inertia * torque with the +0 off-diagonal entries of the reference's matrix
-        double av[3], bv[3], wd[3], phi[3];
-        av[0] = (iI * t3[0] + 0.0 * t3[1]) + 0.0 * t3[2];
-        av[1] = (0.0 * t3[0] + iI * t3[1]) + 0.0 * t3[2];
-        av[2] = (0.0 * t3[0] + 0.0 * t3[1]) + iI * t3[2];
-        for(int r = 0; r < 3; r++) { bv[r] = (R[r * 3] * av[0] + R[r * 3 + 1] * av[1]) + R[r * 3 + 2] * av[2]; }
-        for(int c = 0; c < 3; c++) { wd[c] = (bv[0] * R[c] + bv[1] * R[c + 3]) + bv[2] * R[c + 6]; }
-        for(int e = 0; e < 3; e++) { phi[e] = w3[e] * dt + ((0.5 * wd[e]) * dt) * dt; }
-        const double lp = sqrt(phi[0] * phi[0] + phi[1] * phi[1] + phi[2] * phi[2]);
-        double q[4];
-        if(fabs(lp) < 1e-06) {
-            q[0] = 1.0; q[1] = 0.0; q[2] = 0.0; q[3] = 0.0;
-        } else {
-            const double ca = cos(lp * 0.5), sa = sin(lp * 0.5), il = 1.0 / lp;
-            q[0] = ca; q[1] = sa * (phi[0] * il); q[2] = sa * (phi[1] * il); q[3] = sa * (phi[2] * il);
+        // No torque and no spin: the rotation yields phi = 0, the identity quaternion,
+        // the product q Q = Q bit for bit and, when |Q|^2 is within 1e-8 of one, no
+        // renormalisation -- orientation and angular velocity stay as they are, so the
+        // FP64 rotation arithmetic is skipped (most spheres of a settling packing).
+        const bool still = T.x == 0.0 && T.y == 0.0 && T.z == 0.0 && W.x == 0.0 && W.y == 0.0 && W.z == 0.0 &&
+                           fabs((((Qo[0] * Qo[0] + Qo[1] * Qo[1]) + Qo[2] * Qo[2]) + Qo[3] * Qo[3]) - 1.0) < 1e-08;
+        if(!still) {
+            double R[9];
+            quat_matrix(Qo, R);                  // the rotation matrix of the last step
+            const double iI = a.d.inv_inertia[i];
+            // inv_inertia * torque with the +0 off-diagonal entries of the reference's matrix
+            double av[3], bv[3], wd[3], phi[3];
+            av[0] = (iI * t3[0] + 0.0 * t3[1]) + 0.0 * t3[2];
+            av[1] = (0.0 * t3[0] + iI * t3[1]) + 0.0 * t3[2];
+            av[2] = (0.0 * t3[0] + 0.0 * t3[1]) + iI * t3[2];
+            for(int r = 0; r < 3; r++) { bv[r] = (R[r * 3] * av[0] + R[r * 3 + 1] * av[1]) + R[r * 3 + 2] * av[2]; }
+            for(int c = 0; c < 3; c++) { wd[c] = (bv[0] * R[c] + bv[1] * R[c + 3]) + bv[2] * R[c + 6]; }
+            for(int e = 0; e < 3; e++) { phi[e] = w3[e] * dt + ((0.5 * wd[e]) * dt) * dt; }
+            const double lp = sqrt(phi[0] * phi[0] + phi[1] * phi[1] + phi[2] * phi[2]);
+            double q[4];
+            if(fabs(lp) < 1e-06) {
+                q[0] = 1.0; q[1] = 0.0; q[2] = 0.0; q[3] = 0.0;
+            } else {
+                const double ca = cos(lp * 0.5), sa = sin(lp * 0.5), il = 1.0 / lp;
+                q[0] = ca; q[1] = sa * (phi[0] * il); q[2] = sa * (phi[1] * il); q[3] = sa * (phi[2] * il);
+            }
+            const double r_ = ((q[0] * Qo[0] - q[1] * Qo[1]) - q[2] * Qo[2]) - q[3] * Qo[3];
+            const double i_ = ((q[0] * Qo[1] + q[1] * Qo[0]) + q[2] * Qo[3]) - q[3] * Qo[2];
+            const double j_ = ((q[0] * Qo[2] + q[2] * Qo[0]) + q[3] * Qo[1]) - q[1] * Qo[3];
+            const double k_ = ((q[0] * Qo[3] + q[3] * Qo[0]) + q[1] * Qo[2]) - q[2] * Qo[1];
+            const double len2 = ((r_ * r_ + i_ * i_) + j_ * j_) + k_ * k_;
+            const double il2 = (fabs(len2 - 1.0) < 1e-08) ? 1.0 : 1.0 / sqrt(len2);
+            for(int e = 0; e < 3; e++) { w3[e] = w3[e] + wd[e] * dt; }
+            st_d4(a.d.angvel, i, make_d4(w3[0], w3[1], w3[2], 0.0));
+            st_d4(a.d.quat, i, make_d4(r_ * il2, i_ * il2, j_ * il2, k_ * il2));
         }
-        const double r_ = ((q[0] * Qo[0] - q[1] * Qo[1]) - q[2] * Qo[2]) - q[3] * Qo[3];
-        const double i_ = ((q[0] * Qo[1] + q[1] * Qo[0]) + q[2] * Qo[3]) - q[3] * Qo[2];
-        const double j_ = ((q[0] * Qo[2] + q[2] * Qo[0]) + q[3] * Qo[1]) - q[1] * Qo[3];
-        const double k_ = ((q[0] * Qo[3] + q[3] * Qo[0]) + q[1] * Qo[2]) - q[2] * Qo[1];
-        const double len2 = ((r_ * r_ + i_ * i_) + j_ * j_) + k_ * k_;
-        const double il2 = (fabs(len2 - 1.0) < 1e-08) ? 1.0 : 1.0 / sqrt(len2);
-        for(int e = 0; e < 3; e++) { w3[e] = w3[e] + wd[e] * dt; }
         st_d4(a.d.pos, i, make_d4(x3[0], x3[1], x3[2], X.w));
+        if(a.d.pos32 != nullptr) {
+            st_f4(a.d.pos32, i, make_float4((float) x3[0], (float) x3[1], (float) x3[2], (float) a.d.radius[i]));
+        }
         st_d4(a.d.vel, i, make_d4(v3[0], v3[1], v3[2], 0.0));
-        st_d4(a.d.angvel, i, make_d4(w3[0], w3[1], w3[2], 0.0));
-        st_d4(a.d.quat, i, make_d4(r_ * il2, i_ * il2, j_ * il2, k_ * il2));
         if(a.d.pos_ref != nullptr) {
             const D4 r0 = ldd(a.d.pos_ref, i);
             const double ex = x3[0] - r0.x, ey = x3[1] - r0.y, ez = x3[2] - r0.z;
@@ -476,15 +612,26 @@ int dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *cells
 }
 
 int dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cells, const pg_neighbor_list *list,
-              const pg_contacts *c, const pg_dem_params *prm, pg_status *status, cudaStream_t st) {
+              const pg_contacts *c, const pg_dem_params *prm, int precision, pg_status *status, cudaStream_t st) {
     if(!box || !dem_ok(d) || !cells || !list || !list->nbr || !list->count || !contacts_ok(c, d) || !prm ||
        !status) {
         return PG_ERR_ARGUMENT;
     }
     if(prm->ntypes < 1 || prm->ntypes > 4 || list->stride < d->n) { return PG_ERR_ARGUMENT; }
+    if(precision != PG_FP64 && precision != PG_MIXED) { return PG_ERR_ARGUMENT; }
+    if(precision == PG_MIXED && d->pos32 == nullptr) { return PG_ERR_ARGUMENT; }
     DemArgs a = {};
     a.box = *box; a.d = *d; a.cells = *cells; a.list = *list; a.c = *c; a.prm = *prm; a.status = status;
-    if(d->n > 0) { k_dem_force<<<blocks_for(d->n, kDemBlock), kDemBlock, 0, st>>>(a); note_launch(); }
+    // FP32 rounding of coordinates up to |lo| + 2 len (images), of radii and of the
+    // distance arithmetic, with a factor 64 of room
+    double span = 0.0;
+    for(int k = 0; k < 3; k++) { span = fmax(span, fabs(box->lo[k]) + 2.0 * box->len[k]); }
+    a.screen = (float) (64.0 * span * 1.1920928955078125e-07);
+    if(d->n > 0) {
+        if(precision == PG_FP64) { k_dem_force<<<blocks_for(d->n, kDemBlock), kDemBlock, 0, st>>>(a); }
+        else { k_dem_force_mixed<<<blocks_for(d->n, kDemBlock), kDemBlock, 0, st>>>(a); }
+        note_launch();
+    }
     return launch_status();
 }
 

@@ -93,8 +93,8 @@ __global__ void __launch_bounds__(kBlock) k_ens_split(EnsArgs a) {
     split_pos(x.z, iq, q, h.z, l.z);
     h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);
     l.w = 0.0f;
-    st_f4(a.p.pos_hi, i, h);
-    st_f4(a.p.pos_lo, i, l);
+    st_f4(a.p.pos_hi, hl(a.p, i), h);
+    st_f4(a.p.pos_lo, hl(a.p, i), l);
 }
 
 // ------------------------------------------------------------------ list build
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
     if(i >= a.p.n) { return; }
     const D4 xi = ld_d4(a.p.pos, i);
     st_d4(a.p.pos_ref, i, xi);
-    const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+    const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
     st_f4(a.p.ref_hi, i, hi);
     st_f4(a.p.ref_lo, i, lo);
     const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
                     const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
                     for(int j = b; j < e; j++) {
                         if(j == i && code == 0u) { continue; }
-                        const float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
+                        const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
                         const float fx = ens_delta(hi.x, lo.x, hj.x, lj.x, sx, R.len_hi[0], R.len_lo[0]);
                         const float fy = ens_delta(hi.y, lo.y, hj.y, lj.y, sy, R.len_hi[1], R.len_lo[1]);
                         const float fz = ens_delta(hi.z, lo.z, hj.z, lj.z, sz, R.len_hi[2], R.len_lo[2]);
@@ -195,7 +195,7 @@ __global__ void k_ens_force(EnsArgs a) {
     const int i = g / TPA, t = g % TPA;
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     if(i < a.p.n) {
-        const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+        const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
         const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
         const float lhx = R.len_hi[0], lhy = R.len_hi[1], lhz = R.len_hi[2];
         const float llx = R.len_lo[0], lly = R.len_lo[1], llz = R.len_lo[2];
@@ -205,10 +205,10 @@ __global__ void k_ens_force(EnsArgs a) {
         const size_t row = (size_t) a.list.stride * TPA;
         const float c2 = a.cutoff2;
         for(int k = t, r = 0; k < cnt; k += TPA, r++) {
-            const uint32_t e = (uint32_t) __ldg(nb + r * row);
+            const uint32_t e = (uint32_t) __ldcs(nb + r * row);
             const int j = (int) (e & PG_NBR_INDEX_MASK);
             const uint32_t code = e >> PG_NBR_INDEX_BITS;
-            const float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
+            const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
             float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
             float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
             if(code != 0u) {
@@ -273,8 +273,8 @@ __global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
             ens_resplit(x.z, q, iq, h.z, l.z);
             h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);
             l.w = 0.0f;
-            st_f4(a.p.pos_hi, i, h);
-            st_f4(a.p.pos_lo, i, l);
+            st_f4(a.p.pos_hi, hl(a.p, i), h);
+            st_f4(a.p.pos_lo, hl(a.p, i), l);
             const float4 rh = ld_f4(a.p.ref_hi, i);
             const float4 rl = ld_f4(a.p.ref_lo, i);
             const float dx = (h.x - rh.x) + (l.x - rl.x);

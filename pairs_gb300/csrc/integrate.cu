@@ -73,8 +73,8 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
                 split_pos(x.z, iq, q, hv.z, lv.z);
                 hv.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);
                 lv.w = 0.0f;
-                st_f4(a.p.pos_hi, i, hv);
-                st_f4(a.p.pos_lo, i, lv);
+                st_f4(a.p.pos_hi, hl(a.p, i), hv);
+                st_f4(a.p.pos_lo, hl(a.p, i), lv);
             }
         }
         st_d4(a.p.vel, i, v);
@@ -142,8 +142,8 @@ __global__ void __launch_bounds__(kBlock) k_integrate_mixed(MixArgs a) {
             resplit(x.z, q, iq, h.z, l.z);
             h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);   // type bits
             l.w = 0.0f;
-            st_f4(a.p.pos_hi, i, h);
-            st_f4(a.p.pos_lo, i, l);
+            st_f4(a.p.pos_hi, hl(a.p, i), h);
+            st_f4(a.p.pos_lo, hl(a.p, i), l);
             // guard, screened in FP32 against the positions of the last list build
             const float4 rh = ld_f4(a.p.ref_hi, i);
             const float4 rl = ld_f4(a.p.ref_lo, i);

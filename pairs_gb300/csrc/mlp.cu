@@ -70,33 +70,50 @@ __device__ __forceinline__ void load_params(const float *params, float *s) {
     __syncthreads();
 }
 
-__device__ __forceinline__ float mlp_eval(const float *s, const float *x, float *h1) {
-    for(int u = 0; u < kH; u++) {
-        float z = s[kOffB1 + u];
-        for(int k = 0; k < kIn; k++) { z = fmaf(s[kOffW1 + u * kIn + k], x[k], z); }
-        h1[u] = tanhf(z);
+// One warp evaluates one cell: lane l owns hidden units l and l + 32 of both layers;
+// the first layer's activations reach every lane through shuffles.
+struct WarpAct {
+    float h1a, h1b;      // tanh of layer 1, units l and l+32
+    float h2a, h2b;      // tanh of layer 2
+};
+
+__device__ __forceinline__ float warp_mlp(const float *s, const float x[kIn], WarpAct &act) {
+    const int l = threadIdx.x & 31;
+    float za = s[kOffB1 + l], zb = s[kOffB1 + l + 32];
+    for(int k = 0; k < kIn; k++) {
+        za = fmaf(s[kOffW1 + l * kIn + k], x[k], za);
+        zb = fmaf(s[kOffW1 + (l + 32) * kIn + k], x[k], zb);
     }
-    float o = s[kOffB3];
-    for(int u = 0; u < kH; u++) {
-        float z = s[kOffB2 + u];
-        const float *w = s + kOffW2 + u * kH;
-        #pragma unroll 16
-        for(int k = 0; k < kH; k++) { z = fmaf(w[k], h1[k], z); }
-        o = fmaf(s[kOffW3 + u], tanhf(z), o);
+    act.h1a = tanhf(za);
+    act.h1b = tanhf(zb);
+    float ya = s[kOffB2 + l], yb = s[kOffB2 + l + 32];
+    const float *wa = s + kOffW2 + l * kH, *wb = s + kOffW2 + (l + 32) * kH;
+    #pragma unroll 8
+    for(int j = 0; j < 32; j++) {
+        const float p = __shfl_sync(0xffffffffu, act.h1a, j), q = __shfl_sync(0xffffffffu, act.h1b, j);
+        ya = fmaf(wa[j], p, ya); ya = fmaf(wa[j + 32], q, ya);
+        yb = fmaf(wb[j], p, yb); yb = fmaf(wb[j + 32], q, yb);
     }
-    return o;
+    act.h2a = tanhf(ya);
+    act.h2b = tanhf(yb);
+    float o = s[kOffW3 + l] * act.h2a + s[kOffW3 + l + 32] * act.h2b;
+    for(int off = 16; off > 0; off >>= 1) { o += __shfl_xor_sync(0xffffffffu, o, off); }
+    return o + s[kOffB3];
 }
 
-__global__ void __launch_bounds__(128) k_mlp_forward(const float *params, const float *feat, int ncells,
-                                                     float *out) {
+constexpr int kFwdThreads = 256;
+
+__global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(const float *params, const float *feat, int ncells,
+                                                             float *out) {
     __shared__ float s[kParams];
     load_params(params, s);
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if(c >= ncells) { return; }
     const float *f = feat + (size_t) c * kFeat;
-    float h1[kH];
     const float x[kIn] = {f[0], f[1], f[2]};
-    out[c] = f[3] > 0.0f ? mlp_eval(s, x, h1) : INFINITY;
+    WarpAct act;
+    const float o = warp_mlp(s, x, act);
+    if((threadIdx.x & 31) == 0) { out[c] = f[3] > 0.0f ? o : INFINITY; }
 }
 
 // ---------------------------------------------------------------- soft minimum
@@ -143,25 +160,23 @@ __global__ void k_softmin_finish(float temperature, float *result) {
 
 // ---------------------------------------------------------------- backward
 
-// grads (kParams) accumulate over cells and samples; loss accumulates in *loss.
-// One block walks the sample's cells in chunks of blockDim.x: every thread computes
-// its cell's activations and local gradients (dL/dz2, dL/dz1) into shared memory,
-// then each thread owns a fixed slice of the parameters and sums that slice over the
-// chunk (no atomics on shared data); the block adds each parameter's total to the
-// global gradient once.
-constexpr int kBwdThreads = 128;
+// Gradient of one sample's loss.  A block takes kBwdCells cells: each warp runs the
+// forward and backward pass of its cells (lane l owns hidden units l and l + 32),
+// writing the per-cell vectors dz2 (layer-2 pre-activation gradient), h1, dz1 and
+// the cell's output gradient to shared memory; the block then forms its partial
+// weight gradients (W2 as sum_c dz2 h1^T, thread-owned entries, no shared atomics)
+// and adds them to the global gradient once.
+constexpr int kBwdThreads = 256;
+constexpr int kBwdCells = 16;
+constexpr int kBwdSlice = (kParams + kBwdThreads - 1) / kBwdThreads;
 
 __global__ void __launch_bounds__(kBwdThreads) k_mlp_backward(const float *params, const float *feat,
                                                              const float *out, int ncells, const float *result,
                                                              float target_log, int censored, float inv_t,
                                                              float *grads, float *loss) {
     __shared__ float s[kParams];
-    extern __shared__ float dyn[];
-    float *H1 = dyn;                              // [kBwdThreads][kH]
-    float *DZ2 = H1 + kBwdThreads * kH;           // [kBwdThreads][kH]
-    float *DZ1 = DZ2 + kBwdThreads * kH;          // [kBwdThreads][kH]
-    float *X = DZ1 + kBwdThreads * kH;            // [kBwdThreads][4]: x0, x1, x2, go
-    float *H2 = X + kBwdThreads * 4;              // [kBwdThreads][kH]
+    __shared__ float H1[kBwdCells][kH], DZ2[kBwdCells][kH], DZ1[kBwdCells][kH], H2[kBwdCells][kH];
+    __shared__ float X[kBwdCells][4];
     load_params(params, s);
     const float P = result[0];
     const float m = ordered_to_float(*reinterpret_cast<const int *>(result + 1));
@@ -169,92 +184,65 @@ __global__ void __launch_bounds__(kBwdThreads) k_mlp_backward(const float *param
     float e = P - target_log;
     if(censored) { e = fminf(e, 0.0f); }
     const float dP = 2.0f * e;
-    if(threadIdx.x == 0) { atomicAdd(loss, e * e); }
-    // parameter slice owned by this thread: W2 entries t, t+T, ...; then the small ones
-    float acc[kH * kH / kBwdThreads];
-    float acc_small[(kParams - kH * kH + kBwdThreads - 1) / kBwdThreads];
-    for(int q = 0; q < kH * kH / kBwdThreads; q++) { acc[q] = 0.0f; }
-    for(int q = 0; q < (int) (sizeof(acc_small) / sizeof(float)); q++) { acc_small[q] = 0.0f; }
-    const int t = threadIdx.x;
-    for(int c0 = 0; c0 < ncells; c0 += kBwdThreads) {
-        const int c = c0 + t;
-        float w = 0.0f;
-        if(c < ncells && out[c] < INFINITY) { w = __expf(-(out[c] - m) * inv_t) / Z; }
-        const float go = dP * w;
-        const bool active = go != 0.0f;
-        if(!__syncthreads_or(active)) { continue; }
-        float *h1 = H1 + t * kH, *dz2 = DZ2 + t * kH, *dz1 = DZ1 + t * kH, *h2 = H2 + t * kH;
+    if(blockIdx.x == 0 && threadIdx.x == 0) { atomicAdd(loss, e * e); }
+    const int warp = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int c0 = blockIdx.x * kBwdCells;
+    for(int cc = warp; cc < kBwdCells; cc += kBwdThreads / 32) {
+        const int c = c0 + cc;
+        float go = 0.0f;
+        if(c < ncells && out[c] < INFINITY) { go = dP * __expf(-(out[c] - m) * inv_t) / Z; }
         float x[kIn] = {0.0f, 0.0f, 0.0f};
-        if(active) {
+        if(go != 0.0f) {
             const float *f = feat + (size_t) c * kFeat;
             x[0] = f[0]; x[1] = f[1]; x[2] = f[2];
-            for(int u = 0; u < kH; u++) {
-                float z = s[kOffB1 + u];
-                for(int k = 0; k < kIn; k++) { z = fmaf(s[kOffW1 + u * kIn + k], x[k], z); }
-                h1[u] = tanhf(z);
-                dz1[u] = 0.0f;
+            WarpAct act;
+            warp_mlp(s, x, act);
+            const float da = go * s[kOffW3 + l] * (1.0f - act.h2a * act.h2a);
+            const float db = go * s[kOffW3 + l + 32] * (1.0f - act.h2b * act.h2b);
+            // dz1[k] = (sum_u d2[u] W2[u][k]) (1 - h1[k]^2), k = l and l + 32
+            float ga = 0.0f, gb = 0.0f;
+            #pragma unroll 8
+            for(int j = 0; j < 32; j++) {
+                const float p = __shfl_sync(0xffffffffu, da, j), q = __shfl_sync(0xffffffffu, db, j);
+                ga = fmaf(p, s[kOffW2 + j * kH + l], ga); ga = fmaf(q, s[kOffW2 + (j + 32) * kH + l], ga);
+                gb = fmaf(p, s[kOffW2 + j * kH + l + 32], gb); gb = fmaf(q, s[kOffW2 + (j + 32) * kH + l + 32], gb);
             }
-            for(int u = 0; u < kH; u++) {
-                float z = s[kOffB2 + u];
-                const float *wr = s + kOffW2 + u * kH;
-                for(int k = 0; k < kH; k++) { z = fmaf(wr[k], h1[k], z); }
-                const float hz = tanhf(z);
-                h2[u] = hz;
-                const float d2 = go * s[kOffW3 + u] * (1.0f - hz * hz);
-                dz2[u] = d2;
-                for(int k = 0; k < kH; k++) { dz1[k] = fmaf(d2, wr[k], dz1[k]); }
-            }
-            for(int u = 0; u < kH; u++) { dz1[u] *= (1.0f - h1[u] * h1[u]); }
+            H1[cc][l] = act.h1a; H1[cc][l + 32] = act.h1b;
+            H2[cc][l] = act.h2a; H2[cc][l + 32] = act.h2b;
+            DZ2[cc][l] = da; DZ2[cc][l + 32] = db;
+            DZ1[cc][l] = ga * (1.0f - act.h1a * act.h1a);
+            DZ1[cc][l + 32] = gb * (1.0f - act.h1b * act.h1b);
         } else {
-            for(int u = 0; u < kH; u++) { h1[u] = 0.0f; dz2[u] = 0.0f; dz1[u] = 0.0f; h2[u] = 0.0f; }
+            H1[cc][l] = H1[cc][l + 32] = 0.0f; H2[cc][l] = H2[cc][l + 32] = 0.0f;
+            DZ2[cc][l] = DZ2[cc][l + 32] = 0.0f; DZ1[cc][l] = DZ1[cc][l + 32] = 0.0f;
         }
-        X[t * 4 + 0] = x[0]; X[t * 4 + 1] = x[1]; X[t * 4 + 2] = x[2]; X[t * 4 + 3] = go;
-        __syncthreads();
-        // W2[u][k] += sum_c dz2[c][u] h1[c][k]
-        for(int q = 0; q < kH * kH / kBwdThreads; q++) {
-            const int e2 = t + q * kBwdThreads, u = e2 / kH, k = e2 % kH;
-            float a = 0.0f;
-            for(int cc = 0; cc < kBwdThreads; cc++) { a = fmaf(DZ2[cc * kH + u], H1[cc * kH + k], a); }
-            acc[q] += a;
-        }
-        // the rest: W1[u][k] (dz1 x), b1 (dz1), b2 (dz2), W3 (go h2), b3 (go)
-        for(int q = 0; q < (int) (sizeof(acc_small) / sizeof(float)); q++) {
-            const int r = t + q * kBwdThreads;
-            float a = 0.0f;
-            if(r < kH * kIn) {
-                const int u = r / kIn, k = r % kIn;
-                for(int cc = 0; cc < kBwdThreads; cc++) { a = fmaf(DZ1[cc * kH + u], X[cc * 4 + k], a); }
-            } else if(r < kH * kIn + kH) {
-                const int u = r - kH * kIn;
-                for(int cc = 0; cc < kBwdThreads; cc++) { a += DZ1[cc * kH + u]; }
-            } else if(r < kH * kIn + 2 * kH) {
-                const int u = r - kH * kIn - kH;
-                for(int cc = 0; cc < kBwdThreads; cc++) { a += DZ2[cc * kH + u]; }
-            } else if(r < kH * kIn + 3 * kH) {
-                const int u = r - kH * kIn - 2 * kH;
-                for(int cc = 0; cc < kBwdThreads; cc++) { a = fmaf(X[cc * 4 + 3], H2[cc * kH + u], a); }
-            } else if(r == kH * kIn + 3 * kH) {
-                for(int cc = 0; cc < kBwdThreads; cc++) { a += X[cc * 4 + 3]; }
-            }
-            acc_small[q] += a;
-        }
-        __syncthreads();
+        if(l < 4) { X[cc][l] = l < kIn ? x[l] : go; }
     }
-    for(int q = 0; q < kH * kH / kBwdThreads; q++) {
-        const int e2 = t + q * kBwdThreads;
-        if(acc[q] != 0.0f) { atomicAdd(&grads[kOffW2 + e2], acc[q]); }
-    }
-    for(int q = 0; q < (int) (sizeof(acc_small) / sizeof(float)); q++) {
-        const int r = t + q * kBwdThreads;
-        if(acc_small[q] == 0.0f) { continue; }
-        int dst;
-        if(r < kH * kIn) { dst = kOffW1 + r; }
-        else if(r < kH * kIn + kH) { dst = kOffB1 + (r - kH * kIn); }
-        else if(r < kH * kIn + 2 * kH) { dst = kOffB2 + (r - kH * kIn - kH); }
-        else if(r < kH * kIn + 3 * kH) { dst = kOffW3 + (r - kH * kIn - 2 * kH); }
-        else if(r == kH * kIn + 3 * kH) { dst = kOffB3; }
-        else { continue; }
-        atomicAdd(&grads[dst], acc_small[q]);
+    __syncthreads();
+    // partial gradients of this block's cells; thread t owns parameters t, t+T, ...
+    for(int q = 0; q < kBwdSlice; q++) {
+        const int r = threadIdx.x + q * kBwdThreads;
+        if(r >= kParams) { break; }
+        float a = 0.0f;
+        if(r >= kOffW2 && r < kOffB2) {
+            const int u = (r - kOffW2) / kH, k = (r - kOffW2) % kH;
+            for(int cc = 0; cc < kBwdCells; cc++) { a = fmaf(DZ2[cc][u], H1[cc][k], a); }
+        } else if(r < kOffB1) {
+            const int u = r / kIn, k = r % kIn;
+            for(int cc = 0; cc < kBwdCells; cc++) { a = fmaf(DZ1[cc][u], X[cc][k], a); }
+        } else if(r < kOffW2) {
+            const int u = r - kOffB1;
+            for(int cc = 0; cc < kBwdCells; cc++) { a += DZ1[cc][u]; }
+        } else if(r < kOffW3) {
+            const int u = r - kOffB2;
+            for(int cc = 0; cc < kBwdCells; cc++) { a += DZ2[cc][u]; }
+        } else if(r < kOffB3) {
+            const int u = r - kOffW3;
+            for(int cc = 0; cc < kBwdCells; cc++) { a = fmaf(X[cc][3], H2[cc][u], a); }
+        } else {
+            for(int cc = 0; cc < kBwdCells; cc++) { a += X[cc][3]; }
+        }
+        if(a != 0.0f) { atomicAdd(&grads[r], a); }
     }
 }
 
@@ -287,7 +275,8 @@ int cell_features(const pg_particles *p, const pg_cells *cells, int precision, i
 
 int mlp_forward(const float *params, const float *feat, int32_t ncells, float *out, cudaStream_t st) {
     if(!params || !feat || !out || ncells <= 0) { return PG_ERR_ARGUMENT; }
-    k_mlp_forward<<<blocks_for(ncells, 128), 128, 0, st>>>(params, feat, ncells, out); note_launch();
+    const int blocks = (int) (((int64_t) ncells * 32 + kFwdThreads - 1) / kFwdThreads);
+    k_mlp_forward<<<blocks, kFwdThreads, 0, st>>>(params, feat, ncells, out); note_launch();
     return launch_status();
 }
 
@@ -304,11 +293,8 @@ int mlp_softmin(const float *out, int32_t ncells, float temperature, float *resu
 int mlp_backward(const float *params, const float *feat, const float *out, int32_t ncells, const float *result,
                  float target_log, int censored, float temperature, float *grads, float *loss, cudaStream_t st) {
     if(!params || !feat || !out || !result || !grads || !loss || ncells <= 0) { return PG_ERR_ARGUMENT; }
-    const size_t smem = (size_t) kBwdThreads * (4 * kH + 4) * sizeof(float);
-    if(cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem) != cudaSuccess) {
-        return PG_ERR_CUDA;
-    }
-    k_mlp_backward<<<1, kBwdThreads, smem, st>>>(params, feat, out, ncells, result, target_log, censored,
+    const int blocks = (ncells + kBwdCells - 1) / kBwdCells;
+    k_mlp_backward<<<blocks, kBwdThreads, 0, st>>>(params, feat, out, ncells, result, target_log, censored,
                                                    1.0f / temperature, grads, loss);
     note_launch();
     return launch_status();

@@ -48,27 +48,33 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
     const D4 xi = ld_d4(a.p.pos, i);
     st_d4(a.p.pos_ref, i, xi);
     if(a.p.ref_hi != nullptr) {
-        st_f4(a.p.ref_hi, i, ld_f4(a.p.pos_hi, i));
-        st_f4(a.p.ref_lo, i, ld_f4(a.p.pos_lo, i));
+        st_f4(a.p.ref_hi, i, ld_f4(a.p.pos_hi, hl(a.p, i)));
+        st_f4(a.p.ref_lo, i, ld_f4(a.p.pos_lo, hl(a.p, i)));
     }
     int cnt = 0;
     const bool fixed = a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed);
     const int ci = a.cells.particle_cell[i];
     if(!fixed && ci < a.cells.ncells) {
-        const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+        const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
         const int dz_ = a.cells.dims[2], dy_ = a.cells.dims[1], dx_ = a.cells.dims[0];
         const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
         const int stride = a.list.stride, cap = a.list.max_neighbors;
         int32_t *out = a.list.nbr + i;
-        for(int ox = -1; ox <= 1; ox++) {
+        const int rr = a.cells.reach > 1 ? a.cells.reach : 1;
+        // offsets past one box length are skipped: a box longer than 2 r_list holds no
+        // partner there, and each (cell, image) pair is then visited once
+        for(int ox = -rr; ox <= rr; ox++) {
+            if(ox < -dx_ || ox > dx_) { continue; }
             int nx = cx + ox, sx = 0;
             if(nx < 0) { if(!a.box.periodic[0]) { continue; } nx += dx_; sx = -1; }
             else if(nx >= dx_) { if(!a.box.periodic[0]) { continue; } nx -= dx_; sx = 1; }
-            for(int oy = -1; oy <= 1; oy++) {
+            for(int oy = -rr; oy <= rr; oy++) {
+                if(oy < -dy_ || oy > dy_) { continue; }
                 int ny = cy + oy, sy = 0;
                 if(ny < 0) { if(!a.box.periodic[1]) { continue; } ny += dy_; sy = -1; }
                 else if(ny >= dy_) { if(!a.box.periodic[1]) { continue; } ny -= dy_; sy = 1; }
-                for(int oz = -1; oz <= 1; oz++) {
+                for(int oz = -rr; oz <= rr; oz++) {
+                    if(oz < -dz_ || oz > dz_) { continue; }
                     int nz = cz + oz, sz = 0;
                     if(nz < 0) { if(!a.box.periodic[2]) { continue; } nz += dz_; sz = -1; }
                     else if(nz >= dz_) { if(!a.box.periodic[2]) { continue; } nz -= dz_; sz = 1; }
@@ -81,7 +87,7 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
                         // periodic image from both sides, as the reference's ghosts
                         // always pass its i < j test (sim/interaction.py:107-113)
                         if(a.list.half && code == 0u && j < i) { continue; }
-                        const float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
+                        const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
                         const float fx = comp_delta(hi.x, lo.x, hj.x, lj.x, sx, a.box.len_hi[0], a.box.len_lo[0]);
                         const float fy = comp_delta(hi.y, lo.y, hj.y, lj.y, sy, a.box.len_hi[1], a.box.len_lo[1]);
                         const float fz = comp_delta(hi.z, lo.z, hj.z, lj.z, sz, a.box.len_hi[2], a.box.len_lo[2]);
@@ -122,10 +128,15 @@ int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cell
     if(list->nbr16 != nullptr) { return tile_build(box, p, cells, list, r_list2, status, st); }
     if(!p->pos || !p->pos_hi || !p->pos_lo || !p->pos_ref || !list->nbr || !list->count) { return PG_ERR_ARGUMENT; }
     if(list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS)) { return PG_ERR_ARGUMENT; }
+    const int rr = cells->reach > 1 ? cells->reach : 1;
+    if(rr > 2) { return PG_ERR_ARGUMENT; }
     for(int d = 0; d < 3; d++) {
-        // a stencil of one cell each side covers r_list only if cells are >= r_list
-        if(cells->cell_len[d] * cells->cell_len[d] < r_list2) { return PG_ERR_ARGUMENT; }
-        if(box->periodic[d] && box->len[d] * box->len[d] <= r_list2) { return PG_ERR_ARGUMENT; }
+        // a stencil of `reach` cells each side covers r_list only if reach * cell >= r_list
+        const double span = cells->cell_len[d] * rr;
+        if(span * span < r_list2) { return PG_ERR_ARGUMENT; }
+        // the periodic box must exceed r_list (2 r_list for the 125-cell stencil, whose
+        // offsets would otherwise reach the same image twice)
+        if(box->periodic[d] && box->len[d] * box->len[d] <= (rr == 1 ? 1.0 : 4.0) * r_list2) { return PG_ERR_ARGUMENT; }
     }
     ListArgs a;
     a.box = *box; a.p = *p; a.cells = *cells; a.list = *list; a.r_list2 = r_list2;

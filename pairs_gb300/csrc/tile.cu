@@ -161,8 +161,8 @@ __device__ void tile_stage(const TileArgs &a, const TileRec &r, float4 *sm) {
         const float hx = sx * a.box.len_hi[0], hy = sy * a.box.len_hi[1], hz = sz * a.box.len_hi[2];
         const float lx = sx * a.box.len_lo[0], ly = sy * a.box.len_lo[1], lz = sz * a.box.len_lo[2];
         for(int k = threadIdx.x; k < g.count; k += blockDim.x) {
-            float4 h = ld_f4(a.p.pos_hi, g.start + k);
-            float4 l = ld_f4(a.p.pos_lo, g.start + k);
+            float4 h = ld_f4(a.p.pos_hi, hl(a.p, g.start + k));
+            float4 l = ld_f4(a.p.pos_lo, hl(a.p, g.start + k));
             h.x += hx; h.y += hy; h.z += hz;
             l.x += lx; l.y += ly; l.z += lz;
             sm[2 * (g.base + k)] = h;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_build(TileArgs a) {
     const int stride = a.list.stride, cap = a.list.max_neighbors;
     int wmax = 0;
     for(int i = r.ib + threadIdx.x; i < r.ie; i += blockDim.x) {
-        const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+        const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
         const D4 xi = ld_d4(a.p.pos, i);
         st_d4(a.p.pos_ref, i, xi);
         st_f4(a.p.ref_hi, i, hi);
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_build(TileArgs a) {
                     for(int js = b; js < e; js++) {
                         const int j = g.start + (js - g.base);
                         if(j == i && g.code == 0) { continue; }
-                        float4 hj = ld_f4(a.p.pos_hi, j), lj = ld_f4(a.p.pos_lo, j);
+                        float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
                         hj.x += shx; hj.y += shy; hj.z += shz;
                         lj.x += slx; lj.y += sly; lj.z += slz;
                         const float fx = (hi.x - hj.x) + (lo.x - lj.x);
@@ -282,12 +282,12 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_lj(TileArgs a) {
         float fx = 0.f, fy = 0.f, fz = 0.f;
         const bool live = i < r.ie && !(a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed));
         if(live) {
-            const float4 hi = ld_f4(a.p.pos_hi, i), lo = ld_f4(a.p.pos_lo, i);
+            const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
             const int ti = kOneType ? 0 : __float_as_int(hi.w) * a.lj.ntypes;
             const int cnt = a.list.count[i];
             const uint16_t *nb = a.list.nbr16 + i;
             for(int k = lane; k < cnt; k += TPA) {
-                const int js = __ldg(nb + (size_t) k * stride);
+                const int js = __ldcs(nb + (size_t) k * stride);
                 const float4 hj = sm[2 * js], lj = sm[2 * js + 1];
                 const float dx = (hi.x - hj.x) + (lo.x - lj.x);
                 const float dy = (hi.y - hj.y) + (lo.y - lj.y);

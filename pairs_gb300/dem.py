@@ -185,9 +185,13 @@ def plan_dem(sim):
 
 
 def dem_params(dt, kappa, ln_e, tc, drho, gravity, friction_static, friction_dynamic, pi=math.pi, ntypes=1,
-               skin=0.0):
+               skin=0.0, kn=0.0):
+    """Contact-model constants.  kn = 0: normal stiffness from the collision time tc
+    (examples/dem.py:22-26); kn > 0: that fixed stiffness, damping from the
+    restitution coefficient (ln_e)."""
     p = A.PgDemParams()
     p.dt, p.pi, p.kappa, p.ln_e, p.tc, p.drho, p.gravity, p.skin = dt, pi, kappa, ln_e, tc, drho, gravity, skin
+    p.kn = kn
     p.ntypes = ntypes
     fs = list(friction_static)
     fd = list(friction_dynamic)
@@ -205,7 +209,7 @@ class DEMEngine:
     CONTACT = ("ccount", "partner", "sticking", "history")
 
     def __init__(self, state, *, lo, hi, periodic=(True, True, False), params, skin=None, contact_capacity=20,
-                 neighbor_capacity=32, policy="guard", chunk=None, capacity=None, device="cuda"):
+                 neighbor_capacity=32, policy="guard", chunk=None, capacity=None, device="cuda", precision="fp64"):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -213,6 +217,7 @@ class DEMEngine:
             raise ValueError(f"unknown DEM rebuild policy {policy!r}")
         self.dev = torch.device(device)
         self.policy = policy
+        self.precision = {"fp64": A.PG_FP64, "mixed": A.PG_MIXED}[precision]
         pos = np.asarray(state["pos"], dtype=np.float64).reshape(-1, 3)
         n = len(pos)
         self.n = n
@@ -248,6 +253,7 @@ class DEMEngine:
         t = self.t = {}
         for name in ("pos", "force", "torque", "pos_ref"):
             t[name] = z((cap, 4), f64)
+        t["pos32"] = z((cap, 4), torch.float32)
         for name in ("uid", "flags"):
             t[name] = z((cap,), i32)
         self.sets = []
@@ -367,7 +373,7 @@ class DEMEngine:
         t, cur, spare = self.t, self.sets[0], self.sets[1]
         for st, s, c in ((self.d, cur, self.c), (self.spare, spare, self.spare_c)):
             st.n, st.capacity = self.n, self.cap
-            for name in ("pos", "force", "torque", "pos_ref", "uid", "flags"):
+            for name in ("pos", "force", "torque", "pos_ref", "uid", "flags", "pos32"):
                 setattr(st, name, t[name].data_ptr())
             for name in ("vel", "angvel", "quat", "normal", "mass", "radius", "inv_inertia", "type", "shape"):
                 setattr(st, name, s[name].data_ptr())
@@ -417,7 +423,7 @@ class DEMEngine:
     def _force(self, step):
         self.d.step = step
         A.call("pg_dem_force", C.byref(self.box), C.byref(self.d), C.byref(self.cells), C.byref(self.list),
-               C.byref(self.c), C.byref(self.prm), self.status_ptr, self.sh)
+               C.byref(self.c), C.byref(self.prm), self.precision, self.status_ptr, self.sh)
 
     def _euler(self, step):
         self.d.step = step

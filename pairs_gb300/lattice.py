@@ -265,3 +265,26 @@ def ensemble_configs(count=512, nmin=500, nmax=32000, rho=(0.6, 0.9), temperatur
     rhos = g.uniform(rho[0], rho[1], count)
     temps = g.uniform(temperature[0], temperature[1], count)
     return [dict(natoms=int(s), rho=float(r), temperature=float(t)) for s, r, t in zip(sizes, rhos, temps)]
+
+
+def dem_random_packing(count, box, rmin, rmax, density, seed=7, spacing=None):
+    """`count` spheres, radii uniform in [rmin, rmax], at random non-overlapping
+    positions in `box` (lower corner at the origin), filled from the bottom up: one
+    sphere per site of a cubic lattice of spacing >= 2 rmax, jittered uniformly by
+    up to (spacing/2 - r) per axis so it stays inside its own site cube.  numpy
+    PCG64 with `seed`; mass 4/3 pi r^3 density, zero velocity, uid 1..count."""
+    s = float(spacing or 2.0 * rmax * 1.05)
+    nx, ny, nz = (int(math.floor(box[d] / s)) for d in range(3))
+    if nx * ny * nz < count:
+        raise ValueError(f"box holds only {nx * ny * nz} sites of spacing {s}")
+    g = np.random.default_rng(seed)
+    k = np.arange(count)
+    ix, iy, iz = k % nx, (k // nx) % ny, k // (nx * ny)
+    r = g.uniform(rmin, rmax, count)
+    room = (0.5 * s - r)[:, None]
+    jitter = g.uniform(-1.0, 1.0, (count, 3)) * room
+    pos = (np.stack([ix, iy, iz], axis=1) + 0.5) * s + jitter
+    mass = (4.0 / 3.0) * math.pi * r * r * r * density
+    return dict(pos=pos, vel=np.zeros((count, 3)), mass=mass, radius=r, type=np.zeros(count, np.int32),
+                uid=np.arange(1, count + 1, dtype=np.int32), flags=np.zeros(count, np.int32),
+                shape=np.zeros(count, np.int32))

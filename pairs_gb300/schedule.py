@@ -63,6 +63,8 @@ class LearnedSchedule:
         self.adam_t = 0
         self.out = torch.zeros(self.ncells, dtype=torch.float32, device=dev)
         self.result = torch.zeros(4, dtype=torch.float32, device=dev)
+        self.result_host = torch.zeros(4, dtype=torch.float32).pin_memory()
+        self._next = None
         self.loss = torch.zeros(1, dtype=torch.float32, device=dev)
         self.feat = torch.zeros((max_samples, self.ncells, 4), dtype=torch.float32, device=dev)
         self.feat_all = torch.zeros((self.ncells_all, 4), dtype=torch.float32, device=dev)
@@ -77,11 +79,12 @@ class LearnedSchedule:
         return C.c_void_p(t.data_ptr())
 
     # ---------------------------------------------------------------- features / prediction
-    def features_into(self, slot):
+    def features_into(self, slot, since=None):
         """Per-cell features of the current state; the sample keeps the `ncells`
         cells with the fastest particle (the soft minimum is decided there)."""
         e = self.e
-        A.call("pg_cell_features", C.byref(e.p), C.byref(e.cells), e.precision, e.since_build, e.dt,
+        since = e.since_build if since is None else since
+        A.call("pg_cell_features", C.byref(e.p), C.byref(e.cells), e.precision, since, e.dt,
                0.5 * e.skin, self._ptr(self.feat_all), e.sh)
         if self.ncells == self.ncells_all:
             self.feat[slot].copy_(self.feat_all)
@@ -111,6 +114,30 @@ class LearnedSchedule:
         slot = self._slot()
         self.features_into(slot)
         self.pending.append((slot, step))
+
+    def sample_at_build(self, predict):
+        """Features of the state at a list rebuild, taken before the particles are
+        re-sorted (so velocities and forces still belong to the same particles), as
+        the first sample of the new cycle (steps since the build = 0).  With
+        `predict`, also queue the network's prediction; its value is copied to host
+        memory with the rebuild's own status read.  Returns the sample's slot."""
+        slot = self._slot()
+        self.features_into(slot, since=0)
+        if predict:
+            self.predict_log(slot)
+            self.result_host.copy_(self.result, non_blocking=True)
+        self._next = slot
+        return slot
+
+    def open_cycle(self, step):
+        """Start the new cycle with the sample taken at its build."""
+        if self._next is not None:
+            self.pending.append((self._next, step))
+            self._next = None
+
+    def predicted(self):
+        """Predicted steps of the new cycle (after the rebuild's status read)."""
+        return math.exp(float(self.result_host[0]))
 
     def close_cycle(self, trip_step, end_step):
         """Label the open cycle: tripped at trip_step (exact), or censored at end_step."""

@@ -160,3 +160,75 @@ def test_skin_list_equals_every_step_rebinning():
     ia, _ = a.contacts()
     ib, _ = b.contacts()
     assert np.array_equal(ia, ib)
+
+
+# ---------------------------------------------------------------------------- granular workload model
+
+def granular_setup(count=900, seed=3, v=2.0):
+    """A small version of the 1M-sphere granular workload: radii U[0.4, 0.6] mm,
+    2500 kg/m^3, fixed normal stiffness 1e5 N/m, restitution 0.7, friction 0.5,
+    dt 1e-6 s, bottom plane; random initial velocities so contacts form quickly."""
+    import math
+    from pairs_gb300 import lattice
+    a = 0.0082
+    box = (a, a, 4 * a)
+    st = lattice.dem_random_packing(count, box, 4e-4, 6e-4, 2500, seed=seed, spacing=a / 6.5)
+    g = np.random.default_rng(seed)
+    st["vel"] = g.uniform(-v, v, (count, 3))
+    e = 0.7
+    p = dict(dt=1e-6, mu=0.5, e=e, tc=5e-4, poisson=0.22, rho_p=2500, rho_f=0, gravity=9.81, diameter=1.2e-3)
+    p["kappa"] = 2.0 * (1.0 - p["poisson"]) / (2.0 - p["poisson"])
+    p["ln_e"] = math.log(e)
+    p["cell"] = 1.01 * 1.2e-3
+    planes = [[count + 1, 0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 13]]
+    return box, st, p, planes
+
+
+def granular_engine(sim, p, box, precision):
+    from pairs_gb300.dem import DEMEngine, dem_params
+    ini = sim.initial()
+    uid = np.sort(ini["uid"])
+    st = sim.state(uid)
+    order = np.argsort(ini["uid"], kind="stable")
+    state = dict(uid=uid, type=ini["type"][order], flags=ini["flags"][order], shape=ini["shape"][order],
+                 mass=ini["mass"][order], radius=ini["radius"][order], normal=ini["normal"][order],
+                 pos=st["pos"], vel=st["vel"], angvel=st["angvel"], quat=st["quat"], contacts=sim.contacts())
+    prm = dem_params(p["dt"], p["kappa"], p["ln_e"], p["tc"], 2500.0, p["gravity"], [0.0], [p["mu"]], kn=1e5)
+    return DEMEngine(state, lo=[0, 0, 0], hi=box, periodic=(True, True, False), params=prm, policy="every",
+                     precision=precision)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-5)])
+def test_fixed_stiffness_model_one_step(precision, tol):
+    """The fixed-stiffness contact model (FP64 and mixed) against the oracle's."""
+    box, st, p, planes = granular_setup()
+    sim = dem.Sim(box, planes, p, spheres=st, kn=1e5)
+    sim.run(200)
+    ids, _ = sim.contacts()
+    assert len(ids) > 20                          # colliding pairs exist at this step
+    eng = granular_engine(sim, p, box, precision)
+    sim.step()
+    eng.run(1)
+    got = eng.state()
+    ref = sim.state(got["uid"])
+    for k in ("force", "torque"):
+        assert rel(got[k], ref[k]) < tol, (k, rel(got[k], ref[k]))
+    assert np.array_equal(got["ncontacts"], ref["ncontacts"])
+    gi, gv = eng.contacts()
+    ri, rv = sorted_contacts(*sim.contacts())
+    assert np.array_equal(gi[:, :2], ri[:, :2])
+    assert rel(gv[:, 3], rv[:, 3]) < tol
+
+
+def test_mixed_run_tracks_fp64():
+    box, st, p, planes = granular_setup(seed=5)
+    sim = dem.Sim(box, planes, p, spheres=st, kn=1e5)
+    sim.run(300)
+    a = granular_engine(sim, p, box, "fp64")
+    b = granular_engine(sim, p, box, "mixed")
+    a.run(300)
+    b.run(300)
+    sa, sb = a.state(), b.state()
+    L = box
+    assert np.abs(wrap(sa["pos"], L) - wrap(sb["pos"], L)).max() < 1e-9      # metres; radii are 4e-4..6e-4
+    assert rel(sb["vel"], sa["vel"]) < 1e-4

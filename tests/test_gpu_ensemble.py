@@ -53,7 +53,7 @@ def test_replica_follows_single_system_engine():
     from pairs_gb300.engine import LJEngine
     from pairs_gb300.ensemble import Ensemble
     reps = replicas()
-    ens = Ensemble(reps, tpa=1, reach=1, policy="every")
+    ens = Ensemble(reps, tpa=1, reach=1, policy="every")      # the engine's 27-cell stencil
     ens.run(25)
     ens.synchronize()
     worst = 0.0
