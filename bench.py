@@ -132,7 +132,8 @@ def run_ours(args, rank, world, dist):
 
     def make(precision, half, policy):
         return LJEngine(st, precision=precision, half=half, sync="exact", every=20, policy=policy,
-                        device=str(dev), tiles=tiles if precision == "mixed" else None, tile_tpa=args.tile_tpa)
+                        device=str(dev), tiles=tiles if precision == "mixed" else None, tile_tpa=args.tile_tpa,
+                        fixed_point={"auto": None, "on": True, "off": False}[args.fixed_point])
 
     def kernel_times(eng, k):
         stream = eng.stream
@@ -211,13 +212,14 @@ def run_ours(args, rank, world, dist):
     eng.settle()
     fms = kernel_times(eng, 20)
     pairs_total = int(eng.t["count"][:n].sum().item())
-    # algorithmic bytes of one force launch: own position (32: FP32 hi+lo, or FP64
-    # x,y,z,pad), neighbour count (4), force write (16 FP32 / 32 FP64), one Verlet
+    # algorithmic bytes of one force launch: own position (16 fixed point, 32 FP32 hi+lo
+    # or FP64 x,y,z,pad), neighbour count (4), force write (16 FP32 / 32 FP64), one Verlet
     # entry per pair (4 bytes global, 2 bytes tile-local); a half list adds one
     # reaction write per particle (b_F)
     b_f = 16 if prec == "mixed" else 32
     b_entry = 2 if eng.list.nbr16 else 4
-    b_force = n * (32 + 4 + b_f) + b_entry * pairs_total + (n * b_f if eng.list.half else 0)
+    b_pos = 16 if (prec == "mixed" and eng.fixed_point) else 32     # fixed point: one int4
+    b_force = n * (b_pos + 4 + b_f) + b_entry * pairs_total + (n * b_f if eng.list.half else 0)
     kname = ("k_tile_lj" if eng.list.nbr16 else ("k_lj_mixed" if prec == "mixed" else "k_lj_fp64"))
     f_avg = statistics.mean(fms) if fms else float("nan")
     pk, pk_kind = peaks()
@@ -569,6 +571,9 @@ def main():
                     help="mixed path, full lists: 16-bit shared-memory tile lists or global lists (auto = off)")
     ap.add_argument("--tile-tpa", type=int, default=2, choices=[1, 2, 4],
                     help="threads per atom of the tile force kernel")
+    ap.add_argument("--fixed-point", choices=["auto", "on", "off"], default="auto",
+                    help="FP32 position layout: fixed point (2^32 units per box length, one 16-byte record "
+                         "per partner) or compensated hi/lo pairs (auto = fixed point where the box allows)")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline arm only (profiling runs)")
     args = ap.parse_args()

@@ -28,6 +28,9 @@
  *   float4  pos_hi[n], pos_lo[n]   compensated FP32 positions: hi on a 2^-k grid so
  *                      hi differences and periodic shifts are exact in FP32, lo the
  *                      FP32 residual x - hi
+ *   int4    pos_fx[n]  fixed-point positions (precision PG_MIXED, periodic boxes of
+ *                      at least 4 cells per axis): 2^32 units per box length, so
+ *                      periodic images need no shift; replaces pos_hi/pos_lo there
  *   int     nbr[k * stride + i]    Verlet entry k of particle i (column-major, as
  *                      the reference's GPU layout, sim/neighbor_lists.py:14); bits
  *                      0-25 the partner index, bits 26-31 the periodic image code
@@ -84,6 +87,9 @@ typedef struct {
     float  len_hi[3];            /* len split on the compensated FP32 grid */
     float  len_lo[3];
     double quantum;              /* grid step of pos_hi (a power of two) */
+    double fx_scale[3];          /* 2^32 / len: fixed-point units per length (pos_fx) */
+    float  fx_unit[3];           /* len / 2^32 rounded to FP32: length of one unit */
+    int32_t fx_pad_;
 } pg_box;
 
 /* Per-particle state, sorted order.  Optional arrays may be NULL. */
@@ -101,6 +107,14 @@ typedef struct {
     double *pos_ref;             /* double4[capacity] positions at last rebuild (guard) */
     float  *ref_hi;              /* float4[capacity]  pos_hi at last rebuild (guard screen) */
     float  *ref_lo;              /* float4[capacity]  pos_lo at last rebuild */
+    int32_t *pos_fx;             /* int4[capacity] or NULL (PG_MIXED): fixed-point positions,
+                                    x_fx = round((x - lo) * fx_scale) mod 2^32 per axis, w =
+                                    type.  A box length is 2^32 units, so the wrapped 32-bit
+                                    difference of two coordinates is their minimum-image
+                                    separation; used instead of pos_hi/pos_lo when every
+                                    axis is periodic and has at least 4 cells (6 with
+                                    reach 2) */
+    int32_t *ref_fx;             /* int4[capacity] pos_fx at last rebuild (guard screen) */
     double *mass;                /* [capacity] */
     int32_t *type;               /* [capacity] */
     int32_t *uid;                /* [capacity] user id (the reference's uid property) */
@@ -314,7 +328,9 @@ int pg_bin_particles_noalloc(const pg_box *box, pg_particles *p, pg_cells *cells
  * sim/neighbor_lists.py:21-48 with interaction.py:90-120).  The acceptance test
  * rsq < r_list2 is evaluated exactly as the reference: FP64, image position
  * fl(x_j + s*len), delta, (dx*dx + dy*dy) + dz*dz, no fused multiply-add.  Also
- * records pos_ref for the displacement guard. */
+ * records pos_ref (and ref_hi/ref_lo or ref_fx) for the displacement guard.  The FP32
+ * screen reads pos_fx when it is set and the box allows it (every axis periodic with
+ * at least 4 cells, 6 with reach 2), else pos_hi/pos_lo. */
 int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                             pg_neighbor_list *list, double r_list2, pg_status *status,
                             void *stream);
@@ -324,7 +340,11 @@ int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_c
  * precision PG_FP64 writes p->force, PG_MIXED writes p->force32.  sync_mode selects
  * PG_SYNC_EXACT or PG_SYNC_REFERENCE (FP64 only).  energy, if not NULL, is a device
  * double[2] that receives potential energy and virial sum r.F (FP64 sums).  cells
- * is needed for nbr16 (tile) lists and may be NULL otherwise. */
+ * is needed for nbr16 (tile) lists and may be NULL otherwise.  On the PG_MIXED path a
+ * pair whose FP32 rsq lies within a relative 1e-5 of the cutoff is decided by the
+ * FP64 test of the PG_FP64 path, so both paths apply the force of the same pairs;
+ * such pairs are queued in ws (scratch, at least 8448 bytes; the binning workspace
+ * serves) and applied by a second kernel. */
 int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                 const pg_neighbor_list *list, const pg_lj_params *lj, int precision, int sync_mode,
                 double *energy, pg_workspace ws, void *stream);
@@ -336,7 +356,7 @@ int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
  * precision selects which force array is read.  The initial step also tests every
  * particle's displacement since the last list build against half_skin2 in FP64
  * (the guard; the first offending step is kept in status->guard_tripped) and
- * refreshes pos_hi/pos_lo when present.  With sync_mode PG_SYNC_REFERENCE the caller
+ * refreshes pos_hi/pos_lo and pos_fx when present.  With sync_mode PG_SYNC_REFERENCE the caller
  * rotates the position ring first (prev2 <- prev1 <- pos <- old prev2); the kernel
  * then reads pos_prev1 and writes pos. */
 int pg_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,
@@ -352,9 +372,9 @@ int pg_final_initial_integrate(const pg_box *box, pg_particles *p, double dt, in
 
 /* Mixed-precision integration (FP32 force in, FP64 velocity/position update):
  * kicks = 1 or 2 half kicks merged into one (v += kicks*(dt/2)*F/m), then, if drift,
- * x += dt*v in FP64, pos_hi/pos_lo re-split from the new x, and the FP64
- * displacement guard (screened in FP32 against ref_hi/ref_lo, decided in FP64 near
- * the threshold) recorded in status->guard_tripped. */
+ * x += dt*v in FP64, pos_hi/pos_lo re-split (or pos_fx rounded) from the new x, and
+ * the FP64 displacement guard (screened in FP32 against ref_hi/ref_lo or ref_fx,
+ * decided in FP64 near the threshold) recorded in status->guard_tripped. */
 int pg_integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks, int drift,
                        double half_skin2, int32_t step, pg_status *status, void *stream);
 
@@ -364,7 +384,8 @@ int pg_integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks,
 int pg_compute_thermo(const pg_box *box, const pg_particles *p, double *out,
                       pg_workspace ws, void *stream);
 
-/* Refresh pos_hi / pos_lo from pos (after a host upload or a permutation). */
+/* Refresh pos_hi / pos_lo and pos_fx (those present) from pos (after a host upload
+ * or a permutation). */
 int pg_split_positions(const pg_box *box, pg_particles *p, void *stream);
 
 /* dst[k] = src[perm[k]] for k < n, elements of elem_bytes (4, 8, 16 or 32): applies
@@ -420,9 +441,11 @@ int pg_ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cell
                             double r_list2, pg_status *status, void *stream);
 
 /* Mixed-precision LJ forces (FP32 on compensated positions) for every replica,
- * tpa threads per particle, full lists. */
+ * tpa threads per particle, full lists.  Pairs within a relative 1e-5 of the cutoff
+ * are decided by the FP64 test, as in pg_lj_force, through a queue in ws (scratch, at
+ * least 8448 bytes; the binning workspace serves). */
 int pg_ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list,
-                      const pg_lj_params *lj, void *stream);
+                      const pg_lj_params *lj, pg_workspace ws, void *stream);
 
 /* pg_integrate_mixed for every replica (each re-splits on its own grid); the guard
  * word takes the first step at which any replica's particle moved > skin/2. */

@@ -36,7 +36,8 @@ class PgStatus(C.Structure):
 class PgBox(C.Structure):
     _fields_ = [("lo", C.c_double * 3), ("hi", C.c_double * 3), ("len", C.c_double * 3),
                 ("periodic", C.c_int * 3), ("len_hi", C.c_float * 3), ("len_lo", C.c_float * 3),
-                ("quantum", C.c_double)]
+                ("quantum", C.c_double), ("fx_scale", C.c_double * 3), ("fx_unit", C.c_float * 3),
+                ("fx_pad_", C.c_int32)]
 
 
 class PgParticles(C.Structure):
@@ -44,7 +45,8 @@ class PgParticles(C.Structure):
                 ("pos", C.c_void_p), ("pos_prev1", C.c_void_p), ("pos_prev2", C.c_void_p),
                 ("vel", C.c_void_p), ("force", C.c_void_p), ("force32", C.c_void_p),
                 ("pos_hi", C.c_void_p), ("pos_lo", C.c_void_p), ("pos_ref", C.c_void_p),
-                ("ref_hi", C.c_void_p), ("ref_lo", C.c_void_p),
+                ("ref_hi", C.c_void_p), ("ref_lo", C.c_void_p), ("pos_fx", C.c_void_p),
+                ("ref_fx", C.c_void_p),
                 ("mass", C.c_void_p), ("type", C.c_void_p), ("uid", C.c_void_p),
                 ("flags", C.c_void_p), ("guard", C.c_void_p), ("step", C.c_int32), ("hilo_stride", C.c_int32)]
 
@@ -150,7 +152,7 @@ SIGNATURES = {
     "pg_ensemble_build_lists": (C.c_int, [P(PgEnsemble), P(PgParticles), P(PgCells), P(PgNeighborList),
                                           C.c_double, C.c_void_p, C.c_void_p]),
     "pg_ensemble_force": (C.c_int, [P(PgEnsemble), P(PgParticles), P(PgNeighborList), P(PgLJParams),
-                                    C.c_void_p]),
+                                    PgWorkspace, C.c_void_p]),
     "pg_ensemble_integrate": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_double, C.c_int, C.c_int, C.c_double,
                                         C.c_int32, C.c_void_p, C.c_void_p]),
     "pg_ensemble_thermo": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_void_p, C.c_void_p]),

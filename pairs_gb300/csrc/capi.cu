@@ -10,7 +10,7 @@ int split_positions(const pg_box *box, pg_particles *p, cudaStream_t st);
 int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                          pg_neighbor_list *list, double r_list2, pg_status *status, cudaStream_t st);
 int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, const pg_neighbor_list *list,
-             const pg_lj_params *lj, int precision, int sync_mode, double *energy, cudaStream_t st);
+             const pg_lj_params *lj, int precision, int sync_mode, double *energy, pg_workspace ws, cudaStream_t st);
 int initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision, double half_skin2,
                       int32_t step, pg_status *status, int sync_mode, cudaStream_t st);
 int final_integrate(const pg_box *box, pg_particles *p, double dt, int precision, cudaStream_t st);
@@ -36,7 +36,7 @@ int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_work
 int ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                          double r_list2, pg_status *status, cudaStream_t st);
 int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
-                   cudaStream_t st);
+                   pg_workspace ws, cudaStream_t st);
 int ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift, double half_skin2,
                        int32_t step, pg_status *status, cudaStream_t st);
 int ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, cudaStream_t st);
@@ -93,8 +93,7 @@ int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_c
 int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                 const pg_neighbor_list *list, const pg_lj_params *lj, int precision, int sync_mode,
                 double *energy, pg_workspace ws, void *stream) {
-    (void) ws;
-    return pg::lj_force(box, p, cells, list, lj, precision, sync_mode, energy, S(stream));
+    return pg::lj_force(box, p, cells, list, lj, precision, sync_mode, energy, ws, S(stream));
 }
 
 int pg_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,
@@ -148,8 +147,8 @@ int pg_ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cell
 }
 
 int pg_ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list,
-                      const pg_lj_params *lj, void *stream) {
-    return pg::ensemble_force(e, p, list, lj, S(stream));
+                      const pg_lj_params *lj, pg_workspace ws, void *stream) {
+    return pg::ensemble_force(e, p, list, lj, ws, S(stream));
 }
 
 int pg_ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift,

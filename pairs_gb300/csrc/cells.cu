@@ -175,15 +175,19 @@ __global__ void k_split_positions(pg_box box, pg_particles p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= p.n) { return; }
     const D4 x = ld_d4_plain(p.pos, i);
-    const double q = box.quantum, iq = 1.0 / q;
-    float4 h, l;
-    split_pos(x.x, iq, q, h.x, l.x);
-    split_pos(x.y, iq, q, h.y, l.y);
-    split_pos(x.z, iq, q, h.z, l.z);
-    h.w = __int_as_float(p.type != nullptr ? p.type[i] : 0);
-    l.w = 0.0f;
-    st_f4(p.pos_hi, hl(p, i), h);
-    st_f4(p.pos_lo, hl(p, i), l);
+    const int type = p.type != nullptr ? p.type[i] : 0;
+    if(p.pos_hi != nullptr) {
+        const double q = box.quantum, iq = 1.0 / q;
+        float4 h, l;
+        split_pos(x.x, iq, q, h.x, l.x);
+        split_pos(x.y, iq, q, h.y, l.y);
+        split_pos(x.z, iq, q, h.z, l.z);
+        h.w = __int_as_float(type);
+        l.w = 0.0f;
+        st_f4(p.pos_hi, hl(p, i), h);
+        st_f4(p.pos_lo, hl(p, i), l);
+    }
+    if(p.pos_fx != nullptr) { st_i4(p.pos_fx, i, fx_position(box, x.x, x.y, x.z, type)); }
 }
 
 // workspace layout for pg_bin_particles (all offsets 256-byte aligned)
@@ -273,14 +277,15 @@ int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_worksp
     }
     rc = bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out);
     if(rc || n == 0) { return rc; }
-    if(p->pos_hi != nullptr && p->pos_lo != nullptr) {
+    if((p->pos_hi != nullptr && p->pos_lo != nullptr) || p->pos_fx != nullptr) {
         k_split_positions<<<blocks_for(n), kBlock, 0, st>>>(*box, *p); note_launch();
     }
     return launch_status();
 }
 
 int split_positions(const pg_box *box, pg_particles *p, cudaStream_t st) {
-    if(box == nullptr || p == nullptr || p->pos_hi == nullptr || p->pos_lo == nullptr) { return PG_ERR_ARGUMENT; }
+    if(box == nullptr || p == nullptr || (p->pos_hi == nullptr) != (p->pos_lo == nullptr) ||
+       (p->pos_hi == nullptr && p->pos_fx == nullptr)) { return PG_ERR_ARGUMENT; }
     if(p->n > 0) { k_split_positions<<<blocks_for(p->n), kBlock, 0, st>>>(*box, *p); note_launch(); }
     return launch_status();
 }

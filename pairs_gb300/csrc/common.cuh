@@ -87,6 +87,39 @@ __device__ __forceinline__ double ref_rsq(double dx, double dy, double dz) {
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
+// Cutoff decision of the FP32 force paths.  The truncated LJ force jumps by |F(rc)|
+// (0.039 at rc = 2.5) at the cutoff, so a pair within FP32 rounding of rc that one
+// precision counts and the other does not changes a force by that much.  A pair whose
+// FP32 rsq lies within a relative band of kCutBand around rc^2 is therefore decided by
+// the FP64 path's own test (the reference's rsq of the listed image, FP64 positions):
+// both precisions apply the force of exactly the same pairs.
+constexpr float kCutBand = 1.0e-5f;
+
+// FP64 position load for a rarely taken branch: volatile, so the compiler neither
+// hoists it out of the branch nor keeps it live in registers across a loop
+__device__ __forceinline__ D4 ld_d4_rare(const double *base, int i) {
+    const double *p = base + 4 * (size_t) i;
+    double x, y, z;
+    asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(x), "=d"(y) : "l"(p));
+    asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(z) : "l"(p + 2));
+    return make_d4(x, y, z, 0.0);
+}
+
+__device__ __forceinline__ bool exact_inside(const double *pos, int i, int j, uint32_t code, const double *len,
+                                             double cutoff2) {
+    const D4 xi = ld_d4_rare(pos, i), xj = ld_d4_rare(pos, j);
+    const double jx = ref_image(xj.x, image_shift(code, 0), len[0]);
+    const double jy = ref_image(xj.y, image_shift(code, 1), len[1]);
+    const double jz = ref_image(xj.z, image_shift(code, 2), len[2]);
+    return ref_rsq(__dsub_rn(xi.x, jx), __dsub_rn(xi.y, jy), __dsub_rn(xi.z, jz)) < cutoff2;
+}
+
+// Queue of near-cutoff pairs (particle, list entry) for a second, FP64-deciding pass.
+__device__ __forceinline__ void cut_queue_push(int32_t *count, int2 *rec, int capacity, int i, uint32_t e) {
+    const int slot = atomicAdd(count, 1);
+    if(slot < capacity) { rec[slot] = make_int2(i, (int) e); }
+}
+
 // --- compensated FP32 positions ------------------------------------------------
 // hi = x rounded to a multiple of the box quantum q (a power of two chosen so every
 // |hi| < 2^24 q): differences of hi values and of hi and len_hi are exact in FP32.
@@ -99,6 +132,85 @@ __device__ __forceinline__ void split_pos(double x, double inv_q, double q, floa
     const double h = rint(x * inv_q) * q;
     hi = (float) h;
     lo = (float) (x - h);
+}
+
+// FP32 reciprocal by the hardware approximation (PTX rcp.approx: at most 1 ulp from
+// the rounded reciprocal over the normal range), one instruction instead of the
+// correctly rounded sequence; the mixed-precision force paths use it.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// --- L2 eviction priorities for the force kernels' two streams ------------------
+// The Verlet list (hundreds of MB) is read once per pass; the positions it indexes
+// (16 bytes per particle) are read about 40 times each.  List loads take an L2
+// evict-first policy and skip L1; partner loads take evict-last in L2 and L1, so the
+// list stream does not push positions out of either cache.
+#ifndef PG_L2_HINTS
+#define PG_L2_HINTS 0
+#endif
+
+__device__ __forceinline__ uint64_t l2_policy_stream() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ uint64_t l2_policy_keep() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ int32_t ld_stream(const int32_t *a, uint64_t pol) {
+#if PG_L2_HINTS
+    int32_t v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+#else
+    return __ldcs(a);
+#endif
+}
+
+__device__ __forceinline__ int4 ld_keep_i4(const int32_t *base, int i, uint64_t pol) {
+#if PG_L2_HINTS
+    int4 v;
+    asm("ld.global.nc.L1::evict_last.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(reinterpret_cast<const int4 *>(base) + i), "l"(pol));
+    return v;
+#else
+    return __ldg(reinterpret_cast<const int4 *>(base) + i);
+#endif
+}
+
+// --- fixed-point positions (pg_particles.pos_fx) ---------------------------------
+// x_fx = round((x - lo) * 2^32 / len) mod 2^32 per axis.  One box length is 2^32
+// units, so the wrapped 32-bit difference of two coordinates is the minimum-image
+// separation in units, exact as an integer whenever that separation is below half a
+// box length; no periodic shift is needed.  The unit (len / 2^32 = 2.5e-8 at len =
+// 107.5) is far below the FP32 rounding of a pair distance near 1, and the integer
+// difference converts to FP32 with one rounding.
+
+__device__ __forceinline__ int32_t to_fx(double x, double lo, double scale) {
+    return (int32_t) (uint32_t) (unsigned long long) __double2ll_rn((x - lo) * scale);
+}
+
+__device__ __forceinline__ int4 fx_position(const pg_box &box, double x, double y, double z, int type) {
+    return make_int4(to_fx(x, box.lo[0], box.fx_scale[0]), to_fx(y, box.lo[1], box.fx_scale[1]),
+                     to_fx(z, box.lo[2], box.fx_scale[2]), type);
+}
+
+// wrapped difference a - b of two fixed-point coordinates
+__device__ __forceinline__ int fx_diff(int32_t a, int32_t b) { return (int) ((uint32_t) a - (uint32_t) b); }
+
+__device__ __forceinline__ int4 ld_i4(const int32_t *base, int i) {
+    return __ldg(reinterpret_cast<const int4 *>(base) + i);
+}
+
+__device__ __forceinline__ void st_i4(int32_t *base, int i, int4 v) {
+    reinterpret_cast<int4 *>(base)[i] = v;
 }
 
 // Speculative stepping (see pg_particles.guard): a force pass of step p.step is
@@ -116,6 +228,7 @@ __device__ __forceinline__ bool frozen_integrate(const pg_particles &p) {
 struct LJTableF {
     int ntypes;
     float cutoff2;
+    double cutoff2d;             // the FP64 cutoff test near rc (kCutBand)
     float eps[64];
     float sig6[64];
 };

@@ -35,6 +35,10 @@ struct EnsArgs {
     float r2_lo, r2_hi;
     int ntypes;
     float cutoff2;
+    double cutoff2d;             // FP64 cutoff test near rc (kCutBand)
+    int32_t *cut_count;          // queue of near-cutoff pairs (particle, list entry)
+    int2 *cut_rec;
+    int cut_capacity;
     float eps[64];
     float sig6[64];
     // integration
@@ -188,6 +192,32 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
 
 // ------------------------------------------------------------------ force
 
+// FP32 separation of particle i and list entry e (compensated hi/lo, the replica's
+// exact image shift)
+__device__ __forceinline__ void ens_delta(const pg_replica &R, float4 hi, float4 lo, float4 hj, float4 lj, uint32_t code,
+                                          float &dx, float &dy, float &dz) {
+    float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
+    float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
+    if(code != 0u) {
+        const int sx = image_shift(code, 0), sy = image_shift(code, 1), sz = image_shift(code, 2);
+        dhx -= sx * R.len_hi[0]; dlx -= sx * R.len_lo[0];
+        dhy -= sy * R.len_hi[1]; dly -= sy * R.len_lo[1];
+        dhz -= sz * R.len_hi[2]; dlz -= sz * R.len_lo[2];
+    }
+    dx = dhx + dlx; dy = dhy + dly; dz = dhz + dlz;
+}
+
+__device__ __forceinline__ float ens_lj(const EnsArgs &a, int tij, float rsq) {
+    const float sr2 = rcp_approx(rsq);
+    const float sr6 = sr2 * sr2 * sr2 * a.sig6[tij];
+    return 48.0f * sr6 * (sr6 - 0.5f) * sr2 * a.eps[tij];
+}
+
+// Entries are taken in batches of kEnsBatch per thread: the batch's list words and
+// partner positions are loaded before its pairs are computed.  A pair within kCutBand
+// of the cutoff is queued for k_ens_cutoff_fixup, which decides it in FP64.
+constexpr int kEnsBatch = 4;
+
 template<int TPA, bool kOneType>
 __global__ void k_ens_force(EnsArgs a) {
     if(frozen_force(a.p)) { return; }
@@ -197,34 +227,44 @@ __global__ void k_ens_force(EnsArgs a) {
     if(i < a.p.n) {
         const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
         const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
-        const float lhx = R.len_hi[0], lhy = R.len_hi[1], lhz = R.len_hi[2];
-        const float llx = R.len_lo[0], lly = R.len_lo[1], llz = R.len_lo[2];
         const int ti = kOneType ? 0 : __float_as_int(hi.w) * a.ntypes;
         const int cnt = a.list.count[i];
+        const int rows = cnt > t ? (cnt - t + TPA - 1) / TPA : 0;      // this lane's entries
         const int32_t *nb = a.list.nbr + (size_t) i * TPA + t;
         const size_t row = (size_t) a.list.stride * TPA;
-        const float c2 = a.cutoff2;
-        for(int k = t, r = 0; k < cnt; k += TPA, r++) {
-            const uint32_t e = (uint32_t) __ldcs(nb + r * row);
-            const int j = (int) (e & PG_NBR_INDEX_MASK);
-            const uint32_t code = e >> PG_NBR_INDEX_BITS;
-            const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
-            float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
-            float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
-            if(code != 0u) {
-                const int sx = image_shift(code, 0), sy = image_shift(code, 1), sz = image_shift(code, 2);
-                dhx -= sx * lhx; dlx -= sx * llx;
-                dhy -= sy * lhy; dly -= sy * lly;
-                dhz -= sz * lhz; dlz -= sz * llz;
+        const float c2 = a.cutoff2, band = c2 * kCutBand;
+        for(int r0 = 0; r0 < rows; r0 += kEnsBatch) {
+            uint32_t e[kEnsBatch];
+            float4 hj[kEnsBatch], lj[kEnsBatch];
+#pragma unroll
+            for(int u = 0; u < kEnsBatch; u++) {
+                e[u] = r0 + u < rows ? (uint32_t) __ldcs(nb + (r0 + u) * row) : 0u;
             }
-            const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
-            const float rsq = dx * dx + dy * dy + dz * dz;
-            if(rsq < c2) {
-                const int tij = kOneType ? 0 : ti + __float_as_int(hj.w);
-                const float sr2 = __frcp_rn(rsq);
-                const float sr6 = sr2 * sr2 * sr2 * a.sig6[tij];
-                const float f = 48.0f * sr6 * (sr6 - 0.5f) * sr2 * a.eps[tij];
-                fx += dx * f; fy += dy * f; fz += dz * f;
+#pragma unroll
+            for(int u = 0; u < kEnsBatch; u++) {
+                const int j = (int) (e[u] & PG_NBR_INDEX_MASK);
+                hj[u] = ld_f4(a.p.pos_hi, hl(a.p, j));
+                lj[u] = ld_f4(a.p.pos_lo, hl(a.p, j));
+            }
+            uint32_t pending = 0u;
+#pragma unroll
+            for(int u = 0; u < kEnsBatch; u++) {
+                if(r0 + u >= rows) { continue; }
+                float dx, dy, dz;
+                ens_delta(R, hi, lo, hj[u], lj[u], e[u] >> PG_NBR_INDEX_BITS, dx, dy, dz);
+                const float rsq = dx * dx + dy * dy + dz * dz;
+                const bool near = fabsf(rsq - c2) < band;
+                if(rsq < c2 && !near) {
+                    const float f = ens_lj(a, kOneType ? 0 : ti + __float_as_int(hj[u].w), rsq);
+                    fx += dx * f; fy += dy * f; fz += dz * f;
+                }
+                if(near) { pending |= 1u << u; }
+            }
+            if(pending != 0u) {
+#pragma unroll
+                for(int u = 0; u < kEnsBatch; u++) {
+                    if(pending & (1u << u)) { cut_queue_push(a.cut_count, a.cut_rec, a.cut_capacity, i, e[u]); }
+                }
             }
         }
     }
@@ -238,13 +278,36 @@ __global__ void k_ens_force(EnsArgs a) {
     if(i < a.p.n && t == 0) { st_f4(a.p.force32, i, make_float4(fx, fy, fz, 0.0f)); }
 }
 
+// Queued near-cutoff pairs: the FP64 test of the single-system FP64 path decides;
+// a pair inside adds its FP32 force (full lists: no reaction).
+template<bool kOneType>
+__global__ void __launch_bounds__(kBlock) k_ens_cutoff_fixup(EnsArgs a) {
+    if(frozen_force(a.p)) { return; }
+    const int total = min(*a.cut_count, a.cut_capacity);
+    for(int r = blockIdx.x * blockDim.x + threadIdx.x; r < total; r += gridDim.x * blockDim.x) {
+        const int2 q = a.cut_rec[r];
+        const int i = q.x;
+        const uint32_t e = (uint32_t) q.y;
+        const int j = (int) (e & PG_NBR_INDEX_MASK);
+        const uint32_t code = e >> PG_NBR_INDEX_BITS;
+        const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
+        if(!exact_inside(a.p.pos, i, j, code, R.len, a.cutoff2d)) { continue; }
+        const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
+        const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+        float dx, dy, dz;
+        ens_delta(R, hi, lo, hj, lj, code, dx, dy, dz);
+        const int tij = kOneType ? 0 : __float_as_int(hi.w) * a.ntypes + __float_as_int(hj.w);
+        const float f = ens_lj(a, tij, dx * dx + dy * dy + dz * dz);
+        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
+                     :: "l"(a.p.force32 + 4 * (size_t) i), "f"(dx * f), "f"(dy * f), "f"(dz * f), "f"(0.0f) : "memory");
+    }
+}
+
 // ------------------------------------------------------------------ integrate
 
+// grid point nearest x, rounded in FP64 so that |lo| <= q/2 (the packed residual's range)
 __device__ __forceinline__ void ens_resplit(double x, float q, float iq, float &hi, float &lo) {
-    const float xf = (float) x;
-    const float h = rintf(xf * iq) * q;
-    hi = h;
-    lo = (float) (x - (double) h);
+    split_pos(x, (double) iq, (double) q, hi, lo);
 }
 
 __global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
@@ -369,7 +432,7 @@ static void launch_force(const EnsArgs &a, int n, int block, bool one, cudaStrea
 }
 
 int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
-                   cudaStream_t st) {
+                   pg_workspace ws, cudaStream_t st) {
     if(!ens_ok(e, p) || !list || !list->nbr || !list->count || !lj || !p->pos_hi || !p->pos_lo || !p->force32 ||
        lj->ntypes < 1 || lj->ntypes > 8 || (lj->ntypes > 1 && !p->type)) {
         return PG_ERR_ARGUMENT;
@@ -378,11 +441,18 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
     a.e = *e; a.p = *p; a.list = *list;
     a.ntypes = lj->ntypes;
     a.cutoff2 = (float) lj->cutoff2;
+    a.cutoff2d = lj->cutoff2;
     for(int k = 0; k < lj->ntypes * lj->ntypes; k++) {
         a.eps[k] = (float) lj->epsilon[k];
         a.sig6[k] = (float) lj->sigma6[k];
     }
     if(p->n == 0) { return PG_OK; }
+    // queue of near-cutoff pairs in the workspace (scratch between binnings)
+    if(ws.ptr == nullptr || ws.bytes < 256 + 8 * 1024) { return PG_ERR_ARGUMENT; }
+    a.cut_count = (int32_t *) ws.ptr;
+    a.cut_rec = (int2 *) ((char *) ws.ptr + 256);
+    a.cut_capacity = (int) ((ws.bytes - 256) / 8 < INT32_MAX ? (ws.bytes - 256) / 8 : INT32_MAX);
+    cudaMemsetAsync(a.cut_count, 0, sizeof(int32_t), st);
     const bool one = lj->ntypes == 1;
     switch(e->tpa) {
         case 1: launch_force<1>(a, p->n, e->block, one, st); break;
@@ -390,6 +460,9 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
         case 4: launch_force<4>(a, p->n, e->block, one, st); break;
         default: launch_force<8>(a, p->n, e->block, one, st); break;
     }
+    if(one) { k_ens_cutoff_fixup<true><<<16, kBlock, 0, st>>>(a); }
+    else { k_ens_cutoff_fixup<false><<<16, kBlock, 0, st>>>(a); }
+    note_launch();
     return launch_status();
 }
 

@@ -76,6 +76,9 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
                 st_f4(a.p.pos_hi, hl(a.p, i), hv);
                 st_f4(a.p.pos_lo, hl(a.p, i), lv);
             }
+            if(a.p.pos_fx != nullptr) {
+                st_i4(a.p.pos_fx, i, fx_position(a.box, x.x, x.y, x.z, a.p.type != nullptr ? a.p.type[i] : 0));
+            }
         }
         st_d4(a.p.vel, i, v);
     } else if(i < a.p.n && a.from_prev) {
@@ -89,11 +92,13 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
 
 // ------------------------------------------------------------------ mixed precision
 // Mixed-precision step: FP32 forces in, FP64 velocity and position update, compensated
-// FP32 positions re-split from the new FP64 positions, FP64 displacement guard.
+// FP32 positions re-split (or fixed-point positions rounded) from the new FP64
+// positions, FP64 displacement guard.
 // GB300 issues ~2 FP64 instructions per clock per SM, so FP64 work is kept to what
 // the method needs: the kicks of a deferred final half step and the next initial
 // half step are merged into one (v += k*(dt/2)*F/m, k = 1 or 2), and the guard is
-// screened with the FP32 displacement (hi - hi_ref) + (lo - lo_ref); only particles
+// screened with the FP32 displacement (hi - hi_ref) + (lo - lo_ref), or the exact
+// fixed-point displacement converted to FP32; only particles
 // within a relative band of 1e-3 of the threshold are decided by the exact FP64
 // test |x - x_ref|^2 > (skin/2)^2, so the outcome is the FP64 test's outcome.
 
@@ -109,11 +114,9 @@ struct MixArgs {
     pg_status *status;
 };
 
+// grid point nearest x, rounded in FP64 so that |lo| <= q/2 (the packed residual's range)
 __device__ __forceinline__ void resplit(double x, float q, float iq, float &hi, float &lo) {
-    const float xf = (float) x;
-    const float h = rintf(xf * iq) * q;        // grid point near x (exact multiple of q)
-    hi = h;
-    lo = (float) (x - (double) h);
+    split_pos(x, (double) iq, (double) q, hi, lo);
 }
 
 __global__ void __launch_bounds__(kBlock) k_integrate_mixed(MixArgs a) {
@@ -135,21 +138,32 @@ __global__ void __launch_bounds__(kBlock) k_integrate_mixed(MixArgs a) {
             x.y = fma(a.dt, v.y, x.y);
             x.z = fma(a.dt, v.z, x.z);
             st_d4(a.p.pos, i, x);
-            const float q = (float) a.box.quantum, iq = 1.0f / q;
-            float4 h, l;
-            resplit(x.x, q, iq, h.x, l.x);
-            resplit(x.y, q, iq, h.y, l.y);
-            resplit(x.z, q, iq, h.z, l.z);
-            h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);   // type bits
-            l.w = 0.0f;
-            st_f4(a.p.pos_hi, hl(a.p, i), h);
-            st_f4(a.p.pos_lo, hl(a.p, i), l);
             // guard, screened in FP32 against the positions of the last list build
-            const float4 rh = ld_f4(a.p.ref_hi, i);
-            const float4 rl = ld_f4(a.p.ref_lo, i);
-            const float dx = (h.x - rh.x) + (l.x - rl.x);
-            const float dy = (h.y - rh.y) + (l.y - rl.y);
-            const float dz = (h.z - rh.z) + (l.z - rl.z);
+            const int type = a.p.type != nullptr ? a.p.type[i] : 0;
+            float dx, dy, dz;
+            if(a.p.pos_fx != nullptr) {
+                const int4 xf = fx_position(a.box, x.x, x.y, x.z, type);
+                st_i4(a.p.pos_fx, i, xf);
+                const int4 rf = ld_i4(a.p.ref_fx, i);
+                dx = (float) fx_diff(xf.x, rf.x) * a.box.fx_unit[0];
+                dy = (float) fx_diff(xf.y, rf.y) * a.box.fx_unit[1];
+                dz = (float) fx_diff(xf.z, rf.z) * a.box.fx_unit[2];
+            } else {
+                const float q = (float) a.box.quantum, iq = 1.0f / q;
+                float4 h, l;
+                resplit(x.x, q, iq, h.x, l.x);
+                resplit(x.y, q, iq, h.y, l.y);
+                resplit(x.z, q, iq, h.z, l.z);
+                h.w = __int_as_float(type);   // type bits
+                l.w = 0.0f;
+                st_f4(a.p.pos_hi, hl(a.p, i), h);
+                st_f4(a.p.pos_lo, hl(a.p, i), l);
+                const float4 rh = ld_f4(a.p.ref_hi, i);
+                const float4 rl = ld_f4(a.p.ref_lo, i);
+                dx = (h.x - rh.x) + (l.x - rl.x);
+                dy = (h.y - rh.y) + (l.y - rl.y);
+                dz = (h.z - rh.z) + (l.z - rl.z);
+            }
             const float d2 = dx * dx + dy * dy + dz * dz;
             if(d2 > a.half_skin2_hi) {
                 tripped = true;
@@ -167,10 +181,10 @@ __global__ void __launch_bounds__(kBlock) k_integrate_mixed(MixArgs a) {
 
 int integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks, int drift,
                     double half_skin2, int32_t step, pg_status *status, cudaStream_t st) {
-    if(!box || !p || !p->pos || !p->vel || !p->mass || !p->force32 || !p->pos_hi || !p->pos_lo) {
-        return PG_ERR_ARGUMENT;
-    }
-    if(drift && (!p->pos_ref || !p->ref_hi || !p->ref_lo || !status)) { return PG_ERR_ARGUMENT; }
+    if(!box || !p || !p->pos || !p->vel || !p->mass || !p->force32) { return PG_ERR_ARGUMENT; }
+    const bool fx = p->pos_fx != nullptr;
+    if(!fx && (!p->pos_hi || !p->pos_lo)) { return PG_ERR_ARGUMENT; }
+    if(drift && (!p->pos_ref || !status || (fx ? !p->ref_fx : (!p->ref_hi || !p->ref_lo)))) { return PG_ERR_ARGUMENT; }
     if(kicks < 1 || kicks > 2) { return PG_ERR_ARGUMENT; }
     MixArgs a;
     a.box = *box; a.p = *p; a.dt = dt; a.kick = kicks * (dt * 0.5); a.drift = drift;

@@ -12,15 +12,16 @@
 // Two precisions:
 //   FP64   every operation in double; the cutoff test uses the reference's exact
 //          rsq (no fused multiply-add) so the same pairs interact.
-//   MIXED  delta from compensated FP32 positions (hi on a 2^-k grid, lo residual),
-//          force arithmetic and accumulation in FP32; optional energy/virial in FP64.
+//   MIXED  delta from fixed-point positions (2^32 units per box length) or from
+//          compensated FP32 positions (hi on a 2^-k grid, lo residual), force
+//          arithmetic and accumulation in FP32; optional energy/virial in FP64.
 //
 // One thread per particle: consecutive threads read consecutive entries of the
 // column-major list (coalesced 128-byte rows), partner positions are gathered from
 // the cell-sorted arrays (mostly L1/L2 hits).  The list stream is the dominant DRAM
-// traffic: 4 bytes per entry, read with the streaming (evict-first) cache hint so it
-// does not push the partners' positions out of L2 (ncu: 285 instead of 323 MB of DRAM
-// reads per launch at 1M atoms).
+// traffic: 4 bytes per entry, read with the streaming (evict-first) cache hint.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace pg {
@@ -44,6 +45,9 @@ struct ForceArgs {
     LJTable lj;
     int sync_ref;
     double *energy;
+    int32_t *cut_count;          // pairs within the cutoff band (mixed path), and their
+    int2 *cut_rec;               // records (particle, list entry)
+    int cut_capacity;
 };
 
 __device__ __forceinline__ void block_add_energy(double pe, double vir, double *energy) {
@@ -134,7 +138,58 @@ __device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float 
                  :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(0.0f) : "memory");
 }
 
-template<bool kHalf, bool kOneType, bool kEnergy>
+// kFixed: positions from pos_fx (fixed point, 2^32 units per box length).  The wrapped
+// 32-bit difference of two coordinates is the pair's minimum-image separation, which
+// is the listed image's as long as the pair stays closer than half a box length (the
+// list is rebuilt long before: the box spans at least 4 cells of r_list), so no image
+// shift is applied and one 16-byte load per partner carries position and type.
+//
+// The list is walked in batches of kBatch entries.  The reaction of a pair is a `red`
+// with a memory clobber, which no load may pass, so a plain loop would issue the next
+// list load only after the previous pair is done and wait a full DRAM round trip per
+// entry.  Here the next batch's entries are loaded before the current batch's pairs
+// are computed, and a batch's partner gathers are issued together.
+#ifndef PG_LJ_BATCH
+#define PG_LJ_BATCH 4
+#endif
+constexpr int kBatch = PG_LJ_BATCH;
+
+// Pair separation on the mixed path: fixed point (wrapped difference, no image shift)
+// or compensated hi/lo with the listed image's exact shift.
+template<bool kFixed>
+__device__ __forceinline__ void mixed_delta(const ForceArgs &a, int4 fi, float4 hi, float4 lo, int4 fj, float4 hj,
+                                            float4 lj, uint32_t code, float &dx, float &dy, float &dz) {
+    if(kFixed) {
+        dx = (float) fx_diff(fi.x, fj.x) * a.box.fx_unit[0];
+        dy = (float) fx_diff(fi.y, fj.y) * a.box.fx_unit[1];
+        dz = (float) fx_diff(fi.z, fj.z) * a.box.fx_unit[2];
+    } else {
+        float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
+        float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
+        if(code != 0u) {
+            const int sx = image_shift(code, 0), sy = image_shift(code, 1), sz = image_shift(code, 2);
+            dhx -= sx * a.box.len_hi[0]; dlx -= sx * a.box.len_lo[0];
+            dhy -= sy * a.box.len_hi[1]; dly -= sy * a.box.len_lo[1];
+            dhz -= sz * a.box.len_hi[2]; dlz -= sz * a.box.len_lo[2];
+        }
+        dx = dhx + dlx; dy = dhy + dly; dz = dhz + dlz;
+    }
+}
+
+// Queue a near-cutoff pair for k_lj_cutoff_fixup.  The expected load is a few pairs
+// per thousand particles against a capacity of several per particle.
+__device__ __forceinline__ void cut_push(const ForceArgs &a, int i, uint32_t e) {
+    cut_queue_push(a.cut_count, a.cut_rec, a.cut_capacity, i, e);
+}
+
+// FP32 LJ pair force factor f (F_i = delta * f) and sr6
+__device__ __forceinline__ float mixed_lj(const ForceArgs &a, int tij, float rsq, float &sr6) {
+    const float sr2 = rcp_approx(rsq);
+    sr6 = sr2 * sr2 * sr2 * a.lj.sig6f[tij];
+    return 48.0f * sr6 * (sr6 - 0.5f) * sr2 * a.lj.epsf[tij];
+}
+
+template<bool kHalf, bool kOneType, bool kEnergy, bool kFixed>
 __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
     if(frozen_force(a.p)) { return; }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -143,32 +198,33 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
         const bool fixed = a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed);
         float fx = 0.0f, fy = 0.0f, fz = 0.0f;
         if(!fixed) {
-            const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
-            const int ti = kOneType ? 0 : __float_as_int(hi.w) * a.lj.ntypes;
+            float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+            int4 fi = make_int4(0, 0, 0, 0);
+            if(kFixed) {
+                fi = ld_i4(a.p.pos_fx, i);
+            } else {
+                hi = ld_f4(a.p.pos_hi, hl(a.p, i));
+                lo = ld_f4(a.p.pos_lo, hl(a.p, i));
+            }
+            const int ti = kOneType ? 0 : (kFixed ? fi.w : __float_as_int(hi.w)) * a.lj.ntypes;
             const int cnt = a.list.count[i];
             const int32_t *nb = a.list.nbr + i;
-            const int stride = a.list.stride;
-            const float c2 = a.lj.cutoff2f;
-            for(int k = 0; k < cnt; k++) {
-                const uint32_t e = (uint32_t) __ldcs(nb + (size_t) k * stride);
+            const size_t stride = (size_t) a.list.stride;
+            const float c2 = a.lj.cutoff2f, band = c2 * kCutBand;
+            // one list entry.  A pair inside the band around the cutoff is left out here
+            // and queued after its batch (returns true); k_lj_cutoff_fixup decides it in
+            // FP64.
+            auto pair = [&](uint32_t e, float4 hj, float4 lj, int4 fj) -> bool {
                 const int j = (int) (e & PG_NBR_INDEX_MASK);
                 const uint32_t code = e >> PG_NBR_INDEX_BITS;
-                const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
-                float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
-                float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
-                if(code != 0u) {
-                    const int sx = image_shift(code, 0), sy = image_shift(code, 1), sz = image_shift(code, 2);
-                    dhx -= sx * a.box.len_hi[0]; dlx -= sx * a.box.len_lo[0];
-                    dhy -= sy * a.box.len_hi[1]; dly -= sy * a.box.len_lo[1];
-                    dhz -= sz * a.box.len_hi[2]; dlz -= sz * a.box.len_lo[2];
-                }
-                const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
+                float dx, dy, dz;
+                mixed_delta<kFixed>(a, fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
                 const float rsq = dx * dx + dy * dy + dz * dz;
-                if(rsq < c2) {
-                    const int tij = kOneType ? 0 : ti + __float_as_int(hj.w);
-                    const float sr2 = __frcp_rn(rsq);
-                    const float sr6 = sr2 * sr2 * sr2 * a.lj.sig6f[tij];
-                    const float f = 48.0f * sr6 * (sr6 - 0.5f) * sr2 * a.lj.epsf[tij];
+                const bool near = fabsf(rsq - c2) < band;
+                if(rsq < c2 && !near) {
+                    const int tij = kOneType ? 0 : ti + (kFixed ? fj.w : __float_as_int(hj.w));
+                    float sr6;
+                    const float f = mixed_lj(a, tij, rsq, sr6);
                     fx += dx * f; fy += dy * f; fz += dz * f;
                     if(kHalf && code == 0u) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
                     if(kEnergy) {
@@ -177,6 +233,46 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
                         vir += w * (double) (rsq * f);
                     }
                 }
+                return near;
+            };
+            const uint64_t pol_list = l2_policy_stream(), pol_pos = l2_policy_keep();
+            uint32_t cur[kBatch];
+#pragma unroll
+            for(int u = 0; u < kBatch; u++) { cur[u] = u < cnt ? (uint32_t) ld_stream(nb + u * stride, pol_list) : 0u; }
+            for(int k0 = 0; k0 < cnt; k0 += kBatch) {
+                float4 hj[kBatch], lj[kBatch];
+                int4 fj[kBatch];
+#pragma unroll
+                for(int u = 0; u < kBatch; u++) {
+                    const int j = (int) (cur[u] & PG_NBR_INDEX_MASK);      // 0 past the end: a valid row
+                    if(kFixed) {
+                        fj[u] = ld_keep_i4(a.p.pos_fx, j, pol_pos);
+                        hj[u] = lj[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    } else {
+                        hj[u] = ld_f4(a.p.pos_hi, hl(a.p, j));
+                        lj[u] = ld_f4(a.p.pos_lo, hl(a.p, j));
+                        fj[u] = make_int4(0, 0, 0, 0);
+                    }
+                }
+                uint32_t nxt[kBatch];
+                const int32_t *nbn = nb + (size_t) (k0 + kBatch) * stride;
+#pragma unroll
+                for(int u = 0; u < kBatch; u++) {
+                    nxt[u] = k0 + kBatch + u < cnt ? (uint32_t) ld_stream(nbn + u * stride, pol_list) : 0u;
+                }
+                uint32_t pending = 0u;
+#pragma unroll
+                for(int u = 0; u < kBatch; u++) {
+                    if(k0 + u < cnt && pair(cur[u], hj[u], lj[u], fj[u])) { pending |= 1u << u; }
+                }
+                if(pending != 0u) {
+#pragma unroll
+                    for(int u = 0; u < kBatch; u++) {
+                        if(pending & (1u << u)) { cut_push(a, i, cur[u]); }
+                    }
+                }
+#pragma unroll
+                for(int u = 0; u < kBatch; u++) { cur[u] = nxt[u]; }
             }
         }
         if(kHalf) {
@@ -186,6 +282,45 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
         }
     }
     if(kEnergy) { block_add_energy(pe, vir, a.energy); }
+}
+
+// The queued pairs (FP32 rsq within kCutBand of the cutoff): the FP64 path's own
+// test decides each one; a pair inside gets its FP32 force (and, through a half
+// list's interior entry, the reaction), exactly as the main pass would have applied.
+template<bool kHalf, bool kOneType, bool kEnergy, bool kFixed>
+__global__ void __launch_bounds__(kBlock) k_lj_cutoff_fixup(ForceArgs a) {
+    if(frozen_force(a.p)) { return; }
+    const int total = min(*a.cut_count, a.cut_capacity);
+    for(int r = blockIdx.x * blockDim.x + threadIdx.x; r < total; r += gridDim.x * blockDim.x) {
+        const int2 q = a.cut_rec[r];
+        const int i = q.x;
+        const uint32_t e = (uint32_t) q.y;
+        const int j = (int) (e & PG_NBR_INDEX_MASK);
+        const uint32_t code = e >> PG_NBR_INDEX_BITS;
+        if(!exact_inside(a.p.pos, i, j, code, a.box.len, a.lj.cutoff2)) { continue; }
+        float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi, hj = hi, lj = hi;
+        int4 fi = make_int4(0, 0, 0, 0), fj = fi;
+        if(kFixed) {
+            fi = ld_i4(a.p.pos_fx, i); fj = ld_i4(a.p.pos_fx, j);
+        } else {
+            hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i));
+            hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+        }
+        float dx, dy, dz;
+        mixed_delta<kFixed>(a, fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
+        const float rsq = dx * dx + dy * dy + dz * dz;
+        const int ti = kFixed ? fi.w : __float_as_int(hi.w), tj = kFixed ? fj.w : __float_as_int(hj.w);
+        const int tij = kOneType ? 0 : ti * a.lj.ntypes + tj;
+        float sr6;
+        const float f = mixed_lj(a, tij, rsq, sr6);
+        red_add_v4(a.p.force32 + 4 * (size_t) i, dx * f, dy * f, dz * f);
+        if(kHalf && code == 0u) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
+        if(kEnergy) {
+            const double w = (kHalf && code == 0u) ? 1.0 : 0.5;
+            atomicAdd(&a.energy[0], w * 4.0 * (double) a.lj.epsf[tij] * ((double) sr6 * (double) sr6 - (double) sr6));
+            atomicAdd(&a.energy[1], w * (double) (rsq * f));
+        }
+    }
 }
 
 using KernelFn = void (*)(ForceArgs);
@@ -208,31 +343,54 @@ static KernelFn pick_fp64(bool half, bool one, bool en) {
     return en ? k_lj_fp64<false, false, true> : k_lj_fp64<false, false, false>;
 }
 
-static KernelFn pick_mixed(bool half, bool one, bool en) {
-    if(half) {
-        if(one) { return en ? k_lj_mixed<true, true, true> : k_lj_mixed<true, true, false>; }
-        return en ? k_lj_mixed<true, false, true> : k_lj_mixed<true, false, false>;
-    }
-    if(one) { return en ? k_lj_mixed<false, true, true> : k_lj_mixed<false, true, false>; }
-    return en ? k_lj_mixed<false, false, true> : k_lj_mixed<false, false, false>;
+struct MixedKernels { KernelFn main, fixup; };
+
+template<bool kHalf, bool kOneType, bool kEnergy, bool kFixed>
+static MixedKernels mixed_kernels() {
+    return {k_lj_mixed<kHalf, kOneType, kEnergy, kFixed>, k_lj_cutoff_fixup<kHalf, kOneType, kEnergy, kFixed>};
 }
+
+template<bool kFixed>
+static MixedKernels pick_mixed_layout(bool half, bool one, bool en) {
+    if(half) {
+        if(one) { return en ? mixed_kernels<true, true, true, kFixed>() : mixed_kernels<true, true, false, kFixed>(); }
+        return en ? mixed_kernels<true, false, true, kFixed>() : mixed_kernels<true, false, false, kFixed>();
+    }
+    if(one) { return en ? mixed_kernels<false, true, true, kFixed>() : mixed_kernels<false, true, false, kFixed>(); }
+    return en ? mixed_kernels<false, false, true, kFixed>() : mixed_kernels<false, false, false, kFixed>();
+}
+
+static MixedKernels pick_mixed(bool half, bool one, bool en, bool fixed) {
+    return fixed ? pick_mixed_layout<true>(half, one, en) : pick_mixed_layout<false>(half, one, en);
+}
+
+// The mixed path's queue of near-cutoff pairs lives in the caller's workspace: a
+// counter, then int2 records (the binning scratch of the same workspace is free
+// between rebuilds).  The expected load is a few pairs per thousand particles.
+constexpr int64_t kCutQueueMin = 256 + 8 * 1024;
+constexpr int kFixupBlocks = 16;
 
 int tile_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list, const pg_cells *cells,
                   const LJTableF &lj, double *energy, cudaStream_t st);
 
 int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, const pg_neighbor_list *list,
-             const pg_lj_params *lj, int precision, int sync_mode, double *energy, cudaStream_t st) {
+             const pg_lj_params *lj, int precision, int sync_mode, double *energy, pg_workspace ws, cudaStream_t st) {
     if(!box || !p || !list || !lj) { return PG_ERR_ARGUMENT; }
     if(lj->ntypes < 1 || lj->ntypes > kMaxTypes) { return PG_ERR_ARGUMENT; }
     if(precision != PG_FP64 && precision != PG_MIXED) { return PG_ERR_ARGUMENT; }
     if(precision == PG_FP64 && (!p->pos || !p->force)) { return PG_ERR_ARGUMENT; }
-    if(precision == PG_MIXED && (!p->pos_hi || !p->pos_lo || !p->force32)) { return PG_ERR_ARGUMENT; }
+    const bool fixed_point = precision == PG_MIXED && p->pos_fx != nullptr;
+    if(precision == PG_MIXED && (!p->force32 || (!fixed_point && (!p->pos_hi || !p->pos_lo)))) { return PG_ERR_ARGUMENT; }
+    if(fixed_point && !(box->fx_unit[0] > 0.0f && box->fx_unit[1] > 0.0f && box->fx_unit[2] > 0.0f)) {
+        return PG_ERR_ARGUMENT;
+    }
     if(lj->ntypes > 1 && !p->type) { return PG_ERR_ARGUMENT; }
     if(sync_mode == PG_SYNC_REFERENCE && (precision != PG_FP64 || !p->pos_prev1 || !p->pos_prev2)) {
         return PG_ERR_ARGUMENT;
     }
     ForceArgs a;
     a.box = *box; a.p = *p; a.list = *list;
+    a.cut_count = nullptr; a.cut_rec = nullptr; a.cut_capacity = 0;
     a.sync_ref = sync_mode == PG_SYNC_REFERENCE;
     a.energy = energy;
     a.lj.ntypes = lj->ntypes;
@@ -244,7 +402,7 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, co
     }
     const bool half = list->half != 0, one = lj->ntypes == 1, en = energy != nullptr;
     const bool tile = precision == PG_MIXED && list->nbr16 != nullptr;
-    if(tile && !cells) { return PG_ERR_ARGUMENT; }
+    if(tile && (!cells || !p->pos_hi || !p->pos_lo)) { return PG_ERR_ARGUMENT; }
     if(!tile && !list->nbr) { return PG_ERR_ARGUMENT; }
     if(en) { cudaMemsetAsync(energy, 0, 2 * sizeof(double), st); }
     if(half && p->n > 0) {
@@ -255,11 +413,22 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, co
         LJTableF tf;
         tf.ntypes = lj->ntypes;
         tf.cutoff2 = (float) lj->cutoff2;
+        tf.cutoff2d = lj->cutoff2;
         for(int k = 0; k < lj->ntypes * lj->ntypes; k++) { tf.eps[k] = (float) lj->epsilon[k]; tf.sig6[k] = (float) lj->sigma6[k]; }
         return tile_lj_force(box, p, list, cells, tf, energy, st);
     }
-    KernelFn k = precision == PG_FP64 ? pick_fp64(half, one, en) : pick_mixed(half, one, en);
-    k<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch();
+    if(precision == PG_FP64) {
+        pick_fp64(half, one, en)<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch();
+        return launch_status();
+    }
+    if(ws.ptr == nullptr || ws.bytes < kCutQueueMin) { return PG_ERR_ARGUMENT; }
+    a.cut_count = (int32_t *) ws.ptr;
+    a.cut_rec = (int2 *) ((char *) ws.ptr + 256);
+    a.cut_capacity = (int) std::min<int64_t>((ws.bytes - 256) / 8, INT32_MAX);
+    cudaMemsetAsync(a.cut_count, 0, sizeof(int32_t), st);
+    const MixedKernels k = pick_mixed(half, one, en, fixed_point);
+    k.main<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch();
+    k.fixup<<<kFixupBlocks, kBlock, 0, st>>>(a); note_launch();
     return launch_status();
 }
 

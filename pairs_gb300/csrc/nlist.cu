@@ -42,20 +42,34 @@ __device__ __forceinline__ float comp_delta(float hi_i, float lo_i, float hi_j, 
     return __fadd_rn(dh, dl);
 }
 
+// kFixed: the FP32 screen takes the wrapped difference of fixed-point positions.  It
+// is the separation from the stencil's image of the partner whenever that separation
+// is below half a box length, which holds for every candidate when each axis is
+// periodic and has at least 4 cells (6 with reach 2): particle and image then lie in
+// cells at most 2 (3) cells apart.
+template<bool kFixed>
 __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= a.p.n) { return; }
     const D4 xi = ld_d4(a.p.pos, i);
     st_d4(a.p.pos_ref, i, xi);
-    if(a.p.ref_hi != nullptr) {
-        st_f4(a.p.ref_hi, i, ld_f4(a.p.pos_hi, hl(a.p, i)));
-        st_f4(a.p.ref_lo, i, ld_f4(a.p.pos_lo, hl(a.p, i)));
+    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+    int4 fi = make_int4(0, 0, 0, 0);
+    if(kFixed) {
+        fi = ld_i4(a.p.pos_fx, i);
+        st_i4(a.p.ref_fx, i, fi);
+    } else {
+        hi = ld_f4(a.p.pos_hi, hl(a.p, i));
+        lo = ld_f4(a.p.pos_lo, hl(a.p, i));
+        if(a.p.ref_hi != nullptr) {
+            st_f4(a.p.ref_hi, i, hi);
+            st_f4(a.p.ref_lo, i, lo);
+        }
     }
     int cnt = 0;
     const bool fixed = a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed);
     const int ci = a.cells.particle_cell[i];
     if(!fixed && ci < a.cells.ncells) {
-        const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
         const int dz_ = a.cells.dims[2], dy_ = a.cells.dims[1], dx_ = a.cells.dims[0];
         const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
         const int stride = a.list.stride, cap = a.list.max_neighbors;
@@ -79,18 +93,33 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
                     if(nz < 0) { if(!a.box.periodic[2]) { continue; } nz += dz_; sz = -1; }
                     else if(nz >= dz_) { if(!a.box.periodic[2]) { continue; } nz -= dz_; sz = 1; }
                     const int c = (nx * dy_ + ny) * dz_ + nz;
-                    const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
                     const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
+                    // half list: an interior pair once, a pair through a periodic image
+                    // from both sides, as the reference's ghosts always pass its i < j
+                    // test (sim/interaction.py:107-113).  Which side stores an interior
+                    // pair is free: the particle of the higher cell stores none (in
+                    // sorted order a lower cell holds only j < i, so it is skipped
+                    // whole), and within a cell the index parity splits the pairs
+                    // evenly, (j > i) xor odd(i + j), so that counts do not depend on a
+                    // particle's place in its cell.
+                    if(a.list.half && code == 0u && c < ci) { continue; }
+                    const bool own = a.list.half && code == 0u && c == ci;
+                    const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
                     for(int j = b; j < e; j++) {
                         if(j == i) { continue; }
-                        // half list: an interior pair once (i < j); a pair through a
-                        // periodic image from both sides, as the reference's ghosts
-                        // always pass its i < j test (sim/interaction.py:107-113)
-                        if(a.list.half && code == 0u && j < i) { continue; }
-                        const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
-                        const float fx = comp_delta(hi.x, lo.x, hj.x, lj.x, sx, a.box.len_hi[0], a.box.len_lo[0]);
-                        const float fy = comp_delta(hi.y, lo.y, hj.y, lj.y, sy, a.box.len_hi[1], a.box.len_lo[1]);
-                        const float fz = comp_delta(hi.z, lo.z, hj.z, lj.z, sz, a.box.len_hi[2], a.box.len_lo[2]);
+                        if(own && ((j > i) == (((i ^ j) & 1) != 0))) { continue; }
+                        float fx, fy, fz;
+                        if(kFixed) {
+                            const int4 fj = ld_i4(a.p.pos_fx, j);
+                            fx = (float) fx_diff(fi.x, fj.x) * a.box.fx_unit[0];
+                            fy = (float) fx_diff(fi.y, fj.y) * a.box.fx_unit[1];
+                            fz = (float) fx_diff(fi.z, fj.z) * a.box.fx_unit[2];
+                        } else {
+                            const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+                            fx = comp_delta(hi.x, lo.x, hj.x, lj.x, sx, a.box.len_hi[0], a.box.len_lo[0]);
+                            fy = comp_delta(hi.y, lo.y, hj.y, lj.y, sy, a.box.len_hi[1], a.box.len_lo[1]);
+                            fz = comp_delta(hi.z, lo.z, hj.z, lj.z, sz, a.box.len_hi[2], a.box.len_lo[2]);
+                        }
                         const float r2f = fx * fx + fy * fy + fz * fz;
                         bool keep;
                         if(r2f < a.r2_lo) { keep = true; }
@@ -119,6 +148,16 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
     }
 }
 
+// the fixed-point screen is exact for every candidate (see k_build_list)
+static bool fixed_point_screen(const pg_box *box, const pg_particles *p, const pg_cells *cells) {
+    if(p->pos_fx == nullptr || p->ref_fx == nullptr) { return false; }
+    const int rr = cells->reach > 1 ? cells->reach : 1;
+    for(int d = 0; d < 3; d++) {
+        if(!box->periodic[d] || cells->dims[d] < (rr == 1 ? 4 : 6)) { return false; }
+    }
+    return true;
+}
+
 int tile_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                double r_list2, pg_status *status, cudaStream_t st);
 
@@ -126,7 +165,10 @@ int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cell
                          pg_neighbor_list *list, double r_list2, pg_status *status, cudaStream_t st) {
     if(!box || !p || !cells || !list || !status) { return PG_ERR_ARGUMENT; }
     if(list->nbr16 != nullptr) { return tile_build(box, p, cells, list, r_list2, status, st); }
-    if(!p->pos || !p->pos_hi || !p->pos_lo || !p->pos_ref || !list->nbr || !list->count) { return PG_ERR_ARGUMENT; }
+    const bool fx = fixed_point_screen(box, p, cells);
+    if(!p->pos || (!fx && (!p->pos_hi || !p->pos_lo)) || !p->pos_ref || !list->nbr || !list->count) {
+        return PG_ERR_ARGUMENT;
+    }
     if(list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS)) { return PG_ERR_ARGUMENT; }
     const int rr = cells->reach > 1 ? cells->reach : 1;
     if(rr > 2) { return PG_ERR_ARGUMENT; }
@@ -143,7 +185,11 @@ int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cell
     a.r2_lo = (float) r_list2 * (1.0f - kBand);
     a.r2_hi = (float) r_list2 * (1.0f + kBand);
     list->steps_since_build = 0;
-    if(p->n > 0) { k_build_list<<<blocks_for(p->n), kBlock, 0, st>>>(a, status); note_launch(); }
+    if(p->n > 0) {
+        if(fx) { k_build_list<true><<<blocks_for(p->n), kBlock, 0, st>>>(a, status); }
+        else { k_build_list<false><<<blocks_for(p->n), kBlock, 0, st>>>(a, status); }
+        note_launch();
+    }
     return launch_status();
 }
 

@@ -293,9 +293,18 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_lj(TileArgs a) {
                 const float dy = (hi.y - hj.y) + (lo.y - lj.y);
                 const float dz = (hi.z - hj.z) + (lo.z - lj.z);
                 const float rsq = dx * dx + dy * dy + dz * dz;
-                if(rsq < c2) {
+                bool inside = rsq < c2;
+                if(fabsf(rsq - c2) < c2 * kCutBand) {
+                    // the slot's segment gives the global partner and its image
+                    int s = 0;
+                    while(s + 1 < r.nsegs && r.segs[s + 1].base <= js) { s++; }
+                    const Seg g = r.segs[s];
+                    inside = exact_inside(a.p.pos, i, g.start + (js - g.base), (uint32_t) g.code, a.box.len,
+                                          a.lj.cutoff2d);
+                }
+                if(inside) {
                     const int tij = kOneType ? 0 : ti + __float_as_int(hj.w);
-                    const float sr2 = __frcp_rn(rsq);
+                    const float sr2 = rcp_approx(rsq);
                     const float sr6 = sr2 * sr2 * sr2 * a.lj.sig6[tij];
                     const float f = 48.0f * sr6 * (sr6 - 0.5f) * sr2 * a.lj.eps[tij];
                     fx += dx * f; fy += dy * f; fz += dz * f;

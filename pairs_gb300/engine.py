@@ -37,13 +37,22 @@ def _box_quantum(lo, hi):
     return 2.0 ** (math.ceil(math.log2(span)) - 22)
 
 
+def set_fixed_point_units(box):
+    """Fixed-point position units of a box (pg_box.fx_scale / fx_unit): 2^32 units
+    per box length on every axis."""
+    for d in range(3):
+        box.fx_scale[d] = 2.0 ** 32 / box.len[d]
+        box.fx_unit[d] = float(np.float32(box.len[d] / 2.0 ** 32))
+
+
 class LJEngine:
     """One periodic (or walled) box of point masses with Lennard-Jones forces."""
 
     def __init__(self, state, *, lo=None, hi=None, periodic=(True, True, True), cutoff=2.5, skin=0.3,
                  dt=0.005, ntypes=1, epsilon=None, sigma6=None, precision="fp64", half=False,
                  sync="exact", every=20, neighbor_capacity=100, policy="fixed", device="cuda",
-                 capacity=None, fused=True, tiles=None, tile_tpa=2, tile_atoms=224, cell_reach=1):
+                 capacity=None, fused=True, tiles=None, tile_tpa=2, tile_atoms=224, cell_reach=1,
+                 fixed_point=None):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -92,6 +101,7 @@ class LJEngine:
             self.box.len_hi[d] = lh
             self.box.len_lo[d] = self.box.len[d] - lh
         self.box.quantum = q
+        set_fixed_point_units(self.box)
 
         # ---- particles
         f64, f32, i32 = torch.float64, torch.float32, torch.int32
@@ -102,12 +112,6 @@ class LJEngine:
         t["pos"] = z((cap, 4), f64)
         t["vel"] = z((cap, 4), f64)
         t["pos_ref"] = z((cap, 4), f64)
-        # hi and lo as two float4 arrays (an interleaved 32-byte record per particle,
-        # hilo_stride 2, measured slower for the partner gathers: 257 vs 233 us)
-        t["pos_hi"] = z((cap, 4), f32)
-        t["pos_lo"] = z((cap, 4), f32)
-        t["ref_hi"] = z((cap, 4), f32)
-        t["ref_lo"] = z((cap, 4), f32)
         t["mass"] = z((cap,), f64)
         t["type"] = z((cap,), i32)
         t["uid"] = z((cap,), i32)
@@ -154,6 +158,28 @@ class LJEngine:
             self.cells.cell_len[d] = L / dims
             ncells *= dims
         self.cells.ncells = ncells
+
+        # ---- FP32 position layout (the mixed path's forces, the list build's screen).
+        # Fixed point (one int4 per particle, periodic images without shifts) where
+        # the box allows it: every axis periodic with at least 4 cells (6 with reach
+        # 2); compensated hi/lo float4 pairs otherwise, and for tile lists.
+        fx_ok = (not tiles and all(periodic) and
+                 all(self.cells.dims[d] >= (4 if reach == 1 else 6) for d in range(3)))
+        if fixed_point and not fx_ok:
+            raise ValueError("fixed-point positions need global lists and a periodic box "
+                             "of at least 4 cells per axis (6 with cell_reach 2)")
+        self.fixed_point = fx_ok if fixed_point is None else bool(fixed_point)
+        if self.fixed_point:
+            t["pos_fx"] = z((cap, 4), i32)
+            t["ref_fx"] = z((cap, 4), i32)
+        else:
+            # hi and lo as two float4 arrays (an interleaved 32-byte record per particle,
+            # hilo_stride 2, measured slower for the partner gathers: 257 vs 233 us)
+            t["pos_hi"] = z((cap, 4), f32)
+            t["pos_lo"] = z((cap, 4), f32)
+            t["ref_hi"] = z((cap, 4), f32)
+            t["ref_lo"] = z((cap, 4), f32)
+        self._bind_particles()
         t["cell_start"] = z((ncells + 2,), i32)
         t["cell_count"] = z((ncells + 1,), i32)
         t["particle_cell"] = z((cap,), i32)
@@ -221,7 +247,7 @@ class LJEngine:
     def _bind_particles(self):
         t, p = self.t, self.p
         for name in ("pos", "pos_prev1", "pos_prev2", "vel", "force", "force32", "pos_hi", "pos_lo",
-                     "pos_ref", "ref_hi", "ref_lo", "mass", "type", "uid", "flags"):
+                     "pos_ref", "ref_hi", "ref_lo", "pos_fx", "ref_fx", "mass", "type", "uid", "flags"):
             setattr(p, name, t[name].data_ptr() if name in t else None)
 
     # shared memory per tile block: 32 B per staged particle, below the 227 KB a

