@@ -405,6 +405,11 @@ int pg_mlp_param_count(void);
 int pg_cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t steps_since_build,
                      double dt, double half_skin, float *features, void *stream);
 
+/* The cells of one sample (no counterpart in the reference): the ncells feature rows
+ * are split into k contiguous groups and each group's row with the largest feature 0
+ * (fastest particle) is copied to out[k][4].  ncells >= k. */
+int pg_cell_select(const float *features, int32_t ncells, int32_t k, float *out, void *stream);
+
 /* out[c] = network output (log steps until the cell's first displacement > skin/2)
  * for non-empty cells, +inf for empty ones. */
 int pg_mlp_forward(const float *params, const float *features, int32_t ncells, float *out, void *stream);

@@ -26,6 +26,7 @@ int cell_features(const pg_particles *p, const pg_cells *cells, int precision, i
                   double half_skin, float *feat, cudaStream_t st);
 int mlp_forward(const float *params, const float *feat, int32_t ncells, float *out, cudaStream_t st);
 int mlp_softmin(const float *out, int32_t ncells, float temperature, float *result, cudaStream_t st);
+int cell_select(const float *features, int32_t ncells, int32_t k, float *out, cudaStream_t st);
 int mlp_backward(const float *params, const float *feat, const float *out, int32_t ncells, const float *result,
                  float target_log, int censored, float temperature, float *grads, float *loss, cudaStream_t st);
 int mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float b1, float b2, float eps,
@@ -186,6 +187,10 @@ int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin
 int pg_cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t steps_since_build,
                      double dt, double half_skin, float *features, void *stream) {
     return pg::cell_features(p, cells, precision, steps_since_build, dt, half_skin, features, S(stream));
+}
+
+int pg_cell_select(const float *features, int32_t ncells, int32_t k, float *out, void *stream) {
+    return pg::cell_select(features, ncells, k, out, S(stream));
 }
 
 int pg_mlp_forward(const float *params, const float *features, int32_t ncells, float *out, void *stream) {

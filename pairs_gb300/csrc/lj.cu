@@ -325,10 +325,12 @@ __global__ void __launch_bounds__(kBlock) k_lj_cutoff_fixup(ForceArgs a) {
 
 using KernelFn = void (*)(ForceArgs);
 
-// zero the force array before a half-list pass (skipped like the pass when frozen)
-__global__ void k_zero_force(pg_particles p, int fp64) {
+// zero the force array before a half-list pass, and the mixed path's near-cutoff queue
+// (skipped like the pass when frozen)
+__global__ void k_zero_force(pg_particles p, int fp64, int32_t *cut_count) {
     if(frozen_force(p)) { return; }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i == 0 && cut_count != nullptr) { *cut_count = 0; }
     if(i >= p.n) { return; }
     if(fp64) { st_d4(p.force, i, make_d4(0.0, 0.0, 0.0, 0.0)); }
     else { st_f4(p.force32, i, make_float4(0.0f, 0.0f, 0.0f, 0.0f)); }
@@ -405,8 +407,17 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, co
     if(tile && (!cells || !p->pos_hi || !p->pos_lo)) { return PG_ERR_ARGUMENT; }
     if(!tile && !list->nbr) { return PG_ERR_ARGUMENT; }
     if(en) { cudaMemsetAsync(energy, 0, 2 * sizeof(double), st); }
+    const bool queue = precision == PG_MIXED && !tile;
+    if(queue) {
+        if(ws.ptr == nullptr || ws.bytes < kCutQueueMin) { return PG_ERR_ARGUMENT; }
+        a.cut_count = (int32_t *) ws.ptr;
+        a.cut_rec = (int2 *) ((char *) ws.ptr + 256);
+        a.cut_capacity = (int) std::min<int64_t>((ws.bytes - 256) / 8, INT32_MAX);
+    }
     if(half && p->n > 0) {
-        k_zero_force<<<blocks_for(p->n), kBlock, 0, st>>>(*p, precision == PG_FP64); note_launch();
+        k_zero_force<<<blocks_for(p->n), kBlock, 0, st>>>(*p, precision == PG_FP64, a.cut_count); note_launch();
+    } else if(queue) {
+        cudaMemsetAsync(a.cut_count, 0, sizeof(int32_t), st);
     }
     if(p->n == 0) { return launch_status(); }
     if(tile) {
@@ -421,11 +432,6 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, co
         pick_fp64(half, one, en)<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch();
         return launch_status();
     }
-    if(ws.ptr == nullptr || ws.bytes < kCutQueueMin) { return PG_ERR_ARGUMENT; }
-    a.cut_count = (int32_t *) ws.ptr;
-    a.cut_rec = (int2 *) ((char *) ws.ptr + 256);
-    a.cut_capacity = (int) std::min<int64_t>((ws.bytes - 256) / 8, INT32_MAX);
-    cudaMemsetAsync(a.cut_count, 0, sizeof(int32_t), st);
     const MixedKernels k = pick_mixed(half, one, en, fixed_point);
     k.main<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch();
     k.fixup<<<kFixupBlocks, kBlock, 0, st>>>(a); note_launch();

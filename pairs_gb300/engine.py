@@ -224,6 +224,8 @@ class LJEngine:
         t["status_init"] = torch.tensor(np.frombuffer(bytes(init), dtype=np.int32).copy(), device=self.dev)
         t["status"] = t["status_init"].clone()
         self.status_ptr = C.c_void_p(t["status"].data_ptr())
+        self.status_host = torch.zeros_like(t["status"], device="cpu").pin_memory()
+        self.status_event = torch.cuda.Event()
         wsb = A.load().pg_workspace_bytes(cap, ncells)
         t["ws"] = torch.empty((int(wsb),), dtype=torch.uint8, device=self.dev)
         self.ws = A.PgWorkspace(t["ws"].data_ptr(), int(wsb))
@@ -288,30 +290,54 @@ class LJEngine:
         s = self.t["status"].cpu().numpy()
         return A.PgStatus.from_buffer_copy(s.tobytes())
 
+    def _snapshot_status(self):
+        """Queue a copy of the status to pinned host memory (read by _wait_status)."""
+        self.status_host.copy_(self.t["status"], non_blocking=True)
+        self.status_event.record(self.stream)
+
+    def _wait_status(self):
+        self.status_event.synchronize()
+        self.host_syncs += 1
+        return A.PgStatus.from_buffer_copy(self.status_host.numpy().tobytes())
+
     def reset_status(self):
         self.t["status"].copy_(self.t["status_init"])
 
     # ------------------------------------------------------------------ modules
 
-    def rebuild(self, pre_bin=None):
+    def rebuild(self, pre_bin=None, then=None):
         """Bin + sort + Verlet build, growing the list until it fits.  Returns the
         step at which the guard had tripped before this build (INT32_MAX if none).
         pre_bin, if given, queues work on the state before the particles are
-        re-sorted (the learned schedule's features and prediction)."""
+        re-sorted (the learned schedule's features and prediction).  then, if given,
+        queues the work that uses the new list (the force pass) before the host waits
+        for the build's status, so the host's bookkeeping overlaps it; it is queued
+        again if the build has to be repeated."""
         by = C.byref
         if pre_bin is not None:
             pre_bin()
+        st_dev = self.t["status"]
+        st_dev[0:3].zero_()                             # overflow, max_cell_count, max_neighbors
         A.call("pg_bin_particles", by(self.box), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
         guard = None
+        first = True
         while True:
-            self.t["status"][0] = 0                     # overflow bits
-            self.t["status"][2] = 0                     # max_neighbors
-            self.t["status"][6] = 0                     # max_tile_staged
+            if not first:
+                st_dev[0] = 0
+                st_dev[2] = 0
+            first = False
             if self.tiles:
+                st_dev[6] = 0                           # max_tile_staged
                 self.list.tile_capacity = self.TILE_LIMIT
             A.call("pg_build_neighbor_lists", by(self.box), by(self.p), by(self.cells), by(self.list),
                    self.r_list2, self.status_ptr, self.sh)
-            st = self.read_status()
+            self._snapshot_status()
+            st_dev[4] = INT32_MAX                       # guard reset, after the snapshot
+            early = then is not None and not self.tiles
+            if early:
+                self.list.steps_since_build = 0
+                then()
+            st = self._wait_status()
             guard = st.guard_tripped if guard is None else guard
             if st.nonfinite:
                 raise A.PairsError("non-finite particle position met while binning")
@@ -334,7 +360,8 @@ class LJEngine:
         self.list.steps_since_build = 0
         self.since_build = 0
         self.nbuilds += 1
-        self.t["status"][4] = INT32_MAX                 # guard reset
+        if then is not None and not early:
+            then()
         return guard
 
     def force(self, energy=False):
@@ -422,7 +449,7 @@ class LJEngine:
         are x(s) and the build is the one step s needed: rewind to s."""
         if ts != 0 and ts != self.next_rebuild:
             return False
-        s = self.rebuild(pre_bin=self._schedule_hook())
+        s = self.rebuild(pre_bin=self._schedule_hook(), then=self.force)
         tripped_at = None
         if ts > 0 and s <= ts:
             tripped_at = s
@@ -491,16 +518,16 @@ class LJEngine:
         ts = self.ts
         self.p.step = ts
         if built:
-            pass
+            pass                                        # the rebuild queued the force pass
         elif rebuild:
-            self.rebuild(pre_bin=self._schedule_hook() if self.speculative else None)
+            self.rebuild(pre_bin=self._schedule_hook() if self.speculative else None, then=self.force)
             self._cycle_start = ts
             if self.speculative:
                 self._after_rebuild_schedule(ts, tripped_at)
         else:
             self.since_build += 1
             self.list.steps_since_build = self.since_build
-        self.force()
+            self.force()
         if ts > 0:
             self._pending_final = True
             if not self.fused:

@@ -80,8 +80,9 @@ class LearnedSchedule:
 
     # ---------------------------------------------------------------- features / prediction
     def features_into(self, slot, since=None):
-        """Per-cell features of the current state; the sample keeps the `ncells`
-        cells with the fastest particle (the soft minimum is decided there)."""
+        """Per-cell features of the current state.  The sample keeps `ncells` cells:
+        the fastest of each of `ncells` slabs of the grid, among them the fastest cell
+        of the system (the soft minimum is decided by the fast cells)."""
         e = self.e
         since = e.since_build if since is None else since
         A.call("pg_cell_features", C.byref(e.p), C.byref(e.cells), e.precision, since, e.dt,
@@ -89,8 +90,8 @@ class LearnedSchedule:
         if self.ncells == self.ncells_all:
             self.feat[slot].copy_(self.feat_all)
         else:
-            idx = torch.topk(self.feat_all[:, 0], self.ncells, sorted=False).indices
-            torch.index_select(self.feat_all, 0, idx, out=self.feat[slot])
+            A.call("pg_cell_select", self._ptr(self.feat_all), self.ncells_all, self.ncells, self._ptr(self.feat[slot]),
+                   e.sh)
 
     def predict_log(self, slot):
         """Soft-min prediction for the features in `slot` (device scalar in result[0])."""
@@ -151,11 +152,12 @@ class LearnedSchedule:
         self.pending = []
         self.cycles += 1
         if self.trained and self.online_every and self.cycles % self.online_every == 0:
-            self.train(self.online_steps, recent=self.online_recent)
+            self.train(self.online_steps, recent=self.online_recent, log=False)
 
     # ---------------------------------------------------------------- training
-    def train(self, steps=None, recent=None):
-        """Adam steps on the stored samples (the `recent` newest ones if given)."""
+    def train(self, steps=None, recent=None, log=True):
+        """Adam steps on the stored samples (the `recent` newest ones if given).  With
+        log, the final loss is read back (a host sync) and returned."""
         e = self.e
         steps = self.train_steps if steps is None else steps
         if not self.labels:
@@ -172,9 +174,11 @@ class LearnedSchedule:
             self.adam_t += 1
             A.call("pg_mlp_adam", self._ptr(self.params), self._ptr(self.grads), self._ptr(self.m1),
                    self._ptr(self.m2), self.lr, 0.9, 0.999, 1e-8, self.adam_t, 1.0 / ns, e.sh)
+        self.trained = True
+        if not log:
+            return None
         final = float(self.loss.item()) / ns
         self.train_log.append(final)
-        self.trained = True
         return final
 
     def predicted_steps(self):
