@@ -388,6 +388,12 @@ int pg_compute_thermo(const pg_box *box, const pg_particles *p, double *out,
  * or a permutation). */
 int pg_split_positions(const pg_box *box, pg_particles *p, void *stream);
 
+/* Device address of the permutation of the last pg_bin_particles call that used ws
+ * with these sizes (new index k holds old particle perm[k]), or NULL if ws is too
+ * small.  No counterpart in the reference, whose exchange moves every property
+ * itself: callers that keep further per-particle arrays permute them with it. */
+const int32_t *pg_bin_permutation(int32_t n, int32_t ncells, pg_workspace ws);
+
 /* dst[k] = src[perm[k]] for k < n, elements of elem_bytes (4, 8, 16 or 32): applies
  * the last binning permutation to caller-held per-particle arrays. */
 int pg_permute(int32_t n, const int32_t *perm, const void *src, void *dst, int elem_bytes,

@@ -44,6 +44,14 @@ CONFIGS = {
     "lj4_t4": dict(kind="md", n=[4, 4, 4], timesteps=100, ntypes=4, reneighbor_every=20, thermo_every=100),
     "lj8": dict(kind="md", n=[8, 8, 8], timesteps=100, ntypes=1, reneighbor_every=20, thermo_every=100),
     "lj6x5x4": dict(kind="md", n=[6, 5, 4], timesteps=60, ntypes=1, reneighbor_every=10, thermo_every=20),
+    # kernels outside the LJ / velocity-Verlet templates (oracle/ref_custom.py): a
+    # force-shifted, capped LJ pair kernel and a damped velocity-Verlet half step
+    "custom6": dict(kind="custom", n=[6, 6, 6], timesteps=60, ntypes=2, reneighbor_every=10, thermo_every=20,
+                    epsilon=[1.0, 1.2, 1.2, 0.8], sigma6=[1.0, 1.1, 1.1, 0.9],
+                    symbols=dict(dt=0.005, fshift=-0.039, fcap=60.0, vmax2=5.0, damping=0.999)),
+    "custom6_half": dict(kind="custom", n=[6, 6, 6], timesteps=60, ntypes=2, reneighbor_every=10,
+                         thermo_every=20, half=True, epsilon=[1.0, 1.2, 1.2, 0.8], sigma6=[1.0, 1.1, 1.1, 0.9],
+                         symbols=dict(dt=0.005, fshift=-0.039, fcap=60.0, vmax2=5.0, damping=0.999)),
     # DEM example program (spheres on a simple-cubic grid falling on a bottom wall);
     # "dem_dense" packs the grid tighter so sphere-sphere contacts start early
     "dem_small": dict(kind="dem", timesteps=300, domain_size=[0.03, 0.03, 0.05], spacing=0.005,
@@ -67,7 +75,7 @@ def generate(name, cfg):
     full = dict(cfg)
     full["name"] = name
     env["PAIRS_ORACLE_CFG"] = json.dumps(full)
-    script = os.path.join(HERE, "ref_md.py" if cfg["kind"] == "md" else "ref_dem.py")
+    script = os.path.join(HERE, {"md": "ref_md.py", "custom": "ref_custom.py"}.get(cfg["kind"], "ref_dem.py"))
     subprocess.run([sys.executable, script, "cpu"], cwd=wd, env=env, check=True,
                    stdout=subprocess.DEVNULL)
     return wd, os.path.join(wd, name + ".cpp")

@@ -143,6 +143,7 @@ SIGNATURES = {
                                    C.c_void_p, C.c_void_p]),
     "pg_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "pg_mlp_softmin": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.c_void_p]),
+    "pg_bin_permutation": (C.c_void_p, [C.c_int32, C.c_int32, PgWorkspace]),
     "pg_cell_select": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "pg_mlp_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_int,
                                   C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),

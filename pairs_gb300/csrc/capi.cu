@@ -3,6 +3,7 @@
 
 namespace pg {
 int64_t bin_workspace_bytes(int32_t n, int32_t ncells);
+const int32_t *bin_permutation(int32_t n, int32_t ncells, pg_workspace ws);
 int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_workspace ws,
                   pg_status *status, cudaStream_t st, int32_t **perm_out);
 int gather_array(int n, const int32_t *perm, const void *src, void *dst, int elem_bytes, cudaStream_t st);
@@ -73,6 +74,10 @@ int pg_struct_sizes(int64_t *out, int n) {
     if(out == nullptr) { return m; }
     for(int k = 0; k < n && k < m; k++) { out[k] = sizes[k]; }
     return m;
+}
+
+const int32_t *pg_bin_permutation(int32_t n, int32_t ncells, pg_workspace ws) {
+    return pg::bin_permutation(n, ncells, ws);
 }
 
 int64_t pg_workspace_bytes(int32_t n, int32_t ncells) {

@@ -218,6 +218,13 @@ int64_t bin_workspace_bytes(int32_t n, int32_t ncells) {
     return (int64_t) bin_ws_layout(n, ncells, nullptr, nullptr);
 }
 
+const int32_t *bin_permutation(int32_t n, int32_t ncells, pg_workspace ws) {
+    if(ws.ptr == nullptr || n < 0 || ncells < 0 || ws.bytes < bin_workspace_bytes(n, ncells)) { return nullptr; }
+    BinWs w;
+    bin_ws_layout(n, ncells, (char *) ws.ptr, &w);
+    return w.perm;
+}
+
 // Zero the cell counters of the workspace (the count pass adds into them).
 int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cudaStream_t st) {
     if(ws.ptr == nullptr || ws.bytes < bin_workspace_bytes(n, ncells)) { return PG_ERR_ARGUMENT; }

@@ -205,7 +205,11 @@ class Simulation:
         assert self.position_prop is not None, "position property not declared"
         kinds = [s[0] for s in self.setups]
         if self._shapes == [Shapes.PointMass]:
-            self.plan = self._plan_lj()
+            try:
+                self.plan = self._plan_lj()
+            except NotImplementedError as why:
+                # not the LJ / velocity-Verlet program: generated kernels (codegen.py)
+                self.plan = dict(program="generic", reason=str(why))
         elif Shapes.Sphere in self._shapes:
             from .dem import plan_dem
             self.plan = plan_dem(self)
@@ -278,6 +282,13 @@ class Simulation:
     def build_engine(self):
         if self.plan is None:
             self.generate()
+        if self.plan["program"] == "generic":
+            from .generic import GenericEngine
+            if self.precision != "fp64":
+                raise NotImplementedError("generated kernels run in FP64: use double_prec=True")
+            setups = [dict(e, setup=True, cutoff=None) for e in self.setup_functions]
+            return GenericEngine(self, self._initial_state(), self.pre_step_functions + self.functions, setups,
+                                 device=self.device)
         if self.plan["program"] != "lj":
             from .dem import build_dem_engine
             return build_dem_engine(self)

@@ -36,6 +36,8 @@ KEEP = {
     "lj4_t4": dict(steps=[0, 1, 100], pairs=[]),
     "lj8": dict(steps=[1, 100], pairs=[]),
     "lj6x5x4": dict(steps=[0, 1, 10, 11, 60], pairs=[]),
+    "custom6": dict(steps=[0, 1, 9, 10, 11, 30, 60], pairs=[]),
+    "custom6_half": dict(steps=[0, 1, 10, 60], pairs=[]),
 }
 
 
