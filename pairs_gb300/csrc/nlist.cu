@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
         const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
         const int stride = a.list.stride, cap = a.list.max_neighbors;
         int32_t *out = a.list.nbr + i;
+        int32_t *wp = out;
         const int rr = a.cells.reach > 1 ? a.cells.reach : 1;
         // offsets past one box length are skipped: a box longer than 2 r_list holds no
         // partner there, and each (cell, image) pair is then visited once
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
                             keep = ref_rsq(ddx, ddy, ddz) < a.r_list2;
                         }
                         if(keep) {
-                            if(cnt < cap) { out[(size_t) cnt * stride] = (int32_t) (code | (uint32_t) j); }
+                            if(cnt < cap) { *wp = (int32_t) (code | (uint32_t) j); wp += stride; }
                             cnt++;
                         }
                     }
