@@ -13,7 +13,12 @@ namespace pg {
 
 // Wrap into the periodic box exactly as the reference's exchange pack does
 // (x + mult*len with mult = +1 below lo, -1 above hi), then compute the cell.
-__global__ void k_bin_count(pg_box box, pg_particles p, pg_cells cells, int32_t *count,
+// inv_len: 1 / cell_len per axis (host FP64); the cell of a coordinate is
+// floor((x - lo) * inv_len), clamped.  Between rebuilds particles stay mostly in cell
+// order, so a warp's particles fall into a few cells: one atomic per distinct cell.
+struct InvLen { double v[3]; };
+
+__global__ void k_bin_count(pg_box box, pg_particles p, pg_cells cells, InvLen inv, int32_t *count,
                             pg_status *status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= p.n) { return; }
@@ -42,14 +47,15 @@ __global__ void k_bin_count(pg_box box, pg_particles p, pg_cells cells, int32_t 
     } else {
         int idx = 0;
         for(int d = 0; d < 3; d++) {
-            int c = (int) floor((c3[d] - box.lo[d]) / cells.cell_len[d]);
+            int c = (int) floor((c3[d] - box.lo[d]) * inv.v[d]);
             c = c < 0 ? 0 : (c >= cells.dims[d] ? cells.dims[d] - 1 : c);
             idx = idx * cells.dims[d] + c;
         }
         cell = idx;
     }
     cells.particle_cell[i] = cell;
-    atomicAdd(&count[cell], 1);
+    const unsigned peers = __match_any_sync(__activemask(), cell);
+    if((threadIdx.x & 31) == (unsigned) (__ffs(peers) - 1)) { atomicAdd(&count[cell], __popc(peers)); }
 }
 
 // Exclusive scan, three passes over blocks of 1024 entries.
@@ -280,7 +286,9 @@ int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_worksp
     int rc = bin_prepare(n, cells->ncells, ws, &count, st);
     if(rc) { return rc; }
     if(n > 0) {
-        k_bin_count<<<blocks_for(n), kBlock, 0, st>>>(*box, *p, *cells, count, status); note_launch();
+        InvLen inv;
+        for(int d = 0; d < 3; d++) { inv.v[d] = 1.0 / cells->cell_len[d]; }
+        k_bin_count<<<blocks_for(n), kBlock, 0, st>>>(*box, *p, *cells, inv, count, status); note_launch();
     }
     rc = bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out);
     if(rc || n == 0) { return rc; }
