@@ -261,6 +261,30 @@ def run_ours(args, rank, world, dist):
         drift_headline = drift(ed, args.drift_steps)
         del ed
 
+    # force error of the mixed path against the FP64 path (which matches the FP64
+    # oracle to 1e-12) on one equilibrated state: RMS and maximum error over the RMS
+    # force, both engines rebuilt from the same positions
+    def force_error():
+        eq = make(prec, half, "guard")
+        eq.run(100)
+        pos, vel, _ = eq.state()
+        del eq
+        st2 = dict(st, pos=pos, vel=vel)
+        out = {}
+        for p_ in (prec, "fp64"):
+            e_ = LJEngine(st2, precision=p_, half=half, sync="exact", every=20, policy="fixed", device=str(dev))
+            e_.rebuild()
+            e_.force()
+            out[p_] = e_.state()[2]
+            del e_
+        ref = out["fp64"]
+        err = out[prec] - ref
+        rms = float(np.sqrt((ref ** 2).mean()))
+        return {"rms_rel": float(np.sqrt((err ** 2).mean())) / rms, "max_rel": float(np.abs(err).max()) / rms,
+                "state": "after 100 steps from the lattice"}
+
+    ferr = force_error() if prec == "mixed" else None
+
     # plain FP64 path on the same workload: fixed every-20 schedule and exact guard
     fp64 = {}
     k64 = max(10, args.steps // 10)
@@ -327,6 +351,7 @@ def run_ours(args, rank, world, dist):
                    "l2": "inputs larger than L2 (Verlet list %.0f MB)" % (pairs_total * 4 / 1e6)},
         "roofline": roofline, "schedule": schedule,
         "energy_drift_1000": {"headline": drift_headline, "fp64_guard": drift64, "steps": args.drift_steps},
+        "force_error_vs_fp64": ferr,
         "fp64": {"best_value": best64, **fp64, "speedup_headline_vs_fp64": value / world / best64},
         "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
     }
