@@ -52,6 +52,10 @@ CONFIGS = {
     "custom6_half": dict(kind="custom", n=[6, 6, 6], timesteps=60, ntypes=2, reneighbor_every=10,
                          thermo_every=20, half=True, epsilon=[1.0, 1.2, 1.2, 0.8], sigma6=[1.0, 1.1, 1.1, 0.9],
                          symbols=dict(dt=0.005, fshift=-0.039, fcap=60.0, vmax2=5.0, damping=0.999)),
+    "custom_wca": dict(kind="custom", program="wca", n=[5, 6, 7], timesteps=40, ntypes=1, reneighbor_every=8,
+                       thermo_every=10, rho=0.7, temp=1.2,
+                       symbols=dict(dt=0.004, wca_rc2=1.2599210498948732, ksoft=20.0, sigma_s=1.15,
+                                    vmax2=4.0, vscale=0.998)),
     # DEM example program (spheres on a simple-cubic grid falling on a bottom wall);
     # "dem_dense" packs the grid tighter so sphere-sphere contacts start early
     "dem_small": dict(kind="dem", timesteps=300, domain_size=[0.03, 0.03, 0.05], spacing=0.005,

@@ -4,8 +4,11 @@ reference code generator (test oracle input).
 Run by oracle/ref_build.py with the reference's `src/` on PYTHONPATH; it writes
 `<name>.cpp` into the working directory.  The kernels exercise the parts of the
 reference's kernel language that the generated-kernel path (pairs_gb300/codegen.py)
-lowers: locals, symbols, feature tables, sqrt, min, squared_length, if / else,
-apply() in a pair kernel, property stores of vectors and of a user real property.
+lowers: locals (scalar and vector), symbols, feature tables, sqrt, min, max, select,
+length, normalized, dot, squared_length, skip_when, if / else, apply() in a pair
+kernel, property stores of vectors and of user real, integer and vector properties.
+Program "capped" (default): capped_lj + damped_final_integrate; program "wca":
+wca_soft + clamped_final_integrate.
 The same functions are in tests/scripts/custom_script.py for the product's API.
 Test infrastructure only.
 """
@@ -40,6 +43,27 @@ def damped_final_integrate(i):
     kinetic[i] = 0.5 * mass[i] * speed2
 
 
+def wca_soft(i, j):
+    d = delta(i, j)
+    rsq = squared_distance(i, j)
+    skip_when(rsq > wca_rc2)
+    r = sqrt(rsq)
+    sr2 = 1.0 / rsq
+    sr6 = sr2 * sr2 * sr2
+    fwca = 48.0 * sr6 * (sr6 - 0.5) * sr2
+    fsoft = max(ksoft * (sigma_s - r), 0.0) / r
+    apply(force, d * (fwca + fsoft))
+
+
+def clamped_final_integrate(i):
+    linear_velocity[i] += (dt * 0.5) * force[i] / mass[i]
+    v2 = dot(linear_velocity[i], linear_velocity[i])
+    scale = select(v2 > vmax2, vscale, 1.0)
+    linear_velocity[i] = linear_velocity[i] * scale
+    steps_done[i] += 1
+    accel[i] = normalized(force[i]) * length(force[i]) / mass[i]
+
+
 cfg = json.loads(os.environ["PAIRS_ORACLE_CFG"])
 name = cfg["name"]
 ntypes = cfg.get("ntypes", 1)
@@ -54,6 +78,8 @@ psim.add_property('mass', pairs.real(), 1.0)
 psim.add_property('linear_velocity', pairs.vector())
 psim.add_property('force', pairs.vector(), volatile=True)
 psim.add_property('kinetic', pairs.real(), 0.0)
+psim.add_property('steps_done', pairs.int32(), 0)
+psim.add_property('accel', pairs.vector())
 psim.add_feature('type', ntypes)
 psim.add_feature_property('type', 'epsilon', pairs.real(), eps)
 psim.add_feature_property('type', 'sigma6', pairs.real(), sig6)
@@ -66,7 +92,13 @@ if cfg.get("half", False):
     psim.compute_half()
 psim.build_neighbor_lists(cfg.get("cutoff", 2.5) + cfg.get("skin", 0.3))
 psim.compute(initial_integrate, symbols={'dt': sym["dt"]}, pre_step=True, skip_first=True)
-psim.compute(capped_lj, cfg.get("cutoff", 2.5), symbols={'fshift': sym["fshift"], 'fcap': sym["fcap"]})
-psim.compute(damped_final_integrate, symbols={'dt': sym["dt"], 'vmax2': sym["vmax2"], 'damping': sym["damping"]},
-             skip_first=True)
+if cfg.get("program", "capped") == "capped":
+    psim.compute(capped_lj, cfg.get("cutoff", 2.5), symbols={'fshift': sym["fshift"], 'fcap': sym["fcap"]})
+    psim.compute(damped_final_integrate, symbols={'dt': sym["dt"], 'vmax2': sym["vmax2"],
+                                                  'damping': sym["damping"]}, skip_first=True)
+else:
+    psim.compute(wca_soft, cfg.get("cutoff", 2.5), symbols={'wca_rc2': sym["wca_rc2"], 'ksoft': sym["ksoft"],
+                                                             'sigma_s': sym["sigma_s"]})
+    psim.compute(clamped_final_integrate, symbols={'dt': sym["dt"], 'vmax2': sym["vmax2"],
+                                                   'vscale': sym["vscale"]}, skip_first=True)
 psim.generate()

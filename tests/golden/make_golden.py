@@ -38,6 +38,7 @@ KEEP = {
     "lj6x5x4": dict(steps=[0, 1, 10, 11, 60], pairs=[]),
     "custom6": dict(steps=[0, 1, 9, 10, 11, 30, 60], pairs=[]),
     "custom6_half": dict(steps=[0, 1, 10, 60], pairs=[]),
+    "custom_wca": dict(steps=[0, 1, 7, 8, 9, 20, 40], pairs=[]),
 }
 
 

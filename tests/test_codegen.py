@@ -43,7 +43,7 @@ def test_lowering_finds_roles_and_properties():
     pair = mods[1]
     assert pair.applied == ["force"] and pair.read_j == {"type"}
     assert mods[2].written == {"linear_velocity", "kinetic"}
-    assert layout.slots == ["force", "kinetic"]
+    assert layout.slots == ["force", "kinetic", "steps_done", "accel"]
     # operation order of the reference's generated C (left-associative products,
     # min() as the keyword's select chain, the symbol printed as a literal)
     assert "((((48.0 * v_sr6) * (v_sr6 - 0.5)) * v_sr2)" in src

@@ -26,7 +26,7 @@ def rms_rel(a, b):
     return np.abs(a - b).max() / max(np.sqrt((b ** 2).mean()), 1.0)
 
 
-@pytest.mark.parametrize("name", ["custom6", "custom6_half"])
+@pytest.mark.parametrize("name", ["custom6", "custom6_half", "custom_wca"])
 def test_generated_kernels_follow_the_reference(name):
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     cfg = json.loads(str(g["cfg"]))
@@ -46,13 +46,19 @@ def test_generated_kernels_follow_the_reference(name):
         if ts == 0 or (ts + 1) % every == 0:
             thermo.append("%g\t%g" % eng.compute_thermo())
     assert thermo == list(g["thermo"])
-    # the user property written by the damped half step: 0.5 m |v|^2 before damping
     v = eng.property("linear_velocity")
     m = eng.property("mass")
-    kin = eng.property("kinetic")
-    s2 = (v ** 2).sum(axis=1)
-    undamped = np.where(kin > 0.5 * m * cfg["symbols"]["vmax2"] * (1 - 1e-9), s2 / 0.999 ** 2, s2)
-    assert np.allclose(kin, 0.5 * m * undamped, rtol=1e-9, atol=0)
+    if cfg.get("program", "capped") == "capped":
+        # the user property written by the damped half step: 0.5 m |v|^2 before damping
+        kin = eng.property("kinetic")
+        s2 = (v ** 2).sum(axis=1)
+        undamped = np.where(kin > 0.5 * m * cfg["symbols"]["vmax2"] * (1 - 1e-9), s2 / 0.999 ** 2, s2)
+        assert np.allclose(kin, 0.5 * m * undamped, rtol=1e-9, atol=0)
+    else:
+        # integer and vector user properties of the clamped half step
+        assert np.array_equal(eng.property("steps_done"), np.full(len(m), cfg["timesteps"], dtype=np.int32))
+        frc = eng.state()[2]
+        assert np.allclose(eng.property("accel"), frc / m[:, None], rtol=1e-12, atol=1e-12)
 
 
 def test_api_run_prints_the_reference_thermo():
