@@ -143,48 +143,6 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
-// --- L2 eviction priorities for the force kernels' two streams ------------------
-// The Verlet list (hundreds of MB) is read once per pass; the positions it indexes
-// (16 bytes per particle) are read about 40 times each.  List loads take an L2
-// evict-first policy and skip L1; partner loads take evict-last in L2 and L1, so the
-// list stream does not push positions out of either cache.
-#ifndef PG_L2_HINTS
-#define PG_L2_HINTS 0
-#endif
-
-__device__ __forceinline__ uint64_t l2_policy_stream() {
-    uint64_t p;
-    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
-
-__device__ __forceinline__ uint64_t l2_policy_keep() {
-    uint64_t p;
-    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
-
-__device__ __forceinline__ int32_t ld_stream(const int32_t *a, uint64_t pol) {
-#if PG_L2_HINTS
-    int32_t v;
-    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
-    return v;
-#else
-    return __ldcs(a);
-#endif
-}
-
-__device__ __forceinline__ int4 ld_keep_i4(const int32_t *base, int i, uint64_t pol) {
-#if PG_L2_HINTS
-    int4 v;
-    asm("ld.global.nc.L1::evict_last.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
-        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(reinterpret_cast<const int4 *>(base) + i), "l"(pol));
-    return v;
-#else
-    return __ldg(reinterpret_cast<const int4 *>(base) + i);
-#endif
-}
-
 // --- fixed-point positions (pg_particles.pos_fx) ---------------------------------
 // x_fx = round((x - lo) * 2^32 / len) mod 2^32 per axis.  One box length is 2^32
 // units, so the wrapped 32-bit difference of two coordinates is the minimum-image

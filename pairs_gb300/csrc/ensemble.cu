@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(kBlock) k_ens_cutoff_fixup(EnsArgs a) {
 
 // ------------------------------------------------------------------ integrate
 
-// grid point nearest x, rounded in FP64 so that |lo| <= q/2 (the packed residual's range)
+// grid point nearest x, rounded in FP64 (|lo| <= q/2)
 __device__ __forceinline__ void ens_resplit(double x, float q, float iq, float &hi, float &lo) {
     split_pos(x, (double) iq, (double) q, hi, lo);
 }

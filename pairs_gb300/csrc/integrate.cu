@@ -114,7 +114,7 @@ struct MixArgs {
     pg_status *status;
 };
 
-// grid point nearest x, rounded in FP64 so that |lo| <= q/2 (the packed residual's range)
+// grid point nearest x, rounded in FP64 (|lo| <= q/2)
 __device__ __forceinline__ void resplit(double x, float q, float iq, float &hi, float &lo) {
     split_pos(x, (double) iq, (double) q, hi, lo);
 }

@@ -235,10 +235,9 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
                 }
                 return near;
             };
-            const uint64_t pol_list = l2_policy_stream(), pol_pos = l2_policy_keep();
             uint32_t cur[kBatch];
 #pragma unroll
-            for(int u = 0; u < kBatch; u++) { cur[u] = u < cnt ? (uint32_t) ld_stream(nb + u * stride, pol_list) : 0u; }
+            for(int u = 0; u < kBatch; u++) { cur[u] = u < cnt ? (uint32_t) __ldcs(nb + u * stride) : 0u; }
             for(int k0 = 0; k0 < cnt; k0 += kBatch) {
                 float4 hj[kBatch], lj[kBatch];
                 int4 fj[kBatch];
@@ -246,7 +245,7 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
                 for(int u = 0; u < kBatch; u++) {
                     const int j = (int) (cur[u] & PG_NBR_INDEX_MASK);      // 0 past the end: a valid row
                     if(kFixed) {
-                        fj[u] = ld_keep_i4(a.p.pos_fx, j, pol_pos);
+                        fj[u] = ld_i4(a.p.pos_fx, j);
                         hj[u] = lj[u] = make_float4(0.f, 0.f, 0.f, 0.f);
                     } else {
                         hj[u] = ld_f4(a.p.pos_hi, hl(a.p, j));
@@ -258,7 +257,7 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
                 const int32_t *nbn = nb + (size_t) (k0 + kBatch) * stride;
 #pragma unroll
                 for(int u = 0; u < kBatch; u++) {
-                    nxt[u] = k0 + kBatch + u < cnt ? (uint32_t) ld_stream(nbn + u * stride, pol_list) : 0u;
+                    nxt[u] = k0 + kBatch + u < cnt ? (uint32_t) __ldcs(nbn + u * stride) : 0u;
                 }
                 uint32_t pending = 0u;
 #pragma unroll
