@@ -224,7 +224,8 @@ typedef struct {
     int32_t n;
     int32_t capacity;
     double *pos;                 /* double4[capacity] */
-    double *vel;                 /* double4[capacity] linear velocity */
+    double *vel;                 /* double4[capacity] linear velocity; w = 1 / mass, written
+                                    by pg_dem_setup (0 for half spaces) */
     double *angvel;              /* double4[capacity] angular velocity */
     double *force;               /* double4[capacity] */
     double *torque;              /* double4[capacity] */

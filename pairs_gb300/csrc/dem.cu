@@ -71,6 +71,12 @@ __global__ void k_dem_setup(pg_dem_particles d) {
         d.mass[i] = __longlong_as_double(0x7ff0000000000000ll);
         d.inv_inertia[i] = 0.0;
     }
+    // vel.w keeps 1 / mass (0 for half spaces): the kernels read it with the velocity
+    // instead of dividing every step (the same IEEE quotient, so FP64 results are
+    // unchanged)
+    D4 v = ldd(d.vel, i);
+    v.w = 1.0 / d.mass[i];
+    st_d4(d.vel, i, v);
 }
 
 // ------------------------------------------------------------------ binning
@@ -168,7 +174,7 @@ __global__ void __launch_bounds__(kBlock) k_dem_list(DemArgs a) {
 // generated operation order; T = float is the mixed-precision contact model (the
 // overlap itself comes from FP64 geometry, see k_dem_force_mixed).
 template<typename T>
-__device__ void spring_dashpot(const pg_dem_params &p, T inv_mi, T mj, int tij, const T vi[3], const T vj[3],
+__device__ void spring_dashpot(const pg_dem_params &p, T inv_mi, T inv_mj, int tij, const T vi[3], const T vj[3],
                                const T wi[3], const T wj[3], const T n[3], const T ri[3], const T rj[3], T delta,
                                int &sticking, T h[4], T facc[3], T tacc[3]) {
     T vwi[3], vwj[3], rel[3], reln[3], relt[3];
@@ -183,7 +189,7 @@ __device__ void spring_dashpot(const pg_dem_params &p, T inv_mi, T mj, int tij, 
     for(int e = 0; e < 3; e++) { reln[e] = vn * n[e]; relt[e] = rel[e] - reln[e]; }
     const T lrt = sqrt(relt[0] * relt[0] + relt[1] * relt[1] + relt[2] * relt[2]);
     const bool cond1a = (sticking == 1) && (lrt < T(1e-08));
-    const T meff = T(1.0) / (inv_mi + (T(1.0) / mj));
+    const T meff = T(1.0) / (inv_mi + inv_mj);
     const T pi = T(p.pi), ln_e = T(p.ln_e), kappa = T(p.kappa), dt = T(p.dt);
     T kn, dn;
     if(p.kn > 0.0) {
@@ -274,7 +280,7 @@ __device__ __forceinline__ void dem_contact(const DemArgs &a, int i, int j, cons
     const int tij = ti * a.prm.ntypes + (a.d.type ? a.d.type[j] : 0);
     const D4 vj4 = ldd(a.d.vel, j), wj4 = ldd(a.d.angvel, j);
     const T vj[3] = {T(vj4.x), T(vj4.y), T(vj4.z)}, wj[3] = {T(wj4.x), T(wj4.y), T(wj4.z)};
-    spring_dashpot<T>(a.prm, inv_mi, T(a.d.mass[j]), tij, vi, vj, wi, wj, n, ri, rj, delta, sticking, h, f, t);
+    spring_dashpot<T>(a.prm, inv_mi, T(vj4.w), tij, vi, vj, wi, wj, n, ri, rj, delta, sticking, h, f, t);
     a.c.sticking[s] = sticking;
     st_d4(a.c.history, (int) s, make_d4(h[0], h[1], h[2], h[3]));
 }
@@ -323,7 +329,7 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force(DemArgs a) {
     const D4 xi = ldd(a.d.pos, i), v4 = ldd(a.d.vel, i), w4 = ldd(a.d.angvel, i);
     const double vi[3] = {v4.x, v4.y, v4.z}, wi[3] = {w4.x, w4.y, w4.z};
     const double ri = a.d.radius[i];
-    const double inv_mi = 1.0 / a.d.mass[i];
+    const double inv_mi = v4.w;                  // 1 / mass (pg_dem_setup)
     const int ti = a.d.type ? a.d.type[i] : 0;
     int nc = a.c.count[i];
     uint32_t used[2] = {0u, 0u};
@@ -402,7 +408,7 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force_mixed(DemArgs a) {
     const float vi[3] = {(float) v4.x, (float) v4.y, (float) v4.z};
     const float wi[3] = {(float) w4.x, (float) w4.y, (float) w4.z};
     const double ri = a.d.radius[i];
-    const float inv_mi = 1.0f / (float) a.d.mass[i];
+    const float inv_mi = (float) v4.w;
     // FP32 screen: a candidate whose FP32 distance exceeds the contact distance by more
     // than the FP32 rounding of the coordinates (a.screen) cannot touch
     const float4 pi32 = ld_f4(a.d.pos32, i);
@@ -498,7 +504,7 @@ __global__ void __launch_bounds__(kBlock) k_dem_euler(DemArgs a) {
         const D4 X = ldd(a.d.pos, i), V = ldd(a.d.vel, i), W = ldd(a.d.angvel, i);
         const D4 F = ldd(a.d.force, i), T = ldd(a.d.torque, i), Qd = ldd(a.d.quat, i);
         const double Qo[4] = {Qd.x, Qd.y, Qd.z, Qd.w};
-        const double im = 1.0 / a.d.mass[i];
+        const double im = V.w;                   // 1 / mass (pg_dem_setup)
         const double h = 0.5 * im;
         const double f3[3] = {F.x, F.y, F.z}, t3[3] = {T.x, T.y, T.z};
         double x3[3] = {X.x, X.y, X.z}, v3[3] = {V.x, V.y, V.z}, w3[3] = {W.x, W.y, W.z};
@@ -544,7 +550,7 @@ __global__ void __launch_bounds__(kBlock) k_dem_euler(DemArgs a) {
         if(a.d.pos32 != nullptr) {
             st_f4(a.d.pos32, i, make_float4((float) x3[0], (float) x3[1], (float) x3[2], (float) a.d.radius[i]));
         }
-        st_d4(a.d.vel, i, make_d4(v3[0], v3[1], v3[2], 0.0));
+        st_d4(a.d.vel, i, make_d4(v3[0], v3[1], v3[2], V.w));
         if(a.d.pos_ref != nullptr) {
             const D4 r0 = ldd(a.d.pos_ref, i);
             const double ex = x3[0] - r0.x, ey = x3[1] - r0.y, ez = x3[2] - r0.z;
