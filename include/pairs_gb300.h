@@ -199,6 +199,9 @@ typedef struct {
     double  quantum;             /* grid step of this replica's pos_hi */
     float   len_hi[3];
     float   len_lo[3];
+    double  fx_scale[3];         /* 2^32 / len: fixed-point units of this replica's box (pos_fx) */
+    float   fx_unit[3];          /* len / 2^32 rounded to FP32 */
+    int32_t fx_pad_;
 } pg_replica;
 
 /* A batched ensemble (config: hundreds of independent periodic LJ replicas run by
@@ -452,8 +455,9 @@ int pg_ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_w
 int pg_ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                             double r_list2, pg_status *status, void *stream);
 
-/* Mixed-precision LJ forces (FP32 on compensated positions) for every replica,
- * tpa threads per particle, full lists.  Pairs within a relative 1e-5 of the cutoff
+/* Mixed-precision LJ forces for every replica, tpa threads per particle, full lists:
+ * FP32 on fixed-point positions (p->pos_fx, each replica's box 2^32 units, used when set)
+ * or on compensated positions.  Pairs within a relative 1e-5 of the cutoff
  * are decided by the FP64 test, as in pg_lj_force, through a queue in ws (scratch, at
  * least 8448 bytes; the binning workspace serves). */
 int pg_ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list,

@@ -85,11 +85,18 @@ __global__ void __launch_bounds__(kBlock) k_ens_count(EnsArgs a, int32_t *count)
     atomicAdd(&count[cell], 1);
 }
 
-// hi/lo split on each replica's own grid
+// fixed-point position on a replica's own box (2^32 units per box length)
+__device__ __forceinline__ int4 ens_fx(const pg_replica &R, const D4 &x, int type) {
+    return make_int4(to_fx(x.x, R.lo[0], R.fx_scale[0]), to_fx(x.y, R.lo[1], R.fx_scale[1]),
+                     to_fx(x.z, R.lo[2], R.fx_scale[2]), type);
+}
+
+// hi/lo split on each replica's own grid (and its fixed-point position)
 __global__ void __launch_bounds__(kBlock) k_ens_split(EnsArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= a.p.n) { return; }
-    const double q = a.e.replicas[a.e.replica_of[i]].quantum, iq = 1.0 / q;
+    const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
+    const double q = R.quantum, iq = 1.0 / q;
     const D4 x = ld_d4_plain(a.p.pos, i);
     float4 h, l;
     split_pos(x.x, iq, q, h.x, l.x);
@@ -99,6 +106,7 @@ __global__ void __launch_bounds__(kBlock) k_ens_split(EnsArgs a) {
     l.w = 0.0f;
     st_f4(a.p.pos_hi, hl(a.p, i), h);
     st_f4(a.p.pos_lo, hl(a.p, i), l);
+    if(a.p.pos_fx != nullptr) { st_i4(a.p.pos_fx, i, ens_fx(R, x, __float_as_int(h.w))); }
 }
 
 // ------------------------------------------------------------------ list build
@@ -129,8 +137,12 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
     const D4 xi = ld_d4(a.p.pos, i);
     st_d4(a.p.pos_ref, i, xi);
     const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
-    st_f4(a.p.ref_hi, i, hi);
-    st_f4(a.p.ref_lo, i, lo);
+    if(a.p.ref_fx != nullptr) {
+        st_i4(a.p.ref_fx, i, ld_i4(a.p.pos_fx, i));
+    } else {
+        st_f4(a.p.ref_hi, i, hi);
+        st_f4(a.p.ref_lo, i, lo);
+    }
     const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
     const int tpa = a.e.tpa;
     int cnt = 0;
@@ -218,16 +230,34 @@ __device__ __forceinline__ float ens_lj(const EnsArgs &a, int tij, float rsq) {
 // of the cutoff is queued for k_ens_cutoff_fixup, which decides it in FP64.
 constexpr int kEnsBatch = 4;
 
-template<int TPA, bool kOneType>
+// A pair's separation: fixed point (wrapped difference in the replica's units, no
+// image shift) or compensated hi/lo with the listed image.
+template<bool kFixed>
+__device__ __forceinline__ void ens_pair_delta(const pg_replica &R, const int4 &fi, const float4 &hi, const float4 &lo,
+                                               const int4 &fj, const float4 &hj, const float4 &lj, uint32_t code,
+                                               float &dx, float &dy, float &dz) {
+    if(kFixed) {
+        dx = (float) fx_diff(fi.x, fj.x) * R.fx_unit[0];
+        dy = (float) fx_diff(fi.y, fj.y) * R.fx_unit[1];
+        dz = (float) fx_diff(fi.z, fj.z) * R.fx_unit[2];
+    } else {
+        ens_delta(R, hi, lo, hj, lj, code, dx, dy, dz);
+    }
+}
+
+template<int TPA, bool kOneType, bool kFixed>
 __global__ void k_ens_force(EnsArgs a) {
     if(frozen_force(a.p)) { return; }
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = g / TPA, t = g % TPA;
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     if(i < a.p.n) {
-        const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
+        float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+        int4 fi = make_int4(0, 0, 0, 0);
+        if(kFixed) { fi = ld_i4(a.p.pos_fx, i); }
+        else { hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i)); }
         const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
-        const int ti = kOneType ? 0 : __float_as_int(hi.w) * a.ntypes;
+        const int ti = kOneType ? 0 : (kFixed ? fi.w : __float_as_int(hi.w)) * a.ntypes;
         const int cnt = a.list.count[i];
         const int rows = cnt > t ? (cnt - t + TPA - 1) / TPA : 0;      // this lane's entries
         const int32_t *nb = a.list.nbr + (size_t) i * TPA + t;
@@ -236,6 +266,7 @@ __global__ void k_ens_force(EnsArgs a) {
         for(int r0 = 0; r0 < rows; r0 += kEnsBatch) {
             uint32_t e[kEnsBatch];
             float4 hj[kEnsBatch], lj[kEnsBatch];
+            int4 fj[kEnsBatch];
 #pragma unroll
             for(int u = 0; u < kEnsBatch; u++) {
                 e[u] = r0 + u < rows ? (uint32_t) __ldcs(nb + (r0 + u) * row) : 0u;
@@ -243,19 +274,26 @@ __global__ void k_ens_force(EnsArgs a) {
 #pragma unroll
             for(int u = 0; u < kEnsBatch; u++) {
                 const int j = (int) (e[u] & PG_NBR_INDEX_MASK);
-                hj[u] = ld_f4(a.p.pos_hi, hl(a.p, j));
-                lj[u] = ld_f4(a.p.pos_lo, hl(a.p, j));
+                if(kFixed) {
+                    fj[u] = ld_i4(a.p.pos_fx, j);
+                    hj[u] = lj[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                } else {
+                    hj[u] = ld_f4(a.p.pos_hi, hl(a.p, j));
+                    lj[u] = ld_f4(a.p.pos_lo, hl(a.p, j));
+                    fj[u] = make_int4(0, 0, 0, 0);
+                }
             }
             uint32_t pending = 0u;
 #pragma unroll
             for(int u = 0; u < kEnsBatch; u++) {
                 if(r0 + u >= rows) { continue; }
                 float dx, dy, dz;
-                ens_delta(R, hi, lo, hj[u], lj[u], e[u] >> PG_NBR_INDEX_BITS, dx, dy, dz);
+                ens_pair_delta<kFixed>(R, fi, hi, lo, fj[u], hj[u], lj[u], e[u] >> PG_NBR_INDEX_BITS, dx, dy, dz);
                 const float rsq = dx * dx + dy * dy + dz * dz;
                 const bool near = fabsf(rsq - c2) < band;
                 if(rsq < c2 && !near) {
-                    const float f = ens_lj(a, kOneType ? 0 : ti + __float_as_int(hj[u].w), rsq);
+                    const int tj = kFixed ? fj[u].w : __float_as_int(hj[u].w);
+                    const float f = ens_lj(a, kOneType ? 0 : ti + tj, rsq);
                     fx += dx * f; fy += dy * f; fz += dz * f;
                 }
                 if(near) { pending |= 1u << u; }
@@ -280,7 +318,7 @@ __global__ void k_ens_force(EnsArgs a) {
 
 // Queued near-cutoff pairs: the FP64 test of the single-system FP64 path decides;
 // a pair inside adds its FP32 force (full lists: no reaction).
-template<bool kOneType>
+template<bool kOneType, bool kFixed>
 __global__ void __launch_bounds__(kBlock) k_ens_cutoff_fixup(EnsArgs a) {
     if(frozen_force(a.p)) { return; }
     const int total = min(*a.cut_count, a.cut_capacity);
@@ -292,11 +330,18 @@ __global__ void __launch_bounds__(kBlock) k_ens_cutoff_fixup(EnsArgs a) {
         const uint32_t code = e >> PG_NBR_INDEX_BITS;
         const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
         if(!exact_inside(a.p.pos, i, j, code, R.len, a.cutoff2d)) { continue; }
-        const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
-        const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+        float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi, hj = hi, lj = hi;
+        int4 fi = make_int4(0, 0, 0, 0), fj = fi;
+        if(kFixed) {
+            fi = ld_i4(a.p.pos_fx, i); fj = ld_i4(a.p.pos_fx, j);
+        } else {
+            hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i));
+            hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+        }
         float dx, dy, dz;
-        ens_delta(R, hi, lo, hj, lj, code, dx, dy, dz);
-        const int tij = kOneType ? 0 : __float_as_int(hi.w) * a.ntypes + __float_as_int(hj.w);
+        ens_pair_delta<kFixed>(R, fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
+        const int ti = kFixed ? fi.w : __float_as_int(hi.w), tj = kFixed ? fj.w : __float_as_int(hj.w);
+        const int tij = kOneType ? 0 : ti * a.ntypes + tj;
         const float f = ens_lj(a, tij, dx * dx + dy * dy + dz * dz);
         asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
                      :: "l"(a.p.force32 + 4 * (size_t) i), "f"(dx * f), "f"(dy * f), "f"(dz * f), "f"(0.0f) : "memory");
@@ -329,20 +374,34 @@ __global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
             x.y = fma(a.dt, v.y, x.y);
             x.z = fma(a.dt, v.z, x.z);
             st_d4(a.p.pos, i, x);
-            const float q = (float) a.e.replicas[a.e.replica_of[i]].quantum, iq = 1.0f / q;
-            float4 h, l;
-            ens_resplit(x.x, q, iq, h.x, l.x);
-            ens_resplit(x.y, q, iq, h.y, l.y);
-            ens_resplit(x.z, q, iq, h.z, l.z);
-            h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);
-            l.w = 0.0f;
-            st_f4(a.p.pos_hi, hl(a.p, i), h);
-            st_f4(a.p.pos_lo, hl(a.p, i), l);
-            const float4 rh = ld_f4(a.p.ref_hi, i);
-            const float4 rl = ld_f4(a.p.ref_lo, i);
-            const float dx = (h.x - rh.x) + (l.x - rl.x);
-            const float dy = (h.y - rh.y) + (l.y - rl.y);
-            const float dz = (h.z - rh.z) + (l.z - rl.z);
+            const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
+            const int type = a.p.type != nullptr ? a.p.type[i] : 0;
+            float dx, dy, dz;
+            if(a.p.pos_fx != nullptr) {
+                // fixed point only: hi/lo are split again at the next binning, which is
+                // the only reader of them
+                const int4 xf = ens_fx(R, x, type);
+                st_i4(a.p.pos_fx, i, xf);
+                const int4 rf = ld_i4(a.p.ref_fx, i);
+                dx = (float) fx_diff(xf.x, rf.x) * R.fx_unit[0];
+                dy = (float) fx_diff(xf.y, rf.y) * R.fx_unit[1];
+                dz = (float) fx_diff(xf.z, rf.z) * R.fx_unit[2];
+            } else {
+                const float q = (float) R.quantum, iq = 1.0f / q;
+                float4 h, l;
+                ens_resplit(x.x, q, iq, h.x, l.x);
+                ens_resplit(x.y, q, iq, h.y, l.y);
+                ens_resplit(x.z, q, iq, h.z, l.z);
+                h.w = __int_as_float(type);
+                l.w = 0.0f;
+                st_f4(a.p.pos_hi, hl(a.p, i), h);
+                st_f4(a.p.pos_lo, hl(a.p, i), l);
+                const float4 rh = ld_f4(a.p.ref_hi, i);
+                const float4 rl = ld_f4(a.p.ref_lo, i);
+                dx = (h.x - rh.x) + (l.x - rl.x);
+                dy = (h.y - rh.y) + (l.y - rl.y);
+                dz = (h.z - rh.z) + (l.z - rl.z);
+            }
             const float d2 = dx * dx + dy * dy + dz * dz;
             if(d2 > a.half_skin2_hi) {
                 tripped = true;
@@ -409,8 +468,9 @@ int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_work
 
 int ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                          double r_list2, pg_status *status, cudaStream_t st) {
-    if(!ens_ok(e, p) || !cells || !list || !list->nbr || !list->count || !status || !p->pos_ref || !p->ref_hi ||
-       !p->ref_lo || list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS) || list->half) {
+    if(!ens_ok(e, p) || !cells || !list || !list->nbr || !list->count || !status || !p->pos_ref || !p->pos_hi ||
+       !p->pos_lo || (p->ref_fx != nullptr ? !p->pos_fx : (!p->ref_hi || !p->ref_lo)) || list->stride < p->n ||
+       p->n >= (1 << PG_NBR_INDEX_BITS) || list->half) {
         return PG_ERR_ARGUMENT;
     }
     EnsArgs a = {};
@@ -423,18 +483,24 @@ int ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *
 }
 
 template<int TPA>
-static void launch_force(const EnsArgs &a, int n, int block, bool one, cudaStream_t st) {
+static void launch_force(const EnsArgs &a, int n, int block, bool one, bool fixed, cudaStream_t st) {
     const int64_t threads = (int64_t) n * TPA;
     const int grid = (int) ((threads + block - 1) / block);
-    if(one) { k_ens_force<TPA, true><<<grid, block, 0, st>>>(a); }
-    else { k_ens_force<TPA, false><<<grid, block, 0, st>>>(a); }
+    if(fixed) {
+        if(one) { k_ens_force<TPA, true, true><<<grid, block, 0, st>>>(a); }
+        else { k_ens_force<TPA, false, true><<<grid, block, 0, st>>>(a); }
+    } else {
+        if(one) { k_ens_force<TPA, true, false><<<grid, block, 0, st>>>(a); }
+        else { k_ens_force<TPA, false, false><<<grid, block, 0, st>>>(a); }
+    }
     note_launch();
 }
 
 int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
                    pg_workspace ws, cudaStream_t st) {
-    if(!ens_ok(e, p) || !list || !list->nbr || !list->count || !lj || !p->pos_hi || !p->pos_lo || !p->force32 ||
-       lj->ntypes < 1 || lj->ntypes > 8 || (lj->ntypes > 1 && !p->type)) {
+    const bool fixed = p->pos_fx != nullptr;
+    if(!ens_ok(e, p) || !list || !list->nbr || !list->count || !lj || (!fixed && (!p->pos_hi || !p->pos_lo)) ||
+       !p->force32 || lj->ntypes < 1 || lj->ntypes > 8 || (lj->ntypes > 1 && !p->type)) {
         return PG_ERR_ARGUMENT;
     }
     EnsArgs a = {};
@@ -455,21 +521,28 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
     cudaMemsetAsync(a.cut_count, 0, sizeof(int32_t), st);
     const bool one = lj->ntypes == 1;
     switch(e->tpa) {
-        case 1: launch_force<1>(a, p->n, e->block, one, st); break;
-        case 2: launch_force<2>(a, p->n, e->block, one, st); break;
-        case 4: launch_force<4>(a, p->n, e->block, one, st); break;
-        default: launch_force<8>(a, p->n, e->block, one, st); break;
+        case 1: launch_force<1>(a, p->n, e->block, one, fixed, st); break;
+        case 2: launch_force<2>(a, p->n, e->block, one, fixed, st); break;
+        case 4: launch_force<4>(a, p->n, e->block, one, fixed, st); break;
+        default: launch_force<8>(a, p->n, e->block, one, fixed, st); break;
     }
-    if(one) { k_ens_cutoff_fixup<true><<<16, kBlock, 0, st>>>(a); }
-    else { k_ens_cutoff_fixup<false><<<16, kBlock, 0, st>>>(a); }
+    if(fixed) {
+        if(one) { k_ens_cutoff_fixup<true, true><<<16, kBlock, 0, st>>>(a); }
+        else { k_ens_cutoff_fixup<false, true><<<16, kBlock, 0, st>>>(a); }
+    } else {
+        if(one) { k_ens_cutoff_fixup<true, false><<<16, kBlock, 0, st>>>(a); }
+        else { k_ens_cutoff_fixup<false, false><<<16, kBlock, 0, st>>>(a); }
+    }
     note_launch();
     return launch_status();
 }
 
 int ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift, double half_skin2,
                        int32_t step, pg_status *status, cudaStream_t st) {
-    if(!ens_ok(e, p) || !p->pos || !p->vel || !p->mass || !p->force32 || !p->pos_hi || !p->pos_lo || !status ||
-       (kicks != 1 && kicks != 2) || (drift && (!p->ref_hi || !p->ref_lo || !p->pos_ref))) {
+    const bool fixed = p->pos_fx != nullptr;
+    if(!ens_ok(e, p) || !p->pos || !p->vel || !p->mass || !p->force32 || (!fixed && (!p->pos_hi || !p->pos_lo)) ||
+       !status || (kicks != 1 && kicks != 2) ||
+       (drift && (!p->pos_ref || (fixed ? !p->ref_fx : (!p->ref_hi || !p->ref_lo))))) {
         return PG_ERR_ARGUMENT;
     }
     EnsArgs a = {};

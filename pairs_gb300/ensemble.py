@@ -27,7 +27,8 @@ INT32_MAX = 2 ** 31 - 1
 
 class Ensemble:
     def __init__(self, replicas, *, cutoff=2.5, skin=0.3, dt=0.005, epsilon=1.0, sigma6=1.0, tpa=1, block=256,
-                 reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, device="cuda"):
+                 reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, fixed_point=None,
+                 device="cuda"):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -49,6 +50,14 @@ class Ensemble:
         for L in self.boxes:
             if min(L) <= 2.0 * self.r_list:
                 raise ValueError("every replica box must be longer than 2 (cutoff + skin)")
+        # fixed-point positions (2^32 units per replica box) for the force pass and the
+        # guard: a listed pair stays below half a box while every box exceeds
+        # 2 (r_list + skin) (the guard bounds each displacement by skin/2); the list
+        # build keeps the compensated hi/lo screen, split again at every binning
+        fx_ok = all(min(L) > 2.0 * (self.r_list + skin) for L in self.boxes)
+        if fixed_point and not fx_ok:
+            raise ValueError("fixed-point positions need every replica box longer than 2 (cutoff + 2 skin)")
+        self.fixed_point = fx_ok if fixed_point is None else bool(fixed_point)
         self.ts = 0
         self.nbuilds = 0
         self.host_syncs = 0
@@ -67,6 +76,9 @@ class Ensemble:
             t[name] = z((n, 4), f64)
         for name in ("pos_hi", "pos_lo", "ref_hi", "ref_lo", "force32"):
             t[name] = z((n, 4), f32)
+        if self.fixed_point:
+            t["pos_fx"] = z((n, 4), i32)
+            t["ref_fx"] = z((n, 4), i32)
         t["mass"] = z((n,), f64)
         t["type"] = z((n,), i32)
         t["uid"] = z((n,), i32)
@@ -84,8 +96,8 @@ class Ensemble:
         self.p = A.PgParticles()
         self.p.n = self.p.capacity = n
         for name in ("pos", "vel", "pos_ref", "pos_hi", "pos_lo", "ref_hi", "ref_lo", "force32", "mass", "type",
-                     "uid"):
-            setattr(self.p, name, t[name].data_ptr())
+                     "uid", "pos_fx", "ref_fx"):
+            setattr(self.p, name, t[name].data_ptr() if name in t else None)
         self.p.guard = None
 
         self.lj = A.PgLJParams()
@@ -144,6 +156,8 @@ class Ensemble:
                 lh = round(L[d] / q) * q
                 R.len_hi[d] = lh
                 R.len_lo[d] = L[d] - lh
+                R.fx_scale[d] = 2.0 ** 32 / L[d]
+                R.fx_unit[d] = float(np.float32(L[d] / 2.0 ** 32))
             cell0 += nc
         self.ncells = cell0
         self.e.ncells = cell0

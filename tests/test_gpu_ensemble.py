@@ -6,7 +6,8 @@
 * forces agree with the FP64 oracle to the mixed path's 1e-5 (RMS-normalised), and
   the layouts agree with each other;
 * a replica advanced inside the ensemble follows the single-system mixed engine
-  (same kernels' arithmetic) to round-off, step for step;
+  (same kernels' arithmetic) to round-off, step for step, and the fixed-point layout
+  follows the compensated one;
 * speculative chunks replayed as CUDA graphs give the same trajectory as the same
   chunks launched one by one;
 * per-replica thermo equals the oracle's temperature of the same velocities.
@@ -53,7 +54,8 @@ def test_replica_follows_single_system_engine():
     from pairs_gb300.engine import LJEngine
     from pairs_gb300.ensemble import Ensemble
     reps = replicas()
-    ens = Ensemble(reps, tpa=1, reach=1, policy="every")      # the engine's 27-cell stencil
+    # the engine's 27-cell stencil and its compensated hi/lo positions
+    ens = Ensemble(reps, tpa=1, reach=1, policy="every", fixed_point=False)
     ens.run(25)
     ens.synchronize()
     worst = 0.0
@@ -68,6 +70,23 @@ def test_replica_follows_single_system_engine():
     # same arithmetic per pair; the single-system kernel applies a pair within 1e-5 of
     # the cutoff in a second pass, so such a particle's force sums in another order
     assert worst < 1e-8
+
+
+def test_fixed_point_replicas_follow_compensated_replicas():
+    """Fixed-point positions (each replica box 2^32 units) in the force pass and the
+    guard give the trajectory of the compensated hi/lo layout to FP32 round-off."""
+    from pairs_gb300.ensemble import Ensemble
+    reps = replicas()
+    a = Ensemble(reps, tpa=2, policy="every")
+    b = Ensemble(reps, tpa=2, policy="every", fixed_point=False)
+    assert a.fixed_point and not b.fixed_point
+    a.run(25)
+    b.run(25)
+    a.synchronize()
+    b.synchronize()
+    worst = max(np.abs(a.replica_state(r)[0] - b.replica_state(r)[0]).max() for r in range(len(reps)))
+    print("max position difference after 25 steps", worst)
+    assert worst < 1e-6
 
 
 def test_graph_chunks_equal_plain_chunks():
