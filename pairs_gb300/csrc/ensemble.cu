@@ -118,10 +118,6 @@ __device__ __forceinline__ float ens_delta(float hi_i, float lo_i, float hi_j, f
     return __fadd_rn(__fsub_rn(__fsub_rn(hi_i, hi_j), sh), __fsub_rn(__fsub_rn(lo_i, lo_j), sl));
 }
 
-__device__ __forceinline__ size_t ens_slot(int k, int i, int stride, int tpa) {
-    return ((size_t) (k / tpa) * stride + i) * tpa + (k % tpa);
-}
-
 // a periodic stencil coordinate c in [-dims, 2 dims): neighbour cell and image shift
 // (offsets beyond one box are skipped by the caller; replicas are larger than
 // 2 r_list, so they hold no partner)
@@ -151,6 +147,14 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
         const int dz_ = R.dims[2], dy_ = R.dims[1], dx_ = R.dims[0], rr = R.reach;
         const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
         const int stride = a.list.stride, cap = a.list.max_neighbors;
+        // fixed-point screen where the replica's grid keeps every candidate's stencil
+        // image within half a box (at least 4 cells per axis, 6 with reach 2; see
+        // nlist.cu), the compensated one elsewhere
+        const int need = rr == 1 ? 4 : 6;
+        const bool fxs = a.p.pos_fx != nullptr && dx_ >= need && dy_ >= need && dz_ >= need;
+        const int4 fi = fxs ? ld_i4(a.p.pos_fx, i) : make_int4(0, 0, 0, 0);
+        int32_t *wp = a.list.nbr + (size_t) i * tpa;       // entry 0 of the interleaved layout
+        const size_t row_step = (size_t) stride * tpa - (size_t) (tpa - 1);
         for(int ox = -rr; ox <= rr; ox++) {
             if(ox < -dx_ || ox > dx_) { continue; }
             int nx, sx;
@@ -168,10 +172,18 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
                     const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
                     for(int j = b; j < e; j++) {
                         if(j == i && code == 0u) { continue; }
-                        const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
-                        const float fx = ens_delta(hi.x, lo.x, hj.x, lj.x, sx, R.len_hi[0], R.len_lo[0]);
-                        const float fy = ens_delta(hi.y, lo.y, hj.y, lj.y, sy, R.len_hi[1], R.len_lo[1]);
-                        const float fz = ens_delta(hi.z, lo.z, hj.z, lj.z, sz, R.len_hi[2], R.len_lo[2]);
+                        float fx, fy, fz;
+                        if(fxs) {
+                            const int4 fj = ld_i4(a.p.pos_fx, j);
+                            fx = (float) fx_diff(fi.x, fj.x) * R.fx_unit[0];
+                            fy = (float) fx_diff(fi.y, fj.y) * R.fx_unit[1];
+                            fz = (float) fx_diff(fi.z, fj.z) * R.fx_unit[2];
+                        } else {
+                            const float4 hj = ld_f4(a.p.pos_hi, hl(a.p, j)), lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+                            fx = ens_delta(hi.x, lo.x, hj.x, lj.x, sx, R.len_hi[0], R.len_lo[0]);
+                            fy = ens_delta(hi.y, lo.y, hj.y, lj.y, sy, R.len_hi[1], R.len_lo[1]);
+                            fz = ens_delta(hi.z, lo.z, hj.z, lj.z, sz, R.len_hi[2], R.len_lo[2]);
+                        }
                         const float r2f = fx * fx + fy * fy + fz * fz;
                         bool keep;
                         if(r2f < a.r2_lo) { keep = true; }
@@ -185,7 +197,8 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
                         }
                         if(keep) {
                             if(cnt < cap) {
-                                a.list.nbr[ens_slot(cnt, i, stride, tpa)] = (int32_t) (code | (uint32_t) j);
+                                *wp = (int32_t) (code | (uint32_t) j);
+                                wp += ((cnt + 1) & (tpa - 1)) == 0 ? row_step : 1;
                             }
                             cnt++;
                         }
