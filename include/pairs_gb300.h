@@ -215,6 +215,10 @@ typedef struct {
     const int32_t *replica_of;   /* device [capacity]: replica of each particle */
     int32_t tpa;                 /* threads per particle in the force kernel: 1, 2, 4 or 8 */
     int32_t block;               /* threads per block of the force kernel: 64..512 */
+    int32_t half;                /* 1: half lists (the list's own flag must agree); the drift
+                                    pass of pg_ensemble_integrate then zeroes force32 after its
+                                    kick, and the force pass adds reactions into it */
+    int32_t pad_;
 } pg_ensemble;
 
 /* DEM particle state, sorted order (the properties of examples/dem.py:144-162).

@@ -109,7 +109,8 @@ class PgReplica(C.Structure):
 
 class PgEnsemble(C.Structure):
     _fields_ = [("nreplicas", C.c_int32), ("ncells", C.c_int32), ("replicas", C.c_void_p),
-                ("replica_of", C.c_void_p), ("tpa", C.c_int32), ("block", C.c_int32)]
+                ("replica_of", C.c_void_p), ("tpa", C.c_int32), ("block", C.c_int32), ("half", C.c_int32),
+                ("pad_", C.c_int32)]
 
 
 STRUCTS = [PgStatus, PgBox, PgParticles, PgCells, PgNeighborList, PgLJParams, PgWorkspace, PgDemParticles,

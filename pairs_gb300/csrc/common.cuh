@@ -114,6 +114,12 @@ __device__ __forceinline__ bool exact_inside(const double *pos, int i, int j, ui
     return ref_rsq(__dsub_rn(xi.x, jx), __dsub_rn(xi.y, jy), __dsub_rn(xi.z, jz)) < cutoff2;
 }
 
+__device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float c) {
+    // one vector reduction to L2 instead of three scalar atomics (sm_90+)
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
+                 :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(0.0f) : "memory");
+}
+
 // Queue of near-cutoff pairs (particle, list entry) for a second, FP64-deciding pass.
 __device__ __forceinline__ void cut_queue_push(int32_t *count, int2 *rec, int capacity, int i, uint32_t e) {
     const int slot = atomicAdd(count, 1);

@@ -168,10 +168,16 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
                     int nz, sz;
                     wrap_cell(cz + oz, dz_, nz, sz);
                     const int c = R.cell0 + (nx * dy_ + ny) * dz_ + nz;
-                    const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
                     const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
+                    // half lists as the single-system build (nlist.cu): an interior pair
+                    // once, stored by the lower cell's particle, by index parity within a
+                    // cell; a pair through an image from both sides
+                    if(a.list.half && code == 0u && c < a.cells.particle_cell[i]) { continue; }
+                    const bool own = a.list.half && code == 0u && c == a.cells.particle_cell[i];
+                    const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
                     for(int j = b; j < e; j++) {
                         if(j == i && code == 0u) { continue; }
+                        if(own && ((j > i) == (((i ^ j) & 1) != 0))) { continue; }
                         float fx, fy, fz;
                         if(fxs) {
                             const int4 fj = ld_i4(a.p.pos_fx, j);
@@ -308,6 +314,9 @@ __global__ void k_ens_force(EnsArgs a) {
                     const int tj = kFixed ? fj[u].w : __float_as_int(hj[u].w);
                     const float f = ens_lj(a, kOneType ? 0 : ti + tj, rsq);
                     fx += dx * f; fy += dy * f; fz += dz * f;
+                    if(a.list.half && (e[u] >> PG_NBR_INDEX_BITS) == 0u) {
+                        red_add_v4(a.p.force32 + 4 * (size_t) (e[u] & PG_NBR_INDEX_MASK), -dx * f, -dy * f, -dz * f);
+                    }
                 }
                 if(near) { pending |= 1u << u; }
             }
@@ -326,7 +335,10 @@ __global__ void k_ens_force(EnsArgs a) {
             fz += __shfl_xor_sync(0xffffffffu, fz, o);
         }
     }
-    if(i < a.p.n && t == 0) { st_f4(a.p.force32, i, make_float4(fx, fy, fz, 0.0f)); }
+    if(i < a.p.n && t == 0) {
+        if(a.list.half) { red_add_v4(a.p.force32 + 4 * (size_t) i, fx, fy, fz); }   // reactions add too
+        else { st_f4(a.p.force32, i, make_float4(fx, fy, fz, 0.0f)); }
+    }
 }
 
 // Queued near-cutoff pairs: the FP64 test of the single-system FP64 path decides;
@@ -356,8 +368,8 @@ __global__ void __launch_bounds__(kBlock) k_ens_cutoff_fixup(EnsArgs a) {
         const int ti = kFixed ? fi.w : __float_as_int(hi.w), tj = kFixed ? fj.w : __float_as_int(hj.w);
         const int tij = kOneType ? 0 : ti * a.ntypes + tj;
         const float f = ens_lj(a, tij, dx * dx + dy * dy + dz * dz);
-        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
-                     :: "l"(a.p.force32 + 4 * (size_t) i), "f"(dx * f), "f"(dy * f), "f"(dz * f), "f"(0.0f) : "memory");
+        red_add_v4(a.p.force32 + 4 * (size_t) i, dx * f, dy * f, dz * f);
+        if(a.list.half && code == 0u) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
     }
 }
 
@@ -373,7 +385,11 @@ __global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool tripped = false;
     if(i < a.p.n) {
-        const float4 f = ld_f4(a.p.force32, i);
+        // a coherent load: with half lists this pass then zeroes the force (it is the last
+        // reader before the next force pass, which accumulates reactions into zeros), and a
+        // read-only-cache load could be moved past that store
+        const float4 f = reinterpret_cast<const float4 *>(a.p.force32)[i];
+        if(a.e.half && a.drift) { st_f4(a.p.force32, i, make_float4(0.0f, 0.0f, 0.0f, 0.0f)); }
         const double m = a.p.mass[i];
         const double c = m == 1.0 ? a.kick : a.kick / m;
         D4 v = ld_d4_plain(a.p.vel, i);
@@ -483,7 +499,7 @@ int ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *
                          double r_list2, pg_status *status, cudaStream_t st) {
     if(!ens_ok(e, p) || !cells || !list || !list->nbr || !list->count || !status || !p->pos_ref || !p->pos_hi ||
        !p->pos_lo || (p->ref_fx != nullptr ? !p->pos_fx : (!p->ref_hi || !p->ref_lo)) || list->stride < p->n ||
-       p->n >= (1 << PG_NBR_INDEX_BITS) || list->half) {
+       p->n >= (1 << PG_NBR_INDEX_BITS) || (list->half != 0) != (e->half != 0)) {
         return PG_ERR_ARGUMENT;
     }
     EnsArgs a = {};
@@ -513,7 +529,8 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
                    pg_workspace ws, cudaStream_t st) {
     const bool fixed = p->pos_fx != nullptr;
     if(!ens_ok(e, p) || !list || !list->nbr || !list->count || !lj || (!fixed && (!p->pos_hi || !p->pos_lo)) ||
-       !p->force32 || lj->ntypes < 1 || lj->ntypes > 8 || (lj->ntypes > 1 && !p->type)) {
+       !p->force32 || lj->ntypes < 1 || lj->ntypes > 8 || (lj->ntypes > 1 && !p->type) ||
+       (list->half != 0) != (e->half != 0)) {
         return PG_ERR_ARGUMENT;
     }
     EnsArgs a = {};

@@ -132,12 +132,6 @@ __global__ void __launch_bounds__(kBlock) k_lj_fp64(ForceArgs a) {
 
 // ---------------------------------------------------------------------------- MIXED
 
-__device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float c) {
-    // one vector reduction to L2 instead of three scalar atomics (sm_90+)
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
-                 :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(0.0f) : "memory");
-}
-
 // kFixed: positions from pos_fx (fixed point, 2^32 units per box length).  The wrapped
 // 32-bit difference of two coordinates is the pair's minimum-image separation, which
 // is the listed image's as long as the pair stays closer than half a box length (the

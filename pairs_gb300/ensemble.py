@@ -28,7 +28,7 @@ INT32_MAX = 2 ** 31 - 1
 class Ensemble:
     def __init__(self, replicas, *, cutoff=2.5, skin=0.3, dt=0.005, epsilon=1.0, sigma6=1.0, tpa=1, block=256,
                  reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, fixed_point=None,
-                 device="cuda"):
+                 half=False, device="cuda"):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -116,7 +116,13 @@ class Ensemble:
         self.e.replica_of = t["replica_of"].data_ptr()
         self.list = A.PgNeighborList()
         self.list.stride = n
-        self.list.half = 0
+        # half lists (each interior pair once, the reaction by a vector atomic) halve the
+        # build's candidates and list bytes, but with the 125-cell stencil the per-cell loop
+        # dominates the build (4.73 -> 4.40 ms at 512 replicas, no gain per step) and the
+        # atomics make the summation order nondeterministic: full lists by default
+        self.half = bool(half)
+        self.list.half = int(self.half)
+        self.e.half = int(self.half)
         # a liquid at rho <= 0.9 has about 4/3 pi 2.8^3 rho ~ 83 partners within r_list
         self._max_nb = int(neighbor_capacity or 112)
         self.configure(tpa, block, reach)

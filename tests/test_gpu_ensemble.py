@@ -35,16 +35,34 @@ def rms_rel(a, b):
     return np.abs(a - b).max() / max(np.sqrt(np.mean(b * b)), 1.0)
 
 
-@pytest.mark.parametrize("tpa,reach", [(1, 1), (4, 1), (2, 2), (8, 2)])
-def test_lists_and_forces_match_oracle(tpa, reach):
+def unordered(p):
+    """Canonical unordered pair set: (min uid, max uid, image of the larger seen from the smaller)."""
+    p = np.asarray(p)
+    sw = p[:, 0] > p[:, 1]
+    a = np.where(sw, p[:, 1], p[:, 0])
+    b = np.where(sw, p[:, 0], p[:, 1])
+    s = np.where(sw[:, None], -p[:, 2:], p[:, 2:])
+    return np.unique(np.concatenate([a[:, None], b[:, None], s], axis=1), axis=0)
+
+
+@pytest.mark.parametrize("tpa,reach,half", [(1, 1, False), (4, 1, False), (2, 2, False), (8, 2, False),
+                                            (1, 1, True), (2, 2, True), (4, 2, True)])
+def test_lists_and_forces_match_oracle(tpa, reach, half):
     from pairs_gb300.ensemble import Ensemble
     reps = replicas()
-    ens = Ensemble(reps, tpa=tpa, reach=reach, policy="every")
+    ens = Ensemble(reps, tpa=tpa, reach=reach, policy="every", half=half)
     ens.synchronize()
     for r, st in enumerate(reps):
         sim = olj.Sim(st, every=1, exact_sync=True)
         sim.step()
-        assert np.array_equal(canonical_pairs(ens.replica_pairs(r)), canonical_pairs(sim.pairs())), r
+        got, ref = ens.replica_pairs(r), sim.pairs()
+        if half:
+            # each interior pair once, pairs through an image from both sides
+            assert np.array_equal(unordered(got), unordered(ref)), r
+            image = np.any(np.asarray(got)[:, 2:] != 0, axis=1)
+            assert len(unordered(got)) == (~image).sum() + image.sum() // 2, r
+        else:
+            assert np.array_equal(canonical_pairs(got), canonical_pairs(ref)), r
         _, _, f_ref = sim.state()
         _, _, f = ens.replica_state(r)
         assert rms_rel(f, f_ref) < 1e-5, (r, rms_rel(f, f_ref))
@@ -55,7 +73,7 @@ def test_replica_follows_single_system_engine():
     from pairs_gb300.ensemble import Ensemble
     reps = replicas()
     # the engine's 27-cell stencil and its compensated hi/lo positions
-    ens = Ensemble(reps, tpa=1, reach=1, policy="every", fixed_point=False)
+    ens = Ensemble(reps, tpa=1, reach=1, policy="every", fixed_point=False, half=False)
     ens.run(25)
     ens.synchronize()
     worst = 0.0
@@ -105,12 +123,14 @@ def test_graph_chunks_equal_plain_chunks():
         assert np.array_equal(pa, pb) and np.array_equal(va, vb)
 
 
-def test_guard_schedule_keeps_the_pair_set():
+@pytest.mark.parametrize("half", [False, True])
+def test_guard_schedule_keeps_the_pair_set(half):
     """Speculative chunks: after a run, the list rebuilt from the final positions
-    holds every pair within the cutoff that the guarded list held."""
+    holds every pair within the cutoff that the guarded list held (half lists: the
+    integration pass zeroes the force that the next force pass accumulates into)."""
     from pairs_gb300.ensemble import Ensemble
     reps = replicas()
-    ens = Ensemble(reps, tpa=4)
+    ens = Ensemble(reps, tpa=4, half=half)
     ens.run(80)
     ens.synchronize()
     assert ens.nbuilds >= 2
