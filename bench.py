@@ -99,15 +99,16 @@ def dist_setup():
     return init_from_env(os.environ)
 
 
-def traffic_from_profiles(kernel):
-    """DRAM bytes per launch of `kernel` from a committed ncu summary, or None."""
+def traffic_from_profiles(kernel, variant):
+    """DRAM bytes per launch of `kernel` in `variant` from a committed ncu summary
+    (profiles/traffic.txt lines: kernel variant bytes), or None."""
     path = os.path.join(ROOT, "profiles", "traffic.txt")
     try:
         with open(path) as f:
             for line in f:
                 parts = line.split()
-                if len(parts) >= 2 and parts[0] == kernel:
-                    return float(parts[1])
+                if len(parts) >= 3 and parts[0] == kernel and parts[1] == variant:
+                    return float(parts[2])
     except OSError:
         pass
     return None
@@ -226,7 +227,7 @@ def run_ours(args, rank, world, dist):
     achieved = b_force / (f_avg / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_kind": pk_kind,
-                "traffic": traffic_from_profiles(kname), "kernel": "%s (%s)" % (kname, args.variant),
+                "traffic": traffic_from_profiles(kname, args.variant), "kernel": "%s (%s)" % (kname, args.variant),
                 "kernel_ms": round(f_avg, 4), "algorithmic_bytes": b_force, "list_entries": pairs_total}
     schedule = dict(counters, policy=args.policy, calibration_steps=calib_steps,
                     calibration_s=round(calib_s, 3),

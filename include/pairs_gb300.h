@@ -29,7 +29,7 @@
  *                      hi differences and periodic shifts are exact in FP32, lo the
  *                      FP32 residual x - hi
  *   int4    pos_fx[n]  fixed-point positions (precision PG_MIXED, periodic boxes of
- *                      at least 4 cells per axis): 2^32 units per box length, so
+ *                      at least 2 reach + 2 cells per axis): 2^32 units per box length, so
  *                      periodic images need no shift; replaces pos_hi/pos_lo there
  *   int     nbr[k * stride + i]    Verlet entry k of particle i (column-major, as
  *                      the reference's GPU layout, sim/neighbor_lists.py:14); bits
@@ -112,8 +112,8 @@ typedef struct {
                                     type.  A box length is 2^32 units, so the wrapped 32-bit
                                     difference of two coordinates is their minimum-image
                                     separation; used instead of pos_hi/pos_lo when every
-                                    axis is periodic and has at least 4 cells (6 with
-                                    reach 2) */
+                                    axis is periodic and has at least 2 reach + 2 cells
+                                    (the axis's stencil reach) */
     int32_t *ref_fx;             /* int4[capacity] pos_fx at last rebuild (guard screen) */
     double *mass;                /* [capacity] */
     int32_t *type;               /* [capacity] */
@@ -136,8 +136,10 @@ typedef struct {
     int32_t ncells;
     int32_t reach;               /* Verlet build stencil: cells within `reach` per axis (27 cells
                                     for 1, 125 for 2); 0 is taken as 1 */
-    int32_t pad_;
-    double  cell_len[3];         /* len[d] / dims[d] >= list radius / reach */
+    int32_t reach_x;             /* stencil reach along x alone (1 or 2; 0: `reach`).  With
+                                    reach 1 and reach_x 2 the cells are half as wide in x and
+                                    the stencil has 5 x 3 x 3 cells */
+    double  cell_len[3];         /* len[d] / dims[d] >= list radius / reach of axis d */
     int32_t *cell_start;         /* [ncells + 2]: cells, then the bucket of infinite shapes */
     int32_t *cell_count;         /* [ncells + 1] */
     int32_t *particle_cell;      /* [capacity] */
@@ -155,7 +157,10 @@ typedef struct {
 typedef struct {
     int32_t stride;              /* >= capacity of particles */
     int32_t max_neighbors;       /* entries per particle */
-    int32_t half;                /* 1: interior pairs once (Newton's third law) */
+    int32_t half;                /* 1: interior pairs once (Newton's third law), stored by
+                                    the particle whose partner lies above it in x (ties: y,
+                                    z, then the higher index); pairs through a periodic image
+                                    in both lists */
     int32_t *nbr;                /* [max_neighbors * stride] or NULL */
     int32_t *count;              /* [stride] */
     int32_t steps_since_build;   /* host-maintained, for PG_SYNC_REFERENCE */
@@ -338,7 +343,7 @@ int pg_bin_particles_noalloc(const pg_box *box, pg_particles *p, pg_cells *cells
  * fl(x_j + s*len), delta, (dx*dx + dy*dy) + dz*dz, no fused multiply-add.  Also
  * records pos_ref (and ref_hi/ref_lo or ref_fx) for the displacement guard.  The FP32
  * screen reads pos_fx when it is set and the box allows it (every axis periodic with
- * at least 4 cells, 6 with reach 2), else pos_hi/pos_lo. */
+ * at least 2 reach + 2 cells), else pos_hi/pos_lo. */
 int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                             pg_neighbor_list *list, double r_list2, pg_status *status,
                             void *stream);

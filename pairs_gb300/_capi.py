@@ -52,7 +52,7 @@ class PgParticles(C.Structure):
 
 
 class PgCells(C.Structure):
-    _fields_ = [("dims", C.c_int32 * 3), ("ncells", C.c_int32), ("reach", C.c_int32), ("pad_", C.c_int32),
+    _fields_ = [("dims", C.c_int32 * 3), ("ncells", C.c_int32), ("reach", C.c_int32), ("reach_x", C.c_int32),
                 ("cell_len", C.c_double * 3),
                 ("cell_start", C.c_void_p), ("cell_count", C.c_void_p),
                 ("particle_cell", C.c_void_p)]

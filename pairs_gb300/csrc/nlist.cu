@@ -18,6 +18,13 @@
 // Half lists follow the reference's compute_half() semantics: a pair inside the box
 // is stored once (Newton's third law applies the reaction); a pair through a periodic
 // image is stored in both particles' lists and each side computes its own force.
+// Which side stores an interior pair is free (the reference's choice, i < j in its
+// own order, is not observable after the particles are re-sorted).  Here the particle
+// whose partner lies above it in x stores the pair (ties: y, then z, then the higher
+// index), so that every particle keeps the pairs of one half of its neighbourhood
+// sphere.  Counts then vary only with the local density: assigning the pairs by cell
+// order instead made a particle's count depend on its place in its cell, and the
+// warps of the force pass ran at the pace of their longest list.
 #include "common.cuh"
 
 namespace pg {
@@ -42,11 +49,24 @@ __device__ __forceinline__ float comp_delta(float hi_i, float lo_i, float hi_j, 
     return __fadd_rn(dh, dl);
 }
 
+// The partner of a half-list pair in the particle's own x slab of the stencil is
+// kept when it lies above: (x, y, z) of the partner greater in that order, the index
+// breaking exact ties.  d = x_i - x_j from the screen is exactly antisymmetric between
+// the two sides of a pair (an integer difference in fixed point; in the compensated
+// layout the hi difference is exact and round-to-nearest is symmetric in sign), so
+// exactly one side keeps the pair.
+__device__ __forceinline__ bool partner_above(float dx, float dy, float dz, int i, int j) {
+    if(dx != 0.0f) { return dx < 0.0f; }
+    if(dy != 0.0f) { return dy < 0.0f; }
+    if(dz != 0.0f) { return dz < 0.0f; }
+    return j > i;
+}
+
 // kFixed: the FP32 screen takes the wrapped difference of fixed-point positions.  It
 // is the separation from the stencil's image of the partner whenever that separation
 // is below half a box length, which holds for every candidate when each axis is
-// periodic and has at least 4 cells (6 with reach 2): particle and image then lie in
-// cells at most 2 (3) cells apart.
+// periodic and has at least 2 reach + 2 cells: particle and image then lie in cells at
+// most reach cells apart, less than reach + 1 cell lengths.
 template<bool kFixed>
 __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -76,9 +96,10 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
         int32_t *out = a.list.nbr + i;
         int32_t *wp = out;
         const int rr = a.cells.reach > 1 ? a.cells.reach : 1;
+        const int rx = a.cells.reach_x > 0 ? a.cells.reach_x : rr;
         // offsets past one box length are skipped: a box longer than 2 r_list holds no
         // partner there, and each (cell, image) pair is then visited once
-        for(int ox = -rr; ox <= rr; ox++) {
+        for(int ox = -rx; ox <= rx; ox++) {
             if(ox < -dx_ || ox > dx_) { continue; }
             int nx = cx + ox, sx = 0;
             if(nx < 0) { if(!a.box.periodic[0]) { continue; } nx += dx_; sx = -1; }
@@ -97,18 +118,14 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
                     const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
                     // half list: an interior pair once, a pair through a periodic image
                     // from both sides, as the reference's ghosts always pass its i < j
-                    // test (sim/interaction.py:107-113).  Which side stores an interior
-                    // pair is free: the particle of the higher cell stores none (in
-                    // sorted order a lower cell holds only j < i, so it is skipped
-                    // whole), and within a cell the index parity splits the pairs
-                    // evenly, (j > i) xor odd(i + j), so that counts do not depend on a
-                    // particle's place in its cell.
-                    if(a.list.half && code == 0u && c < ci) { continue; }
-                    const bool own = a.list.half && code == 0u && c == ci;
+                    // test (sim/interaction.py:107-113).  An interior partner in a lower
+                    // x slab lies below (binning is monotone in x), one in a higher slab
+                    // above; in the own slab the partner's place decides.
+                    if(a.list.half && code == 0u && ox < 0) { continue; }
+                    const bool slab = a.list.half && code == 0u && ox == 0;
                     const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
                     for(int j = b; j < e; j++) {
                         if(j == i) { continue; }
-                        if(own && ((j > i) == (((i ^ j) & 1) != 0))) { continue; }
                         float fx, fy, fz;
                         if(kFixed) {
                             const int4 fj = ld_i4(a.p.pos_fx, j);
@@ -121,6 +138,7 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
                             fy = comp_delta(hi.y, lo.y, hj.y, lj.y, sy, a.box.len_hi[1], a.box.len_lo[1]);
                             fz = comp_delta(hi.z, lo.z, hj.z, lj.z, sz, a.box.len_hi[2], a.box.len_lo[2]);
                         }
+                        if(slab && !partner_above(fx, fy, fz, i, j)) { continue; }
                         const float r2f = fx * fx + fy * fy + fz * fz;
                         bool keep;
                         if(r2f < a.r2_lo) { keep = true; }
@@ -149,12 +167,17 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
     }
 }
 
+static int axis_reach(const pg_cells *cells, int d) {
+    const int rr = cells->reach > 1 ? cells->reach : 1;
+    return d == 0 && cells->reach_x > 0 ? cells->reach_x : rr;
+}
+
 // the fixed-point screen is exact for every candidate (see k_build_list)
 static bool fixed_point_screen(const pg_box *box, const pg_particles *p, const pg_cells *cells) {
     if(p->pos_fx == nullptr || p->ref_fx == nullptr) { return false; }
-    const int rr = cells->reach > 1 ? cells->reach : 1;
     for(int d = 0; d < 3; d++) {
-        if(!box->periodic[d] || cells->dims[d] < (rr == 1 ? 4 : 6)) { return false; }
+        // a candidate lies within reach + 1 cells of the particle: below half a box
+        if(!box->periodic[d] || cells->dims[d] < 2 * axis_reach(cells, d) + 2) { return false; }
     }
     return true;
 }
@@ -171,13 +194,13 @@ int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cell
         return PG_ERR_ARGUMENT;
     }
     if(list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS)) { return PG_ERR_ARGUMENT; }
-    const int rr = cells->reach > 1 ? cells->reach : 1;
-    if(rr > 2) { return PG_ERR_ARGUMENT; }
+    if(cells->reach > 2 || cells->reach_x < 0 || cells->reach_x > 2) { return PG_ERR_ARGUMENT; }
     for(int d = 0; d < 3; d++) {
+        const int rr = axis_reach(cells, d);
         // a stencil of `reach` cells each side covers r_list only if reach * cell >= r_list
         const double span = cells->cell_len[d] * rr;
         if(span * span < r_list2) { return PG_ERR_ARGUMENT; }
-        // the periodic box must exceed r_list (2 r_list for the 125-cell stencil, whose
+        // the periodic box must exceed r_list (2 r_list along an axis of reach 2, whose
         // offsets would otherwise reach the same image twice)
         if(box->periodic[d] && box->len[d] * box->len[d] <= (rr == 1 ? 1.0 : 4.0) * r_list2) { return PG_ERR_ARGUMENT; }
     }

@@ -52,7 +52,7 @@ class LJEngine:
                  dt=0.005, ntypes=1, epsilon=None, sigma6=None, precision="fp64", half=False,
                  sync="exact", every=20, neighbor_capacity=100, policy="fixed", device="cuda",
                  capacity=None, fused=True, tiles=None, tile_tpa=2, tile_atoms=224, cell_reach=1,
-                 fixed_point=None):
+                 cell_reach_x=None, fixed_point=None):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -149,11 +149,24 @@ class LJEngine:
         if reach not in (1, 2) or (reach == 2 and (tiles or any(periodic[d] and self.box.len[d] <= 2 * self.r_list
                                                                  for d in range(3)))):
             raise ValueError("cell_reach 2 needs global lists and periodic boxes longer than 2 (cutoff + skin)")
+        # half lists: cells half as wide in x (reach 2 along x, 5 x 3 x 3 cells) by
+        # default where the box allows it.  A half list keeps the partners above a
+        # particle in x; with narrower x slabs the build scans 13.5 cell volumes per
+        # particle instead of 18.
+        long_x = not periodic[0] or self.box.len[0] > 2 * self.r_list
+        if cell_reach_x is None:
+            reach_x = 2 if half and not tiles and reach == 1 and long_x else reach
+        else:
+            reach_x = int(cell_reach_x)
+            if reach_x not in (1, 2) or (reach_x == 2 and (tiles or not long_x)):
+                raise ValueError("cell_reach_x 2 needs global lists and a box longer than 2 (cutoff + skin) in x")
         self.cells.reach = reach
+        self.cells.reach_x = reach_x
+        self.reach_axes = (reach_x, reach, reach)
         ncells = 1
         for d in range(3):
             L = self.box.len[d]
-            dims = max(1, int(math.floor(L * reach / self.r_list)))
+            dims = max(1, int(math.floor(L * self.reach_axes[d] / self.r_list)))
             self.cells.dims[d] = dims
             self.cells.cell_len[d] = L / dims
             ncells *= dims
@@ -161,13 +174,14 @@ class LJEngine:
 
         # ---- FP32 position layout (the mixed path's forces, the list build's screen).
         # Fixed point (one int4 per particle, periodic images without shifts) where
-        # the box allows it: every axis periodic with at least 4 cells (6 with reach
-        # 2); compensated hi/lo float4 pairs otherwise, and for tile lists.
+        # the box allows it: every axis periodic with at least 2 reach + 2 cells (a
+        # candidate then lies less than half a box away); compensated hi/lo float4
+        # pairs otherwise, and for tile lists.
         fx_ok = (not tiles and all(periodic) and
-                 all(self.cells.dims[d] >= (4 if reach == 1 else 6) for d in range(3)))
+                 all(self.cells.dims[d] >= 2 * self.reach_axes[d] + 2 for d in range(3)))
         if fixed_point and not fx_ok:
             raise ValueError("fixed-point positions need global lists and a periodic box "
-                             "of at least 4 cells per axis (6 with cell_reach 2)")
+                             "of at least 2 reach + 2 cells per axis")
         self.fixed_point = fx_ok if fixed_point is None else bool(fixed_point)
         if self.fixed_point:
             t["pos_fx"] = z((cap, 4), i32)

@@ -253,3 +253,23 @@ def test_fixed_point_layout_needs_a_large_periodic_box():
     big = lattice.copper_fcc_lattice(8, 8, 8)             # 4 cells per axis
     assert LJEngine(big, precision="mixed").fixed_point
     assert not LJEngine(big, precision="mixed", periodic=(True, True, False)).fixed_point
+
+
+def test_half_list_counts_are_balanced_within_warps():
+    """A half list keeps the partners above each particle in x, so counts vary only
+    with the local density: on a liquid (fcc 16^3 after 40 steps) a warp's 32
+    consecutive particles have lists of nearly one length (mean over max above 0.75;
+    splitting the pairs by cell order gave about 0.6), and the half list holds half
+    the full list's interior pairs plus its image pairs."""
+    from pairs_gb300.engine import LJEngine
+    st = lattice.copper_fcc_lattice(16, 16, 16)
+    e = LJEngine(st, precision="mixed", half=True, policy="guard")
+    e.run(40)
+    e.settle()
+    e.rebuild()
+    cnt = e.t["count"][: e.n].cpu().numpy().astype(np.int64)
+    w = cnt[: len(cnt) // 32 * 32].reshape(-1, 32)
+    assert w.sum() / (32 * w.max(axis=1)).sum() > 0.75
+    full = LJEngine(dict(st, pos=e.state()[0], vel=e.state()[1]), precision="mixed", half=False)
+    full.rebuild()
+    assert np.array_equal(unordered(e.pairs()), unordered(full.pairs()))
