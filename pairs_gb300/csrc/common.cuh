@@ -203,6 +203,19 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// The partner of a half-list pair in the particle's own x slab of the stencil is
+// kept when it lies above: (x, y, z) of the partner greater in that order, the index
+// breaking exact ties.  d = x_i - x_j from the screen is exactly antisymmetric between
+// the two sides of a pair (an integer difference in fixed point; in the compensated
+// layout the hi difference is exact and round-to-nearest is symmetric in sign), so
+// exactly one side keeps the pair.
+__device__ __forceinline__ bool partner_above(float dx, float dy, float dz, int i, int j) {
+    if(dx != 0.0f) { return dx < 0.0f; }
+    if(dy != 0.0f) { return dy < 0.0f; }
+    if(dz != 0.0f) { return dz < 0.0f; }
+    return j > i;
+}
+
 __device__ __forceinline__ int warp_max(int v) {
     for(int o = 16; o > 0; o >>= 1) { v = max(v, __shfl_xor_sync(0xffffffffu, v, o)); }
     return v;

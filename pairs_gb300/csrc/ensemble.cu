@@ -170,14 +170,14 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
                     const int c = R.cell0 + (nx * dy_ + ny) * dz_ + nz;
                     const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
                     // half lists as the single-system build (nlist.cu): an interior pair
-                    // once, stored by the lower cell's particle, by index parity within a
-                    // cell; a pair through an image from both sides
-                    if(a.list.half && code == 0u && c < a.cells.particle_cell[i]) { continue; }
-                    const bool own = a.list.half && code == 0u && c == a.cells.particle_cell[i];
+                    // once, stored by the particle whose partner lies above it in x (cells
+                    // of lower x skipped, the own x slab tested per candidate); a pair
+                    // through an image from both sides
+                    if(a.list.half && code == 0u && ox < 0) { continue; }
+                    const bool slab = a.list.half && code == 0u && ox == 0;
                     const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
                     for(int j = b; j < e; j++) {
                         if(j == i && code == 0u) { continue; }
-                        if(own && ((j > i) == (((i ^ j) & 1) != 0))) { continue; }
                         float fx, fy, fz;
                         if(fxs) {
                             const int4 fj = ld_i4(a.p.pos_fx, j);
@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
                             fy = ens_delta(hi.y, lo.y, hj.y, lj.y, sy, R.len_hi[1], R.len_lo[1]);
                             fz = ens_delta(hi.z, lo.z, hj.z, lj.z, sz, R.len_hi[2], R.len_lo[2]);
                         }
+                        if(slab && !partner_above(fx, fy, fz, i, j)) { continue; }
                         const float r2f = fx * fx + fy * fy + fz * fz;
                         bool keep;
                         if(r2f < a.r2_lo) { keep = true; }

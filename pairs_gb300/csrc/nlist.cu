@@ -49,19 +49,6 @@ __device__ __forceinline__ float comp_delta(float hi_i, float lo_i, float hi_j, 
     return __fadd_rn(dh, dl);
 }
 
-// The partner of a half-list pair in the particle's own x slab of the stencil is
-// kept when it lies above: (x, y, z) of the partner greater in that order, the index
-// breaking exact ties.  d = x_i - x_j from the screen is exactly antisymmetric between
-// the two sides of a pair (an integer difference in fixed point; in the compensated
-// layout the hi difference is exact and round-to-nearest is symmetric in sign), so
-// exactly one side keeps the pair.
-__device__ __forceinline__ bool partner_above(float dx, float dy, float dz, int i, int j) {
-    if(dx != 0.0f) { return dx < 0.0f; }
-    if(dy != 0.0f) { return dy < 0.0f; }
-    if(dz != 0.0f) { return dz < 0.0f; }
-    return j > i;
-}
-
 // kFixed: the FP32 screen takes the wrapped difference of fixed-point positions.  It
 // is the separation from the stencil's image of the partner whenever that separation
 // is below half a box length, which holds for every candidate when each axis is

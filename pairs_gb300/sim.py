@@ -44,7 +44,8 @@ class Simulation:
         self.neighbor_capacity = neighbor_capacity
         self.debug = debug
         # GB300 knobs: FP64 everywhere for double_prec=True (the reference's meaning),
-        # else the mixed path (FP32 force on compensated positions, FP64 integration).
+        # else the mixed path (FP32 force on fixed-point or compensated positions, FP64
+        # integration).
         self.precision = precision or ("fp64" if double_prec else "mixed")
         self.ghost_sync = ghost_sync if self.precision == "fp64" else "exact"
         self.rebuild_policy = rebuild_policy
