@@ -99,19 +99,22 @@ def dist_setup():
     return init_from_env(os.environ)
 
 
-def traffic_from_profiles(kernel, variant):
+def traffic_from_profiles(kernel, variant, atoms):
     """DRAM bytes per launch of `kernel` in `variant` from a committed ncu summary
-    (profiles/traffic.txt lines: kernel variant bytes), or None."""
+    (profiles/traffic.txt lines: kernel variant atoms bytes), scaled to `atoms` by the
+    atom count of the capture (the force pass's traffic grows in proportion: list
+    entries and records per atom are fixed by the density), or (None, None)."""
     path = os.path.join(ROOT, "profiles", "traffic.txt")
     try:
         with open(path) as f:
             for line in f:
                 parts = line.split()
-                if len(parts) >= 3 and parts[0] == kernel and parts[1] == variant:
-                    return float(parts[2])
+                if len(parts) >= 4 and parts[0] == kernel and parts[1] == variant:
+                    ref_atoms, ref_bytes = int(parts[2]), float(parts[3])
+                    return ref_bytes * atoms / ref_atoms, ref_atoms
     except OSError:
         pass
-    return None
+    return None, None
 
 
 # ------------------------------------------------------------------------------ our arm
@@ -225,10 +228,13 @@ def run_ours(args, rank, world, dist):
     f_avg = statistics.mean(fms) if fms else float("nan")
     pk, pk_kind = peaks()
     achieved = b_force / (f_avg / 1e3) / 1e9
+    traffic, traffic_atoms = traffic_from_profiles(kname, args.variant, n)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_kind": pk_kind,
-                "traffic": traffic_from_profiles(kname, args.variant), "kernel": "%s (%s)" % (kname, args.variant),
+                "traffic": traffic, "kernel": "%s (%s)" % (kname, args.variant),
                 "kernel_ms": round(f_avg, 4), "algorithmic_bytes": b_force, "list_entries": pairs_total}
+    if traffic is not None and traffic_atoms != n:
+        roofline["traffic_scaled_from_atoms"] = traffic_atoms
     schedule = dict(counters, policy=args.policy, calibration_steps=calib_steps,
                     calibration_s=round(calib_s, 3),
                     mean_cycle=round(args.steps / max(1, counters["rebuilds"]), 2))

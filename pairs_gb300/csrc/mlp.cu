@@ -28,9 +28,10 @@ constexpr int kFeat = 4;   // f0, f1, f2, valid
 
 // ---------------------------------------------------------------- features
 
-// one warp per cell (8 lanes per cell measured slower: 34.5 vs 31 us at 1M atoms)
-constexpr int kCellLanes = 32;
-
+// kCellLanes lanes per cell, chosen by the host from the mean occupancy: a warp per
+// cell of ~19 particles (8 lanes measured slower there: 34.5 vs 31 us at 1M atoms),
+// half a warp for cells of ~10 (55 us with a warp per cell at 1M atoms in 110k cells)
+template<int kCellLanes>
 __global__ void k_cell_features(pg_particles p, pg_cells cells, int precision, float since, float dt,
                                 float inv_half_skin, float *feat) {
     const int cell = (blockIdx.x * blockDim.x + threadIdx.x) / kCellLanes;
@@ -339,9 +340,14 @@ int cell_features(const pg_particles *p, const pg_cells *cells, int precision, i
     if(!p || !cells || !feat || !p->vel || !p->mass) { return PG_ERR_ARGUMENT; }
     if(precision == PG_MIXED ? !p->force32 : !p->force) { return PG_ERR_ARGUMENT; }
     const int threads = 256;
-    const int blocks = (int) (((int64_t) cells->ncells * kCellLanes + threads - 1) / threads);
-    k_cell_features<<<blocks, threads, 0, st>>>(*p, *cells, precision, (float) since, (float) dt,
-                                                 (float) (1.0 / half_skin), feat); note_launch();
+    const double mean = cells->ncells > 0 ? (double) p->n / cells->ncells : 0.0;
+    const int lanes = mean <= 6.0 ? 8 : (mean <= 14.0 ? 16 : 32);
+    const int blocks = (int) (((int64_t) cells->ncells * lanes + threads - 1) / threads);
+    const float ts = (float) since, fdt = (float) dt, ihs = (float) (1.0 / half_skin);
+    if(lanes == 8) { k_cell_features<8><<<blocks, threads, 0, st>>>(*p, *cells, precision, ts, fdt, ihs, feat); }
+    else if(lanes == 16) { k_cell_features<16><<<blocks, threads, 0, st>>>(*p, *cells, precision, ts, fdt, ihs, feat); }
+    else { k_cell_features<32><<<blocks, threads, 0, st>>>(*p, *cells, precision, ts, fdt, ihs, feat); }
+    note_launch();
     return launch_status();
 }
 

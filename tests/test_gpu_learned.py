@@ -123,3 +123,38 @@ def test_learned_schedule_gain_over_guard_every_step():
     assert l["syncs"] * 3 < g["syncs"], runs
     # rebuilds: never many more than the exact-on-trip count
     assert l["builds"] <= 1.6 * g["builds"], runs
+
+
+@pytest.mark.parametrize("half", [True, False])
+def test_cell_features_match_a_host_computation(half):
+    """pg_cell_features against numpy on the engine's own cells: per cell max|v| dt /
+    (skin/2), mean |F|/m dt^2 / (skin/2), steps since build / 20 and occupancy, for
+    cells of ~10 particles (half lists: half-width x cells) and of ~19 (full lists)."""
+    from pairs_gb300.engine import LJEngine
+    st = lattice.copper_fcc_lattice(16, 16, 16)
+    e = LJEngine(st, precision="mixed", half=half, policy="guard")
+    e.run(30)
+    e.settle()
+    nc = e.cells.ncells
+    feat = torch.zeros((nc, 4), dtype=torch.float32, device="cuda")
+    A.call("pg_cell_features", C.byref(e.p), C.byref(e.cells), e.precision, 7, e.dt, 0.5 * e.skin,
+           C.c_void_p(feat.data_ptr()), e.sh)
+    torch.cuda.synchronize()
+    got = feat.cpu().numpy()
+    start = e.t["cell_start"][:nc].cpu().numpy()
+    count = e.t["cell_count"][:nc].cpu().numpy()
+    vel = e.t["vel"][: e.n, :3].cpu().numpy()
+    frc = e.t["force32"][: e.n, :3].cpu().numpy().astype(np.float64)
+    mass = e.t["mass"][: e.n].cpu().numpy()
+    hs = 0.5 * e.skin
+    vmag = np.sqrt((vel ** 2).sum(axis=1))
+    acc = np.sqrt((frc ** 2).sum(axis=1)) / mass
+    want = np.zeros_like(got)
+    for c in range(nc):
+        b, k = start[c], count[c]
+        if k:
+            want[c] = (vmag[b:b + k].max() * e.dt / hs, acc[b:b + k].mean() * e.dt ** 2 / hs, 7 / 20, 1.0)
+        else:
+            want[c] = (0.0, 0.0, 7 / 20, 0.0)
+    assert (count > 0).mean() > 0.9
+    assert np.allclose(got, want, rtol=2e-6, atol=1e-9)
