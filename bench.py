@@ -310,6 +310,24 @@ def run_ours(args, rank, world, dist):
         drift64 = drift(e64, args.drift_steps)
         del e64
 
+    # rebuild schedules on the same path and workload (mixed, same list kind): the
+    # learned schedule against the reference's fixed every-20 schedule with the exact
+    # guard on (a trip forces the rebuild; the host reads the guard after every step),
+    # the guard alone, and a fixed interval of 7 steps judged by the guard
+    schedules = {}
+    if prec == "mixed":
+        ks = max(100, min(args.steps, 800))
+        for pol in (args.policy, "fixed+guard", "guard", "interval:7"):
+            if pol in schedules:
+                continue
+            es = make(prec, half, pol)
+            cs, _ = calibrate(es)
+            mss, _, _, cnt = timed(es, ks, max(args.warmup, 100 - cs), force_events=False)
+            schedules[pol] = {"ms_per_step": round(mss / ks, 4), "value": n * ks / (mss / 1e3), "steps": ks,
+                              "rebuilds": cnt["rebuilds"], "host_syncs": cnt["host_syncs"],
+                              "rewinds": cnt["rewinds"]}
+            del es
+
     # end to end through the public engine API from pinned host state
     chunk = min(100, args.steps)
     nchunks = max(1, args.steps // chunk)
@@ -360,6 +378,7 @@ def run_ours(args, rank, world, dist):
         "energy_drift_1000": {"headline": drift_headline, "fp64_guard": drift64, "steps": args.drift_steps},
         "force_error_vs_fp64": ferr,
         "fp64": {"best_value": best64, **fp64, "speedup_headline_vs_fp64": value / world / best64},
+        "schedules": schedules,
         "e2e": e2e, "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
     }
     if rank == 0:
