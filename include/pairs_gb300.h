@@ -519,8 +519,10 @@ int pg_dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *c
 
 /* Explicit Euler with rotation (examples/dem.py:77-87), skipping fixed particles,
  * plus the FP64 displacement guard against pos_ref (first step with a displacement
- * above sqrt(half_skin2) kept in status->guard_tripped). */
-int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step,
+ * above sqrt(half_skin2) kept in status->guard_tripped).  precision PG_FP64: the
+ * generated operation order; PG_MIXED: the same FP64 update with fused
+ * multiply-adds. */
+int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, int precision, double half_skin2, int32_t step,
                  pg_status *status, void *stream);
 
 /* cudaStreamSynchronize, returning PG_OK or PG_ERR_CUDA. */

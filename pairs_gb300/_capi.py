@@ -167,7 +167,7 @@ SIGNATURES = {
                                     C.c_void_p, C.c_void_p]),
     "pg_dem_force": (C.c_int, [P(PgBox), P(PgDemParticles), P(PgCells), P(PgNeighborList), P(PgContacts),
                                P(PgDemParams), C.c_int, C.c_void_p, C.c_void_p]),
-    "pg_dem_euler": (C.c_int, [P(PgDemParticles), P(PgDemParams), C.c_double, C.c_int32, C.c_void_p,
+    "pg_dem_euler": (C.c_int, [P(PgDemParticles), P(PgDemParams), C.c_int, C.c_double, C.c_int32, C.c_void_p,
                                C.c_void_p]),
 }
 

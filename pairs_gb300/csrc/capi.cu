@@ -49,7 +49,7 @@ int dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *cells
                    const pg_dem_params *prm, pg_status *status, cudaStream_t st);
 int dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cells, const pg_neighbor_list *list,
               const pg_contacts *c, const pg_dem_params *prm, int precision, pg_status *status, cudaStream_t st);
-int dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step, pg_status *status,
+int dem_euler(pg_dem_particles *d, const pg_dem_params *prm, int precision, double half_skin2, int32_t step, pg_status *status,
               cudaStream_t st);
 }  // namespace pg
 
@@ -184,9 +184,9 @@ int pg_dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *c
     return pg::dem_force(box, d, cells, list, c, prm, precision, status, S(stream));
 }
 
-int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step,
+int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, int precision, double half_skin2, int32_t step,
                  pg_status *status, void *stream) {
-    return pg::dem_euler(d, prm, half_skin2, step, status, S(stream));
+    return pg::dem_euler(d, prm, precision, half_skin2, step, status, S(stream));
 }
 
 int pg_cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t steps_since_build,

@@ -496,6 +496,12 @@ __device__ __forceinline__ void quat_matrix(const double Q[4], double R[9]) {
     R[8] = (1.0 - 2.0 * Q[1] * Q[1]) - 2.0 * Q[2] * Q[2];
 }
 
+// +0 or -0, tested on the bit pattern (integer work: GB300's FP64 rate is low)
+__device__ __forceinline__ bool zero_bits(double v) { return (__double_as_longlong(v) << 1) == 0; }
+
+// kMixed: the mixed path's step, the same FP64 update with fused multiply-adds,
+// x + dt v + (dt^2 / 2m) F and v + (dt / m) F; otherwise the generated operation order.
+template<bool kMixed>
 __global__ void __launch_bounds__(kBlock) k_dem_euler(DemArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool tripped = false;
@@ -505,17 +511,30 @@ __global__ void __launch_bounds__(kBlock) k_dem_euler(DemArgs a) {
         const D4 F = ldd(a.d.force, i), T = ldd(a.d.torque, i), Qd = ldd(a.d.quat, i);
         const double Qo[4] = {Qd.x, Qd.y, Qd.z, Qd.w};
         const double im = V.w;                   // 1 / mass (pg_dem_setup)
-        const double h = 0.5 * im;
         const double f3[3] = {F.x, F.y, F.z}, t3[3] = {T.x, T.y, T.z};
         double x3[3] = {X.x, X.y, X.z}, v3[3] = {V.x, V.y, V.z}, w3[3] = {W.x, W.y, W.z};
-        for(int e = 0; e < 3; e++) { x3[e] = x3[e] + (((h * f3[e]) * dt) * dt + v3[e] * dt); }
-        for(int e = 0; e < 3; e++) { v3[e] = v3[e] + (im * f3[e]) * dt; }
+        if(kMixed) {
+            const double c = (0.5 * im) * (dt * dt), b = im * dt;
+            for(int e = 0; e < 3; e++) { x3[e] = fma(c, f3[e], fma(dt, v3[e], x3[e])); }
+            for(int e = 0; e < 3; e++) { v3[e] = fma(b, f3[e], v3[e]); }
+        } else {
+            const double h = 0.5 * im;
+            for(int e = 0; e < 3; e++) { x3[e] = x3[e] + (((h * f3[e]) * dt) * dt + v3[e] * dt); }
+            for(int e = 0; e < 3; e++) { v3[e] = v3[e] + (im * f3[e]) * dt; }
+        }
         // No torque and no spin: the rotation yields phi = 0, the identity quaternion,
         // the product q Q = Q bit for bit and, when |Q|^2 is within 1e-8 of one, no
         // renormalisation -- orientation and angular velocity stay as they are, so the
-        // FP64 rotation arithmetic is skipped (most spheres of a settling packing).
-        const bool still = T.x == 0.0 && T.y == 0.0 && T.z == 0.0 && W.x == 0.0 && W.y == 0.0 && W.z == 0.0 &&
-                           fabs((((Qo[0] * Qo[0] + Qo[1] * Qo[1]) + Qo[2] * Qo[2]) + Qo[3] * Qo[3]) - 1.0) < 1e-08;
+        // FP64 rotation arithmetic is skipped (most spheres of a settling packing).  A
+        // sphere that never turned (torque and spin +-0, orientation exactly (1, 0, 0, 0),
+        // so |Q|^2 = 1) is recognised from the bit patterns alone.
+        const bool never_turned = zero_bits(T.x) && zero_bits(T.y) && zero_bits(T.z) && zero_bits(W.x) &&
+                                  zero_bits(W.y) && zero_bits(W.z) &&
+                                  __double_as_longlong(Qd.x) == 0x3FF0000000000000ll && zero_bits(Qd.y) &&
+                                  zero_bits(Qd.z) && zero_bits(Qd.w);
+        const bool still = never_turned ||
+                           (T.x == 0.0 && T.y == 0.0 && T.z == 0.0 && W.x == 0.0 && W.y == 0.0 && W.z == 0.0 &&
+                            fabs((((Qo[0] * Qo[0] + Qo[1] * Qo[1]) + Qo[2] * Qo[2]) + Qo[3] * Qo[3]) - 1.0) < 1e-08);
         if(!still) {
             double R[9];
             quat_matrix(Qo, R);                  // the rotation matrix of the last step
@@ -552,9 +571,10 @@ __global__ void __launch_bounds__(kBlock) k_dem_euler(DemArgs a) {
         }
         st_d4(a.d.vel, i, make_d4(v3[0], v3[1], v3[2], V.w));
         if(a.d.pos_ref != nullptr) {
+            // the guard (no counterpart in the reference) with fused multiply-adds
             const D4 r0 = ldd(a.d.pos_ref, i);
             const double ex = x3[0] - r0.x, ey = x3[1] - r0.y, ez = x3[2] - r0.z;
-            tripped = (ex * ex + ey * ey + ez * ez) > a.half_skin2;
+            tripped = fma(ex, ex, fma(ey, ey, ez * ez)) > a.half_skin2;
         }
     }
     if(__any_sync(0xffffffffu, tripped) && (threadIdx.x & 31) == 0) {
@@ -641,12 +661,17 @@ int dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cell
     return launch_status();
 }
 
-int dem_euler(pg_dem_particles *d, const pg_dem_params *prm, double half_skin2, int32_t step, pg_status *status,
-              cudaStream_t st) {
+int dem_euler(pg_dem_particles *d, const pg_dem_params *prm, int precision, double half_skin2, int32_t step,
+              pg_status *status, cudaStream_t st) {
     if(!dem_ok(d) || !prm || !status) { return PG_ERR_ARGUMENT; }
+    if(precision != PG_FP64 && precision != PG_MIXED) { return PG_ERR_ARGUMENT; }
     DemArgs a = {};
     a.d = *d; a.prm = *prm; a.status = status; a.half_skin2 = half_skin2; a.step = step;
-    if(d->n > 0) { k_dem_euler<<<blocks_for(d->n), kBlock, 0, st>>>(a); note_launch(); }
+    if(d->n > 0) {
+        if(precision == PG_MIXED) { k_dem_euler<true><<<blocks_for(d->n), kBlock, 0, st>>>(a); }
+        else { k_dem_euler<false><<<blocks_for(d->n), kBlock, 0, st>>>(a); }
+        note_launch();
+    }
     return launch_status();
 }
 

@@ -427,8 +427,8 @@ class DEMEngine:
 
     def _euler(self, step):
         self.d.step = step
-        A.call("pg_dem_euler", C.byref(self.d), C.byref(self.prm), self.half_skin2, step, self.status_ptr,
-               self.sh)
+        A.call("pg_dem_euler", C.byref(self.d), C.byref(self.prm), self.precision, self.half_skin2, step,
+               self.status_ptr, self.sh)
 
     def _check(self, st):
         if st.overflow & 8:
