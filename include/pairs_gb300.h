@@ -238,7 +238,9 @@ typedef struct {
     double *pos;                 /* double4[capacity] */
     double *vel;                 /* double4[capacity] linear velocity; w = 1 / mass, written
                                     by pg_dem_setup (0 for half spaces) */
-    double *angvel;              /* double4[capacity] angular velocity */
+    double *angvel;              /* double4[capacity] angular velocity; w = the gravity force
+                                    on z, 0 - (drho 4/3 pi r^3) g, written by pg_dem_setup
+                                    (0 for half spaces) */
     double *force;               /* double4[capacity] */
     double *torque;              /* double4[capacity] */
     double *quat;                /* double4[capacity] rotation quaternion (w, x, y, z) */
@@ -486,8 +488,9 @@ int pg_ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out,
 /* Setup kernel update_mass_and_inertia (examples/dem.py:6-15): identity rotation,
  * inv_inertia = the (0,0) entry of inversed(diagonal_matrix(0.4 m r^2)) for spheres
  * (mapping/keywords.py:129-146 arithmetic), mass = +inf and inv_inertia = 0 for half
- * spaces. */
-int pg_dem_setup(pg_dem_particles *d, void *stream);
+ * spaces.  Also stores 1 / mass in vel.w and each sphere's gravity force on z
+ * (examples/dem.py:90-92 with prm) in angvel.w. */
+int pg_dem_setup(pg_dem_particles *d, const pg_dem_params *prm, void *stream);
 
 /* Wrap, bin and sort the DEM particles like pg_bin_particles.  pos, uid, flags and
  * cells->particle_cell are permuted in place; every other per-particle array of d

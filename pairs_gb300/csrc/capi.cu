@@ -42,7 +42,7 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
 int ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift, double half_skin2,
                        int32_t step, pg_status *status, cudaStream_t st);
 int ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, cudaStream_t st);
-int dem_setup(pg_dem_particles *d, cudaStream_t st);
+int dem_setup(pg_dem_particles *d, const pg_dem_params *prm, cudaStream_t st);
 int dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
             const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, cudaStream_t st);
 int dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *cells, pg_neighbor_list *list,
@@ -166,7 +166,9 @@ int pg_ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out,
     return pg::ensemble_thermo(e, p, out, S(stream));
 }
 
-int pg_dem_setup(pg_dem_particles *d, void *stream) { return pg::dem_setup(d, S(stream)); }
+int pg_dem_setup(pg_dem_particles *d, const pg_dem_params *prm, void *stream) {
+    return pg::dem_setup(d, prm, S(stream));
+}
 
 int pg_dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
                const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, void *stream) {

@@ -42,7 +42,15 @@ struct DemArgs {
     double half_skin2;
     int32_t step;
     float screen;                // FP32 candidate screen margin (metres), mixed kernel
+    float len32[3];              // box lengths in FP32 (mixed kernel's image shifts)
 };
+
+// gravity on a sphere, examples/dem.py:90-92 in the generated order (kept in angvel.w
+// by the setup kernel: the radius never changes)
+__device__ __forceinline__ double sphere_gravity(const pg_dem_params &prm, double r) {
+    const double vol = (((4.0 / 3.0) * prm.pi) * r) * r * r;
+    return 0.0 - (prm.drho * vol) * prm.gravity;
+}
 
 __device__ __forceinline__ D4 ldd(const double *b, int i) { return ld_d4_plain(b, i); }
 
@@ -54,7 +62,7 @@ __device__ __forceinline__ bool dem_frozen(const pg_dem_particles &d, bool integ
 
 // ------------------------------------------------------------------ setup
 
-__global__ void k_dem_setup(pg_dem_particles d) {
+__global__ void k_dem_setup(pg_dem_particles d, pg_dem_params prm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= d.n) { return; }
     st_d4(d.quat, i, make_d4(1.0, 0.0, 0.0, 0.0));
@@ -77,6 +85,11 @@ __global__ void k_dem_setup(pg_dem_particles d) {
     D4 v = ldd(d.vel, i);
     v.w = 1.0 / d.mass[i];
     st_d4(d.vel, i, v);
+    // angvel.w keeps the sphere's gravity force on z (0 for half spaces), the value the
+    // contact kernels would otherwise recompute from the radius every step
+    D4 w = ldd(d.angvel, i);
+    w.w = d.shape[i] == 0 ? sphere_gravity(prm, d.radius[i]) : 0.0;
+    st_d4(d.angvel, i, w);
 }
 
 // ------------------------------------------------------------------ binning
@@ -382,9 +395,9 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force(DemArgs a) {
         atomicOr(&a.status->overflow, 8);
         atomicMax(&a.status->max_contacts, a.c.capacity + 1);
     }
-    // reset to 0, gravity on z, then the contact sums (sphere part + half-space part)
-    const double vol = (((4.0 / 3.0) * a.prm.pi) * ri) * ri * ri;
-    const double gz = 0.0 - (a.prm.drho * vol) * a.prm.gravity;
+    // reset to 0, gravity on z (kept in angvel.w), then the contact sums (sphere part +
+    // half-space part)
+    const double gz = w4.w;
     st_d4(a.d.force, i, make_d4(0.0 + (fs[0] + fh[0]), 0.0 + (fs[1] + fh[1]), gz + (fs[2] + fh[2]), 0.0));
     st_d4(a.d.torque, i, make_d4(0.0 + (ts[0] + th[0]), 0.0 + (ts[1] + th[1]), 0.0 + (ts[2] + th[2]), 0.0));
 }
@@ -405,14 +418,22 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force_mixed(DemArgs a) {
         return;
     }
     const D4 xi = ldd(a.d.pos, i), v4 = ldd(a.d.vel, i), w4 = ldd(a.d.angvel, i);
-    const float vi[3] = {(float) v4.x, (float) v4.y, (float) v4.z};
-    const float wi[3] = {(float) w4.x, (float) w4.y, (float) w4.z};
+    // the FP32 velocities and 1/mass are converted at the first contact: most spheres
+    // of a packing touch nothing, and their force is then gravity alone
+    float vi[3], wi[3], inv_mi = 0.0f;
+    bool touched = false;
+    auto convert = [&]() {
+        if(touched) { return; }
+        vi[0] = (float) v4.x; vi[1] = (float) v4.y; vi[2] = (float) v4.z;
+        wi[0] = (float) w4.x; wi[1] = (float) w4.y; wi[2] = (float) w4.z;
+        inv_mi = (float) v4.w;
+        touched = true;
+    };
     const double ri = a.d.radius[i];
-    const float inv_mi = (float) v4.w;
     // FP32 screen: a candidate whose FP32 distance exceeds the contact distance by more
     // than the FP32 rounding of the coordinates (a.screen) cannot touch
     const float4 pi32 = ld_f4(a.d.pos32, i);
-    const float lx = (float) a.box.len[0], ly = (float) a.box.len[1], lz = (float) a.box.len[2];
+    const float lx = a.len32[0], ly = a.len32[1], lz = a.len32[2];
     const int ti = a.d.type ? a.d.type[i] : 0;
     int nc = a.c.count[i];
     uint32_t used[2] = {0u, 0u};
@@ -445,6 +466,7 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force_mixed(DemArgs a) {
         const float kk = (float) rj - 0.5f * delta;
         const float rvj[3] = {n[0] * kk, n[1] * kk, n[2] * kk};
         const float rvi[3] = {rvj[0] - df[0], rvj[1] - df[1], rvj[2] - df[2]};
+        convert();
         dem_contact<float>(a, i, j, vi, wi, inv_mi, ti, n, rvi, rvj, delta, nc, used, overflow, fs, ts);
     }
     const int wb = a.cells.cell_start[a.cells.ncells], we = wb + a.cells.cell_count[a.cells.ncells];
@@ -466,6 +488,7 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force_mixed(DemArgs a) {
         const float rvi[3] = {-tmp * n[0], -tmp * n[1], -tmp * n[2]};
         const float rvj[3] = {(float) (xi.x - xj.x) + rvi[0], (float) (xi.y - xj.y) + rvi[1],
                               (float) (xi.z - xj.z) + rvi[2]};
+        convert();
         dem_contact<float>(a, i, j, vi, wi, inv_mi, ti, n, rvi, rvj, delta, nc, used, overflow, fh, th);
     }
     clear_unused(a, i, nc, used);
@@ -474,8 +497,13 @@ __global__ void __launch_bounds__(kDemBlock) k_dem_force_mixed(DemArgs a) {
         atomicOr(&a.status->overflow, 8);
         atomicMax(&a.status->max_contacts, a.c.capacity + 1);
     }
-    const double vol = (((4.0 / 3.0) * a.prm.pi) * ri) * ri * ri;
-    const double gz = 0.0 - (a.prm.drho * vol) * a.prm.gravity;
+    const double gz = w4.w;                      // gravity on z (pg_dem_setup)
+    if(!touched) {
+        // no contact: the sums are +0, and gz + 0 = gz (gz is never -0)
+        st_d4(a.d.force, i, make_d4(0.0, 0.0, gz, 0.0));
+        st_d4(a.d.torque, i, make_d4(0.0, 0.0, 0.0, 0.0));
+        return;
+    }
     st_d4(a.d.force, i, make_d4((double) (fs[0] + fh[0]), (double) (fs[1] + fh[1]), gz + (double) (fs[2] + fh[2]),
                                 0.0));
     st_d4(a.d.torque, i, make_d4((double) (ts[0] + th[0]), (double) (ts[1] + th[1]), (double) (ts[2] + th[2]), 0.0));
@@ -562,7 +590,7 @@ __global__ void __launch_bounds__(kBlock) k_dem_euler(DemArgs a) {
             const double len2 = ((r_ * r_ + i_ * i_) + j_ * j_) + k_ * k_;
             const double il2 = (fabs(len2 - 1.0) < 1e-08) ? 1.0 : 1.0 / sqrt(len2);
             for(int e = 0; e < 3; e++) { w3[e] = w3[e] + wd[e] * dt; }
-            st_d4(a.d.angvel, i, make_d4(w3[0], w3[1], w3[2], 0.0));
+            st_d4(a.d.angvel, i, make_d4(w3[0], w3[1], w3[2], W.w));
             st_d4(a.d.quat, i, make_d4(r_ * il2, i_ * il2, j_ * il2, k_ * il2));
         }
         st_d4(a.d.pos, i, make_d4(x3[0], x3[1], x3[2], X.w));
@@ -594,9 +622,9 @@ static bool contacts_ok(const pg_contacts *c, const pg_dem_particles *d) {
            c->stride >= d->n;
 }
 
-int dem_setup(pg_dem_particles *d, cudaStream_t st) {
-    if(!dem_ok(d)) { return PG_ERR_ARGUMENT; }
-    if(d->n > 0) { k_dem_setup<<<blocks_for(d->n), kBlock, 0, st>>>(*d); note_launch(); }
+int dem_setup(pg_dem_particles *d, const pg_dem_params *prm, cudaStream_t st) {
+    if(!dem_ok(d) || !prm) { return PG_ERR_ARGUMENT; }
+    if(d->n > 0) { k_dem_setup<<<blocks_for(d->n), kBlock, 0, st>>>(*d, *prm); note_launch(); }
     return launch_status();
 }
 
@@ -653,6 +681,7 @@ int dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *cell
     double span = 0.0;
     for(int k = 0; k < 3; k++) { span = fmax(span, fabs(box->lo[k]) + 2.0 * box->len[k]); }
     a.screen = (float) (64.0 * span * 1.1920928955078125e-07);
+    for(int k = 0; k < 3; k++) { a.len32[k] = (float) box->len[k]; }
     if(d->n > 0) {
         if(precision == PG_FP64) { k_dem_force<<<blocks_for(d->n, kDemBlock), kDemBlock, 0, st>>>(a); }
         else { k_dem_force_mixed<<<blocks_for(d->n, kDemBlock), kDemBlock, 0, st>>>(a); }

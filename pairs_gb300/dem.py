@@ -336,7 +336,7 @@ class DEMEngine:
         self.sh = C.c_void_p(self.stream.cuda_stream)
         if policy == "guard":
             self.d.guard = t["status"].data_ptr() + 4 * 4          # &status->guard_tripped
-        A.call("pg_dem_setup", C.byref(self.d), self.sh)
+        A.call("pg_dem_setup", C.byref(self.d), C.byref(self.prm), self.sh)
         # a state taken mid-run carries its rotations and contact history
         if state.get("quat") is not None:
             put(cur["quat"], np.asarray(state["quat"], dtype=np.float64).reshape(n, 4))
