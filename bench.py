@@ -439,7 +439,7 @@ def run_ensemble(args, rank, world, dist):
     one_steps = args.one_by_one_steps
     t0 = time.perf_counter()
     for st in reps:
-        eng = LJEngine(st, precision="mixed", half=False, tiles=False, policy="guard", sync="exact")
+        eng = LJEngine(st, precision="mixed", half=ens.half, tiles=False, policy="guard", sync="exact")
         eng.run(one_steps + 1)
         del eng
     torch.cuda.synchronize()
@@ -451,13 +451,14 @@ def run_ensemble(args, rank, world, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 force / f64 integrate",
         "data": "synthetic (trimmed fcc lattices, reference velocity rule, seed 2024)",
         "config": {"workload": f"{len(reps)} LJ replicas, {natoms} atoms total, sizes log-uniform 500..32000, "
-                               "rho U[0.6,0.9], T U[0.7,1.5], rc 2.5, skin 0.3, dt 0.005, mixed, full lists, "
-                               "guard rebuilds, CUDA-graph chunks",
+                               "rho U[0.6,0.9], T U[0.7,1.5], rc 2.5, skin 0.3, dt 0.005, mixed, "
+                               f"{'half' if ens.half else 'full'} lists, guard rebuilds, CUDA-graph chunks",
                    "replicas": len(reps), "atoms": natoms,
                    "autotuned": {"tpa": tpa, "block": block, "reach": reach}},
         "autotune_table": table,
         "one_by_one": {"value": one_value, "steps": one_steps, "seconds": one_s,
-                       "definition": "each replica alone through LJEngine (mixed, full list, guard), "
+                       "definition": f"each replica alone through LJEngine (mixed, {'half' if ens.half else 'full'} "
+                                     "list, guard), "
                                      "wall time including its setup"},
         "speedup_vs_one_by_one": value / one_value,
         "schedule": {"rebuilds": ens.nbuilds - b0, "host_syncs": ens.host_syncs - s0},

@@ -28,7 +28,7 @@ INT32_MAX = 2 ** 31 - 1
 class Ensemble:
     def __init__(self, replicas, *, cutoff=2.5, skin=0.3, dt=0.005, epsilon=1.0, sigma6=1.0, tpa=1, block=256,
                  reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, fixed_point=None,
-                 half=False, device="cuda"):
+                 half=True, device="cuda"):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -116,10 +116,10 @@ class Ensemble:
         self.e.replica_of = t["replica_of"].data_ptr()
         self.list = A.PgNeighborList()
         self.list.stride = n
-        # half lists (each interior pair once, the reaction by a vector atomic) halve the
-        # build's candidates and list bytes, but with the 125-cell stencil the per-cell loop
-        # dominates the build (4.73 -> 4.40 ms at 512 replicas, no gain per step) and the
-        # atomics make the summation order nondeterministic: full lists by default
+        # half lists (each interior pair once, the reaction by a vector atomic): at 512
+        # replicas the build takes 3.84 ms instead of 4.60 and the step 1.87 ms instead of
+        # 2.12.  The atomics make the summation order of the forces nondeterministic; full
+        # lists (half=False) give bit-reproducible runs
         self.half = bool(half)
         self.list.half = int(self.half)
         self.e.half = int(self.half)

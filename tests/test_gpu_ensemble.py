@@ -108,10 +108,12 @@ def test_fixed_point_replicas_follow_compensated_replicas():
 
 
 def test_graph_chunks_equal_plain_chunks():
+    """CUDA-graph chunks replay the plain launches bit for bit (full lists: the half
+    lists' reaction atomics sum in a run-dependent order)."""
     from pairs_gb300.ensemble import Ensemble
     reps = replicas()
-    a = Ensemble(reps, tpa=2, graphs=True)
-    b = Ensemble(reps, tpa=2, graphs=False)
+    a = Ensemble(reps, tpa=2, graphs=True, half=False)
+    b = Ensemble(reps, tpa=2, graphs=False, half=False)
     a.run(120)
     b.run(120)
     a.synchronize()
