@@ -224,21 +224,6 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
 
 // ------------------------------------------------------------------ force
 
-// FP32 separation of particle i and list entry e (compensated hi/lo, the replica's
-// exact image shift)
-__device__ __forceinline__ void ens_delta(const pg_replica &R, float4 hi, float4 lo, float4 hj, float4 lj, uint32_t code,
-                                          float &dx, float &dy, float &dz) {
-    float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
-    float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
-    if(code != 0u) {
-        const int sx = image_shift(code, 0), sy = image_shift(code, 1), sz = image_shift(code, 2);
-        dhx -= sx * R.len_hi[0]; dlx -= sx * R.len_lo[0];
-        dhy -= sy * R.len_hi[1]; dly -= sy * R.len_lo[1];
-        dhz -= sz * R.len_hi[2]; dlz -= sz * R.len_lo[2];
-    }
-    dx = dhx + dlx; dy = dhy + dly; dz = dhz + dlz;
-}
-
 __device__ __forceinline__ float ens_lj(const EnsArgs &a, int tij, float rsq) {
     const float sr2 = rcp_approx(rsq);
     const float sr6 = sr2 * sr2 * sr2 * a.sig6[tij];
@@ -250,18 +235,40 @@ __device__ __forceinline__ float ens_lj(const EnsArgs &a, int tij, float rsq) {
 // of the cutoff is queued for k_ens_cutoff_fixup, which decides it in FP64.
 constexpr int kEnsBatch = 4;
 
+// The replica's FP32 units and periodic shifts, held in registers by the force pass:
+// read through the replica table in the pair loop, they would be loaded again after
+// every reaction `red`, whose memory clobber the compiler cannot see past.
+struct RepLen {
+    float u[3];                  // fixed-point unit per axis
+    float h[3], l[3];            // len_hi, len_lo
+};
+
+__device__ __forceinline__ RepLen rep_len(const pg_replica &R) {
+    RepLen L;
+    for(int d = 0; d < 3; d++) { L.u[d] = R.fx_unit[d]; L.h[d] = R.len_hi[d]; L.l[d] = R.len_lo[d]; }
+    return L;
+}
+
 // A pair's separation: fixed point (wrapped difference in the replica's units, no
-// image shift) or compensated hi/lo with the listed image.
+// image shift) or compensated hi/lo with the listed image's exact shift.
 template<bool kFixed>
-__device__ __forceinline__ void ens_pair_delta(const pg_replica &R, const int4 &fi, const float4 &hi, const float4 &lo,
+__device__ __forceinline__ void ens_pair_delta(const RepLen &L, const int4 &fi, const float4 &hi, const float4 &lo,
                                                const int4 &fj, const float4 &hj, const float4 &lj, uint32_t code,
                                                float &dx, float &dy, float &dz) {
     if(kFixed) {
-        dx = (float) fx_diff(fi.x, fj.x) * R.fx_unit[0];
-        dy = (float) fx_diff(fi.y, fj.y) * R.fx_unit[1];
-        dz = (float) fx_diff(fi.z, fj.z) * R.fx_unit[2];
+        dx = (float) fx_diff(fi.x, fj.x) * L.u[0];
+        dy = (float) fx_diff(fi.y, fj.y) * L.u[1];
+        dz = (float) fx_diff(fi.z, fj.z) * L.u[2];
     } else {
-        ens_delta(R, hi, lo, hj, lj, code, dx, dy, dz);
+        float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
+        float dlx = lo.x - lj.x, dly = lo.y - lj.y, dlz = lo.z - lj.z;
+        if(code != 0u) {
+            const int sx = image_shift(code, 0), sy = image_shift(code, 1), sz = image_shift(code, 2);
+            dhx -= sx * L.h[0]; dlx -= sx * L.l[0];
+            dhy -= sy * L.h[1]; dly -= sy * L.l[1];
+            dhz -= sz * L.h[2]; dlz -= sz * L.l[2];
+        }
+        dx = dhx + dlx; dy = dhy + dly; dz = dhz + dlz;
     }
 }
 
@@ -276,7 +283,7 @@ __global__ void k_ens_force(EnsArgs a) {
         int4 fi = make_int4(0, 0, 0, 0);
         if(kFixed) { fi = ld_i4(a.p.pos_fx, i); }
         else { hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i)); }
-        const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
+        const RepLen L = rep_len(a.e.replicas[a.e.replica_of[i]]);
         const int ti = kOneType ? 0 : (kFixed ? fi.w : __float_as_int(hi.w)) * a.ntypes;
         const int cnt = a.list.count[i];
         const int rows = cnt > t ? (cnt - t + TPA - 1) / TPA : 0;      // this lane's entries
@@ -308,7 +315,7 @@ __global__ void k_ens_force(EnsArgs a) {
             for(int u = 0; u < kEnsBatch; u++) {
                 if(r0 + u >= rows) { continue; }
                 float dx, dy, dz;
-                ens_pair_delta<kFixed>(R, fi, hi, lo, fj[u], hj[u], lj[u], e[u] >> PG_NBR_INDEX_BITS, dx, dy, dz);
+                ens_pair_delta<kFixed>(L, fi, hi, lo, fj[u], hj[u], lj[u], e[u] >> PG_NBR_INDEX_BITS, dx, dy, dz);
                 const float rsq = dx * dx + dy * dy + dz * dz;
                 const bool near = fabsf(rsq - c2) < band;
                 if(rsq < c2 && !near) {
@@ -365,7 +372,7 @@ __global__ void __launch_bounds__(kBlock) k_ens_cutoff_fixup(EnsArgs a) {
             hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j));
         }
         float dx, dy, dz;
-        ens_pair_delta<kFixed>(R, fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
+        ens_pair_delta<kFixed>(rep_len(R), fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
         const int ti = kFixed ? fi.w : __float_as_int(hi.w), tj = kFixed ? fj.w : __float_as_int(hj.w);
         const int tij = kOneType ? 0 : ti * a.ntypes + tj;
         const float f = ens_lj(a, tij, dx * dx + dy * dy + dz * dz);
