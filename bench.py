@@ -313,7 +313,7 @@ def run_ours(args, rank, world, dist):
     # rebuild schedules on the same path and workload (mixed, same list kind): the
     # learned schedule against the reference's fixed every-20 schedule with the exact
     # guard on (a trip forces the rebuild; the host reads the guard after every step),
-    # the guard alone, and a fixed interval of 7 steps judged by the guard
+    # the guard alone, and a fixed interval of 7 steps checked by the guard
     schedules = {}
     if prec == "mixed":
         ks = max(100, min(args.steps, 800))

@@ -2,7 +2,7 @@
 
 Policy "learned" of LJEngine.  The exact FP64 displacement guard (a particle moved
 more than skin/2 since the last list build, evaluated every step inside the
-integration kernel) remains the judge of list validity.  What the network decides is
+integration kernel) still decides whether a list is valid.  What the network decides is
 when the host rebuilds and synchronises:
 
 * Warm-up: the host reads the guard after every step and rebuilds exactly at each
