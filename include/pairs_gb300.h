@@ -311,7 +311,10 @@ int64_t pg_workspace_bytes(int32_t n, int32_t ncells);
  * x - len, as the reference's exchange, sim/comm.py:101-151), bin them into the
  * cell grid, and permute every per-particle array into cell order (stable within a
  * cell by uid).  Replaces build_cell_lists + partition_cell_lists
- * (sim/cell_lists.py:90-171) and the exchange half of the halo code. */
+ * (sim/cell_lists.py:90-171) and the exchange half of the halo code.
+ * The grid must have dims[d] >= 1 and a positive, finite cell_len[d] on every axis
+ * and ncells = dims[0]*dims[1]*dims[2]; anything else returns PG_ERR_ARGUMENT before
+ * any work is queued. */
 int pg_bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells,
                      pg_workspace ws, pg_status *status, void *stream);
 
@@ -333,7 +336,11 @@ int pg_bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells,
  * before any stream capture begins.
  * Every call shares the one scratch array and leaves its contents behind (the
  * call clears what it needs zeroed itself); calls whose GPU work overlaps, on
- * different streams or from different host threads, race on it: serialise them. */
+ * different streams or from different host threads, race on it: serialise them.
+ * The binning permutation of such a call stays in the library's array, so
+ * pg_bin_permutation cannot return it: a caller that keeps further per-particle
+ * arrays of its own, which it would permute with pg_permute, uses pg_bin_particles
+ * with a workspace instead. */
 #define PG_NOALLOC_MAX_PARTICLES 131072
 #define PG_NOALLOC_MAX_CELLS     65536
 int pg_bin_particles_noalloc(const pg_box *box, pg_particles *p, pg_cells *cells, pg_status *status,
@@ -358,8 +365,13 @@ int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_c
  * is needed for nbr16 (tile) lists and may be NULL otherwise.  On the PG_MIXED path a
  * pair whose FP32 rsq lies within a relative 1e-5 of the cutoff is decided by the
  * FP64 test of the PG_FP64 path, so both paths apply the force of the same pairs;
- * such pairs are queued in ws (scratch, at least 8448 bytes; the binning workspace
- * serves) and applied by a second kernel. */
+ * such pairs are queued in ws and applied by a second kernel.  ws is scratch of at
+ * least 256 + 8 bytes; its queue holds (ws.bytes - 256) / 8 pairs.  About 1.7e-3
+ * pairs per particle fall in the band with full lists at density 0.84 (half that
+ * with half lists), so 256 + 8 * ceil(0.004 * n) bytes leaves a wide margin, and
+ * pg_workspace_bytes(n, ncells) always does.  A queue that overflows loses no
+ * force: the second kernel then walks every list again for the band's pairs, which
+ * costs about one more force pass. */
 int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                 const pg_neighbor_list *list, const pg_lj_params *lj, int precision, int sync_mode,
                 double *energy, pg_workspace ws, void *stream);
@@ -470,7 +482,7 @@ int pg_ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cell
  * FP32 on fixed-point positions (p->pos_fx, each replica's box 2^32 units, used when set)
  * or on compensated positions.  Pairs within a relative 1e-5 of the cutoff
  * are decided by the FP64 test, as in pg_lj_force, through a queue in ws (scratch, at
- * least 8448 bytes; the binning workspace serves). */
+ * least 256 + 8 bytes, sized as for pg_lj_force; the binning workspace serves). */
 int pg_ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list,
                       const pg_lj_params *lj, pg_workspace ws, void *stream);
 

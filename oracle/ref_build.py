@@ -31,7 +31,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("PAIRS_REFERENCE", "/root/reference")
+# The reference source tree: $PAIRS_REFERENCE, or a checkout named "reference" beside
+# this repository.  Only this recipe and the fixture generator read it.
+REF = os.environ.get("PAIRS_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 OUT = os.path.join(HERE, "_ref")
 
 # Parity configurations of the LJ path.  "lj4" is the 4x4x4 fcc case of the

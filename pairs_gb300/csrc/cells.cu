@@ -276,11 +276,25 @@ int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_c
     return launch_status();
 }
 
+// A cell grid the kernels can index: at least one cell of positive, finite length
+// along every axis, and ncells the product of the dimensions (the binning clamps a
+// coordinate into [0, dims - 1], which is a valid cell only for dims >= 1).
+bool grid_ok(const pg_cells *cells) {
+    if(cells == nullptr) { return false; }
+    int64_t prod = 1;
+    for(int d = 0; d < 3; d++) {
+        if(cells->dims[d] < 1 || !(cells->cell_len[d] > 0.0) || !isfinite(cells->cell_len[d])) { return false; }
+        prod *= cells->dims[d];
+        if(prod > INT32_MAX - 4) { return false; }
+    }
+    return prod == cells->ncells;
+}
+
 int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_workspace ws,
                   pg_status *status, cudaStream_t st, int32_t **perm_out) {
     if(box == nullptr || p == nullptr || cells == nullptr || status == nullptr) { return PG_ERR_ARGUMENT; }
     if(p->n < 0 || p->n > p->capacity || p->pos == nullptr) { return PG_ERR_ARGUMENT; }
-    if(cells->ncells != cells->dims[0] * cells->dims[1] * cells->dims[2]) { return PG_ERR_ARGUMENT; }
+    if(!grid_ok(cells)) { return PG_ERR_ARGUMENT; }
     const int n = p->n;
     int32_t *count = nullptr;
     int rc = bin_prepare(n, cells->ncells, ws, &count, st);

@@ -221,4 +221,26 @@ __device__ __forceinline__ int warp_max(int v) {
     return v;
 }
 
+// Publish a list build's per-particle count: the largest count of the lanes that
+// reach this call together goes to status->max_neighbors and, past the list's
+// capacity, sets overflow bit 2.  Lanes past the particle range return early in the
+// list kernels, so the maximum is taken over the active lanes only (redux.sync over
+// __activemask()) and the lowest of them publishes; a full-mask shuffle would read
+// exited lanes.
+__device__ __forceinline__ void publish_count(int cnt, int capacity, pg_status *status) {
+    const unsigned m = __activemask();
+    const int wm = __reduce_max_sync(m, cnt);
+    if((threadIdx.x & 31) == (unsigned) (__ffs(m) - 1) && wm > 0) {
+        atomicMax(&status->max_neighbors, wm);
+        if(wm > capacity) { atomicOr(&status->overflow, 2); }
+    }
+}
+
+// FP32 squared distance with a fixed operation order (no contraction left to the
+// compiler), so that every kernel that screens a pair against the cutoff band takes
+// the same decision for it.
+__device__ __forceinline__ float pair_rsq(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
 }  // namespace pg

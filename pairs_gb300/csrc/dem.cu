@@ -171,11 +171,7 @@ __global__ void __launch_bounds__(kBlock) k_dem_list(DemArgs a) {
         }
     }
     a.list.count[i] = min(cnt, a.list.max_neighbors);
-    const int wm = warp_max(cnt);
-    if((threadIdx.x & 31) == 0 && wm > 0) {
-        atomicMax(&a.status->max_neighbors, wm);
-        if(wm > a.list.max_neighbors) { atomicOr(&a.status->overflow, 2); }
-    }
+    publish_count(cnt, a.list.max_neighbors, a.status);
 }
 
 // ------------------------------------------------------------------ contact model
@@ -651,9 +647,11 @@ int dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spar
     return launch_status();
 }
 
+bool grid_ok(const pg_cells *cells);
+
 int dem_build_list(const pg_box *box, pg_dem_particles *d, const pg_cells *cells, pg_neighbor_list *list,
                    const pg_dem_params *prm, pg_status *status, cudaStream_t st) {
-    if(!box || !dem_ok(d) || !d->pos_ref || !cells || !list || !list->nbr || !list->count || !prm || !status) {
+    if(!box || !dem_ok(d) || !d->pos_ref || !grid_ok(cells) || !list || !list->nbr || !list->count || !prm || !status) {
         return PG_ERR_ARGUMENT;
     }
     if(list->stride < d->n || d->n >= (1 << PG_NBR_INDEX_BITS) || list->max_neighbors < 1) {

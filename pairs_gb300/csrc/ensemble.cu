@@ -215,11 +215,7 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
         }
     }
     a.list.count[i] = cnt < a.list.max_neighbors ? cnt : a.list.max_neighbors;
-    const int wm = warp_max(cnt);
-    if((threadIdx.x & 31) == 0 && wm > 0) {
-        atomicMax(&a.status->max_neighbors, wm);
-        if(wm > a.list.max_neighbors) { atomicOr(&a.status->overflow, 2); }
-    }
+    publish_count(cnt, a.list.max_neighbors, a.status);
 }
 
 // ------------------------------------------------------------------ force
@@ -316,7 +312,7 @@ __global__ void k_ens_force(EnsArgs a) {
                 if(r0 + u >= rows) { continue; }
                 float dx, dy, dz;
                 ens_pair_delta<kFixed>(L, fi, hi, lo, fj[u], hj[u], lj[u], e[u] >> PG_NBR_INDEX_BITS, dx, dy, dz);
-                const float rsq = dx * dx + dy * dy + dz * dz;
+                const float rsq = pair_rsq(dx, dy, dz);
                 const bool near = fabsf(rsq - c2) < band;
                 if(rsq < c2 && !near) {
                     const int tj = kFixed ? fj[u].w : __float_as_int(hj[u].w);
@@ -349,35 +345,67 @@ __global__ void k_ens_force(EnsArgs a) {
     }
 }
 
-// Queued near-cutoff pairs: the FP64 test of the single-system FP64 path decides;
+// One pair of the cutoff band: the FP64 test of the single-system FP64 path decides;
 // a pair inside adds its FP32 force (full lists: no reaction).
+template<bool kOneType, bool kFixed>
+__device__ __forceinline__ void ens_fixup_pair(const EnsArgs &a, int i, uint32_t e) {
+    const int j = (int) (e & PG_NBR_INDEX_MASK);
+    const uint32_t code = e >> PG_NBR_INDEX_BITS;
+    const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
+    if(!exact_inside(a.p.pos, i, j, code, R.len, a.cutoff2d)) { return; }
+    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi, hj = hi, lj = hi;
+    int4 fi = make_int4(0, 0, 0, 0), fj = fi;
+    if(kFixed) {
+        fi = ld_i4(a.p.pos_fx, i); fj = ld_i4(a.p.pos_fx, j);
+    } else {
+        hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i));
+        hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+    }
+    float dx, dy, dz;
+    ens_pair_delta<kFixed>(rep_len(R), fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
+    const int ti = kFixed ? fi.w : __float_as_int(hi.w), tj = kFixed ? fj.w : __float_as_int(hj.w);
+    const int tij = kOneType ? 0 : ti * a.ntypes + tj;
+    const float f = ens_lj(a, tij, pair_rsq(dx, dy, dz));
+    red_add_v4(a.p.force32 + 4 * (size_t) i, dx * f, dy * f, dz * f);
+    if(a.list.half && code == 0u) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
+}
+
+// The cutoff band's pairs, left out by the force pass: the queued records, or, when
+// the queue overflowed (more band pairs than the workspace holds), every list walked
+// again with the force pass's screen (see k_lj_cutoff_fixup).
 template<bool kOneType, bool kFixed>
 __global__ void __launch_bounds__(kBlock) k_ens_cutoff_fixup(EnsArgs a) {
     if(frozen_force(a.p)) { return; }
-    const int total = min(*a.cut_count, a.cut_capacity);
-    for(int r = blockIdx.x * blockDim.x + threadIdx.x; r < total; r += gridDim.x * blockDim.x) {
-        const int2 q = a.cut_rec[r];
-        const int i = q.x;
-        const uint32_t e = (uint32_t) q.y;
-        const int j = (int) (e & PG_NBR_INDEX_MASK);
-        const uint32_t code = e >> PG_NBR_INDEX_BITS;
-        const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
-        if(!exact_inside(a.p.pos, i, j, code, R.len, a.cutoff2d)) { continue; }
-        float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi, hj = hi, lj = hi;
-        int4 fi = make_int4(0, 0, 0, 0), fj = fi;
-        if(kFixed) {
-            fi = ld_i4(a.p.pos_fx, i); fj = ld_i4(a.p.pos_fx, j);
-        } else {
-            hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i));
-            hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+    const int queued = *a.cut_count;
+    const int first = blockIdx.x * blockDim.x + threadIdx.x, step = gridDim.x * blockDim.x;
+    if(queued <= a.cut_capacity) {
+        for(int r = first; r < queued; r += step) {
+            const int2 q = a.cut_rec[r];
+            ens_fixup_pair<kOneType, kFixed>(a, q.x, (uint32_t) q.y);
         }
-        float dx, dy, dz;
-        ens_pair_delta<kFixed>(rep_len(R), fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
-        const int ti = kFixed ? fi.w : __float_as_int(hi.w), tj = kFixed ? fj.w : __float_as_int(hj.w);
-        const int tij = kOneType ? 0 : ti * a.ntypes + tj;
-        const float f = ens_lj(a, tij, dx * dx + dy * dy + dz * dz);
-        red_add_v4(a.p.force32 + 4 * (size_t) i, dx * f, dy * f, dz * f);
-        if(a.list.half && code == 0u) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
+        return;
+    }
+    const float c2 = a.cutoff2, band = c2 * kCutBand;
+    const int tpa = a.e.tpa;
+    const size_t row = (size_t) a.list.stride * tpa;
+    for(int i = first; i < a.p.n; i += step) {
+        float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+        int4 fi = make_int4(0, 0, 0, 0);
+        if(kFixed) { fi = ld_i4(a.p.pos_fx, i); }
+        else { hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i)); }
+        const RepLen L = rep_len(a.e.replicas[a.e.replica_of[i]]);
+        const int cnt = a.list.count[i];
+        for(int k = 0; k < cnt; k++) {
+            const uint32_t e = (uint32_t) a.list.nbr[(size_t) (k / tpa) * row + (size_t) i * tpa + k % tpa];
+            const int j = (int) (e & PG_NBR_INDEX_MASK);
+            float4 hj = make_float4(0.f, 0.f, 0.f, 0.f), lj = hj;
+            int4 fj = make_int4(0, 0, 0, 0);
+            if(kFixed) { fj = ld_i4(a.p.pos_fx, j); }
+            else { hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j)); }
+            float dx, dy, dz;
+            ens_pair_delta<kFixed>(L, fi, hi, lo, fj, hj, lj, e >> PG_NBR_INDEX_BITS, dx, dy, dz);
+            if(fabsf(pair_rsq(dx, dy, dz) - c2) < band) { ens_fixup_pair<kOneType, kFixed>(a, i, e); }
+        }
     }
 }
 
@@ -482,7 +510,8 @@ __global__ void __launch_bounds__(kBlock) k_ens_thermo(EnsArgs a, double *out) {
 // ------------------------------------------------------------------ host side
 
 static bool ens_ok(const pg_ensemble *e, const pg_particles *p) {
-    return e && p && e->replicas && e->replica_of && e->nreplicas > 0 && p->n >= 0 && p->n <= p->capacity &&
+    return e && p && e->replicas && e->replica_of && e->nreplicas > 0 && e->ncells >= 1 && p->n >= 0 &&
+           p->n <= p->capacity &&
            (e->tpa == 1 || e->tpa == 2 || e->tpa == 4 || e->tpa == 8) && e->block >= 64 && e->block <= 512 &&
            e->block % 32 == 0;
 }
@@ -555,7 +584,8 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
     }
     if(p->n == 0) { return PG_OK; }
     // queue of near-cutoff pairs in the workspace (scratch between binnings)
-    if(ws.ptr == nullptr || ws.bytes < 256 + 8 * 1024) { return PG_ERR_ARGUMENT; }
+    // (one record at least; an overflowing queue makes the fixup walk every list)
+    if(ws.ptr == nullptr || ws.bytes < 256 + 8) { return PG_ERR_ARGUMENT; }
     a.cut_count = (int32_t *) ws.ptr;
     a.cut_rec = (int2 *) ((char *) ws.ptr + 256);
     a.cut_capacity = (int) ((ws.bytes - 256) / 8 < INT32_MAX ? (ws.bytes - 256) / 8 : INT32_MAX);
@@ -568,11 +598,11 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
         default: launch_force<8>(a, p->n, e->block, one, fixed, st); break;
     }
     if(fixed) {
-        if(one) { k_ens_cutoff_fixup<true, true><<<16, kBlock, 0, st>>>(a); }
-        else { k_ens_cutoff_fixup<false, true><<<16, kBlock, 0, st>>>(a); }
+        if(one) { k_ens_cutoff_fixup<true, true><<<2 * kSMs, kBlock, 0, st>>>(a); }
+        else { k_ens_cutoff_fixup<false, true><<<2 * kSMs, kBlock, 0, st>>>(a); }
     } else {
-        if(one) { k_ens_cutoff_fixup<true, false><<<16, kBlock, 0, st>>>(a); }
-        else { k_ens_cutoff_fixup<false, false><<<16, kBlock, 0, st>>>(a); }
+        if(one) { k_ens_cutoff_fixup<true, false><<<2 * kSMs, kBlock, 0, st>>>(a); }
+        else { k_ens_cutoff_fixup<false, false><<<2 * kSMs, kBlock, 0, st>>>(a); }
     }
     note_launch();
     return launch_status();

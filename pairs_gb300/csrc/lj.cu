@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
                 const uint32_t code = e >> PG_NBR_INDEX_BITS;
                 float dx, dy, dz;
                 mixed_delta<kFixed>(a, fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
-                const float rsq = dx * dx + dy * dy + dz * dz;
+                const float rsq = pair_rsq(dx, dy, dz);
                 const bool near = fabsf(rsq - c2) < band;
                 if(rsq < c2 && !near) {
                     const int tij = kOneType ? 0 : ti + (kFixed ? fj.w : __float_as_int(hj.w));
@@ -277,41 +277,74 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(ForceArgs a) {
     if(kEnergy) { block_add_energy(pe, vir, a.energy); }
 }
 
-// The queued pairs (FP32 rsq within kCutBand of the cutoff): the FP64 path's own
-// test decides each one; a pair inside gets its FP32 force (and, through a half
-// list's interior entry, the reaction), exactly as the main pass would have applied.
+// One pair of the cutoff band (FP32 rsq within kCutBand of rc^2): the FP64 path's own
+// test decides it; a pair inside gets its FP32 force (and, through a half list's
+// interior entry, the reaction), exactly as the main pass would have applied it.
+template<bool kHalf, bool kOneType, bool kEnergy, bool kFixed>
+__device__ __forceinline__ void fixup_pair(const ForceArgs &a, int i, uint32_t e) {
+    const int j = (int) (e & PG_NBR_INDEX_MASK);
+    const uint32_t code = e >> PG_NBR_INDEX_BITS;
+    if(!exact_inside(a.p.pos, i, j, code, a.box.len, a.lj.cutoff2)) { return; }
+    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi, hj = hi, lj = hi;
+    int4 fi = make_int4(0, 0, 0, 0), fj = fi;
+    if(kFixed) {
+        fi = ld_i4(a.p.pos_fx, i); fj = ld_i4(a.p.pos_fx, j);
+    } else {
+        hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i));
+        hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+    }
+    float dx, dy, dz;
+    mixed_delta<kFixed>(a, fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
+    const float rsq = pair_rsq(dx, dy, dz);
+    const int ti = kFixed ? fi.w : __float_as_int(hi.w), tj = kFixed ? fj.w : __float_as_int(hj.w);
+    const int tij = kOneType ? 0 : ti * a.lj.ntypes + tj;
+    float sr6;
+    const float f = mixed_lj(a, tij, rsq, sr6);
+    red_add_v4(a.p.force32 + 4 * (size_t) i, dx * f, dy * f, dz * f);
+    if(kHalf && code == 0u) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
+    if(kEnergy) {
+        const double w = (kHalf && code == 0u) ? 1.0 : 0.5;
+        atomicAdd(&a.energy[0], w * 4.0 * (double) a.lj.epsf[tij] * ((double) sr6 * (double) sr6 - (double) sr6));
+        atomicAdd(&a.energy[1], w * (double) (rsq * f));
+    }
+}
+
+// The pairs of the cutoff band, which the main pass left out.  Normally they are the
+// queued records.  When more pairs fell in the band than the queue holds (a workspace
+// too small for the system), the records past its capacity were dropped, so every list
+// is walked again and each band pair is taken from there instead (the screen's
+// arithmetic is the main pass's, so it finds exactly the pairs that pass left out).
+// A small workspace thus costs time, never a force.
 template<bool kHalf, bool kOneType, bool kEnergy, bool kFixed>
 __global__ void __launch_bounds__(kBlock) k_lj_cutoff_fixup(ForceArgs a) {
     if(frozen_force(a.p)) { return; }
-    const int total = min(*a.cut_count, a.cut_capacity);
-    for(int r = blockIdx.x * blockDim.x + threadIdx.x; r < total; r += gridDim.x * blockDim.x) {
-        const int2 q = a.cut_rec[r];
-        const int i = q.x;
-        const uint32_t e = (uint32_t) q.y;
-        const int j = (int) (e & PG_NBR_INDEX_MASK);
-        const uint32_t code = e >> PG_NBR_INDEX_BITS;
-        if(!exact_inside(a.p.pos, i, j, code, a.box.len, a.lj.cutoff2)) { continue; }
-        float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi, hj = hi, lj = hi;
-        int4 fi = make_int4(0, 0, 0, 0), fj = fi;
-        if(kFixed) {
-            fi = ld_i4(a.p.pos_fx, i); fj = ld_i4(a.p.pos_fx, j);
-        } else {
-            hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i));
-            hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j));
+    const int queued = *a.cut_count;
+    const int first = blockIdx.x * blockDim.x + threadIdx.x, step = gridDim.x * blockDim.x;
+    if(queued <= a.cut_capacity) {
+        for(int r = first; r < queued; r += step) {
+            const int2 q = a.cut_rec[r];
+            fixup_pair<kHalf, kOneType, kEnergy, kFixed>(a, q.x, (uint32_t) q.y);
         }
-        float dx, dy, dz;
-        mixed_delta<kFixed>(a, fi, hi, lo, fj, hj, lj, code, dx, dy, dz);
-        const float rsq = dx * dx + dy * dy + dz * dz;
-        const int ti = kFixed ? fi.w : __float_as_int(hi.w), tj = kFixed ? fj.w : __float_as_int(hj.w);
-        const int tij = kOneType ? 0 : ti * a.lj.ntypes + tj;
-        float sr6;
-        const float f = mixed_lj(a, tij, rsq, sr6);
-        red_add_v4(a.p.force32 + 4 * (size_t) i, dx * f, dy * f, dz * f);
-        if(kHalf && code == 0u) { red_add_v4(a.p.force32 + 4 * (size_t) j, -dx * f, -dy * f, -dz * f); }
-        if(kEnergy) {
-            const double w = (kHalf && code == 0u) ? 1.0 : 0.5;
-            atomicAdd(&a.energy[0], w * 4.0 * (double) a.lj.epsf[tij] * ((double) sr6 * (double) sr6 - (double) sr6));
-            atomicAdd(&a.energy[1], w * (double) (rsq * f));
+        return;
+    }
+    const float c2 = a.lj.cutoff2f, band = c2 * kCutBand;
+    for(int i = first; i < a.p.n; i += step) {
+        if(a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed)) { continue; }
+        float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+        int4 fi = make_int4(0, 0, 0, 0);
+        if(kFixed) { fi = ld_i4(a.p.pos_fx, i); }
+        else { hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i)); }
+        const int cnt = a.list.count[i];
+        for(int k = 0; k < cnt; k++) {
+            const uint32_t e = (uint32_t) a.list.nbr[(size_t) k * a.list.stride + i];
+            const int j = (int) (e & PG_NBR_INDEX_MASK);
+            float4 hj = make_float4(0.f, 0.f, 0.f, 0.f), lj = hj;
+            int4 fj = make_int4(0, 0, 0, 0);
+            if(kFixed) { fj = ld_i4(a.p.pos_fx, j); }
+            else { hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j)); }
+            float dx, dy, dz;
+            mixed_delta<kFixed>(a, fi, hi, lo, fj, hj, lj, e >> PG_NBR_INDEX_BITS, dx, dy, dz);
+            if(fabsf(pair_rsq(dx, dy, dz) - c2) < band) { fixup_pair<kHalf, kOneType, kEnergy, kFixed>(a, i, e); }
         }
     }
 }
@@ -361,9 +394,12 @@ static MixedKernels pick_mixed(bool half, bool one, bool en, bool fixed) {
 
 // The mixed path's queue of near-cutoff pairs lives in the caller's workspace: a
 // counter, then int2 records (the binning scratch of the same workspace is free
-// between rebuilds).  The expected load is a few pairs per thousand particles.
-constexpr int64_t kCutQueueMin = 256 + 8 * 1024;
-constexpr int kFixupBlocks = 16;
+// between rebuilds).  The expected load is about 1.7e-3 pairs per particle with full
+// lists and half that with half lists (1e-5 of rc^2 around the cutoff at density
+// 0.84); one record is the minimum, and a queue that overflows makes the fixup pass
+// walk every list again (k_lj_cutoff_fixup).
+constexpr int64_t kCutQueueMin = 256 + 8;
+constexpr int kFixupBlocks = 2 * kSMs;
 
 int tile_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list, const pg_cells *cells,
                   const LJTableF &lj, double *energy, cudaStream_t st);

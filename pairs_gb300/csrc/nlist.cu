@@ -147,11 +147,7 @@ __global__ void __launch_bounds__(kBlock) k_build_list(ListArgs a, pg_status *st
         }
     }
     a.list.count[i] = cnt < a.list.max_neighbors ? cnt : a.list.max_neighbors;
-    const int wm = warp_max(cnt);
-    if((threadIdx.x & 31) == 0 && wm > 0) {
-        atomicMax(&status->max_neighbors, wm);
-        if(wm > a.list.max_neighbors) { atomicOr(&status->overflow, 2); }
-    }
+    publish_count(cnt, a.list.max_neighbors, status);
 }
 
 static int axis_reach(const pg_cells *cells, int d) {
@@ -171,10 +167,11 @@ static bool fixed_point_screen(const pg_box *box, const pg_particles *p, const p
 
 int tile_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                double r_list2, pg_status *status, cudaStream_t st);
+bool grid_ok(const pg_cells *cells);
 
 int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                          pg_neighbor_list *list, double r_list2, pg_status *status, cudaStream_t st) {
-    if(!box || !p || !cells || !list || !status) { return PG_ERR_ARGUMENT; }
+    if(!box || !p || !cells || !list || !status || !grid_ok(cells)) { return PG_ERR_ARGUMENT; }
     if(list->nbr16 != nullptr) { return tile_build(box, p, cells, list, r_list2, status, st); }
     const bool fx = fixed_point_screen(box, p, cells);
     if(!p->pos || (!fx && (!p->pos_hi || !p->pos_lo)) || !p->pos_ref || !list->nbr || !list->count) {

@@ -22,6 +22,7 @@ namespace pg {
 int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_workspace ws, pg_status *status,
                   cudaStream_t st, int32_t **perm_out);
 int64_t bin_workspace_bytes(int32_t n, int32_t ncells);
+bool grid_ok(const pg_cells *cells);
 
 // Size of the binning workspace for the limits above, following the layout of
 // bin_particles' workspace: cell counts, starts and cursors for ncells + 2 entries,
@@ -57,6 +58,7 @@ static int scratch_address(void **out) {
 extern "C" int pg_bin_particles_noalloc(const pg_box *box, pg_particles *p, pg_cells *cells, pg_status *status,
                                         void *stream) {
     if(box == nullptr || p == nullptr || cells == nullptr || status == nullptr) { return PG_ERR_ARGUMENT; }
+    if(p->n < 0 || !pg::grid_ok(cells)) { return PG_ERR_ARGUMENT; }
     if(p->n > PG_NOALLOC_MAX_PARTICLES || cells->ncells > PG_NOALLOC_MAX_CELLS) { return PG_ERR_LIMIT; }
     const int64_t need = pg::bin_workspace_bytes(p->n, cells->ncells);
     if(need < 0 || (size_t) need > pg::kNoAllocBytes) { return PG_ERR_LIMIT; }

@@ -207,6 +207,7 @@ class DEMEngine:
 
     GATHERED = ("vel", "angvel", "quat", "normal", "mass", "radius", "inv_inertia", "type", "shape")
     CONTACT = ("ccount", "partner", "sticking", "history")
+    MAX_CONTACTS = 64            # the contact kernels mark a sphere's used records in a 64-bit mask
 
     def __init__(self, state, *, lo, hi, periodic=(True, True, False), params, skin=None, contact_capacity=20,
                  neighbor_capacity=32, policy="guard", chunk=None, capacity=None, device="cuda", precision="fp64"):
@@ -236,6 +237,7 @@ class DEMEngine:
         self.nbuilds = 0
         self.host_syncs = 0
         self.need_build = True
+        self.contact_regrows = 0
         self.chunk = chunk
         self._cycle = 4
         self._build_ts = 0
@@ -258,8 +260,8 @@ class DEMEngine:
             t[name] = z((cap,), i32)
         self.sets = []
         ccap = int(contact_capacity)
-        if not 1 <= ccap <= 64:
-            raise ValueError("contact_capacity must be in 1..64")
+        if not 1 <= ccap <= self.MAX_CONTACTS:
+            raise ValueError(f"contact_capacity must be in 1..{self.MAX_CONTACTS}")
         for _ in range(2):
             s = {}
             for name in ("vel", "angvel", "quat", "normal"):
@@ -274,6 +276,7 @@ class DEMEngine:
             s["history"] = z((ccap, cap, 4), f64)
             self.sets.append(s)
         self.ccap = ccap
+        self.n_infinite = int((shape != 0).sum())
 
         def put(tensor, arr, width=None):
             a = torch.from_numpy(np.ascontiguousarray(arr))
@@ -350,6 +353,10 @@ class DEMEngine:
         vals = np.asarray(vals, dtype=np.float64).reshape(-1, 4)
         uid = self.t["uid"][:self.n].cpu().numpy()
         index = {int(u): k for k, u in enumerate(uid)}
+        if len(ids):
+            most = int(np.bincount([index[int(u)] for u in ids[:, 0]], minlength=self.n).max())
+            if most > self.ccap:
+                self._grow_contacts(most)
         cnt = np.zeros(self.n, np.int32)
         part = np.zeros((self.ccap, self.n), np.int32)
         stick = np.zeros((self.ccap, self.n), np.int32)
@@ -380,6 +387,26 @@ class DEMEngine:
             c.capacity, c.stride = self.ccap, self.cap
             c.count, c.partner = s["ccount"].data_ptr(), s["partner"].data_ptr()
             c.sticking, c.history = s["sticking"].data_ptr(), s["history"].data_ptr()
+
+    def _grow_contacts(self, need):
+        """Give both contact sets room for `need` records per sphere, keeping the
+        current records (the reference's resize of its contact arrays,
+        transformations/modules.py:159-205)."""
+        if need > self.MAX_CONTACTS:
+            raise A.CapacityOverflow(f"a sphere may need {need} contact records, more than the "
+                                     f"{self.MAX_CONTACTS} the contact kernels track")
+        old = self.ccap
+        for s in self.sets:
+            for name in ("partner", "sticking", "history"):
+                t = s[name]
+                grown = torch.zeros((need,) + tuple(t.shape[1:]), dtype=t.dtype, device=self.dev)
+                grown[:old].copy_(t)
+                s[name] = grown
+        self.ccap = need
+        guard = self.d.guard
+        self._bind()
+        self.d.guard = guard
+        self.contact_regrows += 1
 
     def _alloc_list(self, max_nb):
         self.list.max_neighbors = max_nb
@@ -415,6 +442,12 @@ class DEMEngine:
                 self._alloc_list(int(st.max_neighbors * 1.2) + 8)
                 continue
             break
+        # A sphere's contact records name partners it touches this step: list partners
+        # and half spaces.  Room for that many records per sphere means the contact
+        # kernel can never run out of records before the next build.
+        need = int(st.max_neighbors) + self.n_infinite
+        if need > self.ccap:
+            self._grow_contacts(min(need, self.MAX_CONTACTS))
         self.t["status"][4] = INT32_MAX
         self.nbuilds += 1
         self.need_build = False

@@ -1,6 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Needs the reference source tree (PAIRS_REFERENCE, default /root/reference) and g++:
+Needs the reference source tree (PAIRS_REFERENCE, default: a checkout named
+"reference" beside this repository) and g++:
 for each configuration it runs oracle/ref_build.py (generate the reference's CPU
 program, insert the dump hooks, compile), runs the program, and stores a compact
 record of its output:

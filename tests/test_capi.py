@@ -57,3 +57,46 @@ def test_argument_errors_without_gpu(lib):
     assert lib.pg_build_neighbor_lists(None, None, None, None, 7.84, None, None) == _capi.PG_ERR_ARGUMENT
     assert lib.pg_lj_force(None, None, None, None, None, 0, 0, None, _capi.PgWorkspace(), None) == _capi.PG_ERR_ARGUMENT
     assert lib.pg_permute(-1, None, None, None, 4, None) == _capi.PG_ERR_ARGUMENT
+
+
+def _grid(dims, cell_len):
+    cells = _capi.PgCells()
+    for d in range(3):
+        cells.dims[d] = dims[d]
+        cells.cell_len[d] = cell_len[d]
+    cells.ncells = dims[0] * dims[1] * dims[2]
+    return cells
+
+
+@pytest.mark.parametrize("dims,cell_len", [((0, 4, 4), (1.0, 1.0, 1.0)), ((4, -1, -4), (1.0, 1.0, 1.0)),
+                                           ((4, 4, 4), (1.0, 0.0, 1.0)), ((4, 4, 4), (1.0, float("nan"), 1.0))])
+def test_bad_cell_grid_is_rejected_before_any_device_work(lib, dims, cell_len):
+    """A grid with an empty axis or a non-positive cell length would give negative cell
+    indices in the binning kernel: every entry point that bins or scans cells returns
+    PG_ERR_ARGUMENT first.  The device pointers below are never dereferenced (no CUDA
+    call happens on this path, which is why it runs without a GPU)."""
+    fake = C.c_void_p(0x1000)
+    box = _capi.PgBox()
+    p = _capi.PgParticles()
+    p.n = p.capacity = 10
+    p.pos = fake
+    cells = _grid(dims, cell_len)
+    ws = _capi.PgWorkspace(fake, 1 << 20)
+    assert lib.pg_bin_particles(C.byref(box), C.byref(p), C.byref(cells), ws, fake, None) == _capi.PG_ERR_ARGUMENT
+    assert lib.pg_bin_particles_noalloc(C.byref(box), C.byref(p), C.byref(cells), fake, None) == \
+        _capi.PG_ERR_ARGUMENT
+    lst = _capi.PgNeighborList()
+    assert lib.pg_build_neighbor_lists(C.byref(box), C.byref(p), C.byref(cells), C.byref(lst), 7.84, fake,
+                                       None) == _capi.PG_ERR_ARGUMENT
+
+
+def test_grid_product_must_match_ncells(lib):
+    fake = C.c_void_p(0x1000)
+    box = _capi.PgBox()
+    p = _capi.PgParticles()
+    p.n = p.capacity = 10
+    p.pos = fake
+    cells = _grid((4, 4, 4), (1.0, 1.0, 1.0))
+    cells.ncells = 63
+    ws = _capi.PgWorkspace(fake, 1 << 20)
+    assert lib.pg_bin_particles(C.byref(box), C.byref(p), C.byref(cells), ws, fake, None) == _capi.PG_ERR_ARGUMENT

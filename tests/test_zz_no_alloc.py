@@ -59,6 +59,16 @@ def make_set(n, box, ncells_axis, seed, dev):
     return t, p, cells, bx
 
 
+def host_recount(out, box, nc):
+    """Cell of every binned particle recomputed on the host from its (wrapped)
+    position: floor((x - lo) * (1 / cell_len)) per axis in FP64, clamped to the grid,
+    exactly the kernel's arithmetic.  Returns (counts per cell, cell of each particle)."""
+    inv = 1.0 / (box / nc)
+    c = np.clip(np.floor((out["pos"][:, :3] - 0.0) * inv).astype(np.int64), 0, nc - 1)
+    flat = (c[:, 0] * nc + c[:, 1]) * nc + c[:, 2]
+    return np.bincount(flat, minlength=nc ** 3), flat
+
+
 def outputs(t):
     return {k: t[k].cpu().numpy().copy() for k in
             ("pos", "vel", "mass", "type", "uid", "flags", "cell_start", "cell_count", "particle_cell")}
@@ -91,6 +101,14 @@ def test_no_alloc_binning_matches_workspace_binning():
         a, b = outputs(ref_t), outputs(new_t)
         for k in a:
             assert np.array_equal(a[k], b[k]), (call, k)
+        # both entry points share their kernels, so the cells are also checked against
+        # an independent count on the host
+        counts, flat = host_recount(b, box, nc)
+        assert np.array_equal(b["cell_count"][: nc ** 3], counts), call
+        assert b["cell_count"][nc ** 3] == 0, call              # no particle parked in the extra bucket
+        assert np.array_equal(b["cell_start"][: nc ** 3 + 1], np.concatenate([[0], np.cumsum(counts)])), call
+        assert np.array_equal(b["particle_cell"], flat), call
+        assert np.all(np.diff(flat) >= 0), call                 # particles stored in cell order
         assert np.array_equal(ref_t["status"].cpu().numpy(), new_t["status"].cpu().numpy())
 
 
@@ -100,6 +118,7 @@ def test_no_alloc_rejects_inputs_beyond_its_scratch():
     p.n = p.capacity = A.NOALLOC_MAX_PARTICLES + 1
     cells = A.PgCells()
     cells.dims[0] = cells.dims[1] = cells.dims[2] = 4
+    cells.cell_len[0] = cells.cell_len[1] = cells.cell_len[2] = 1.0
     cells.ncells = 64
     bx = A.PgBox()
     st = torch.zeros(8, dtype=torch.int32, device="cuda")
