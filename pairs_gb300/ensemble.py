@@ -200,10 +200,17 @@ class Ensemble:
 
     def read_status(self):
         self.host_syncs += 1
-        s = self.t["status"].cpu().numpy()
+        with torch.cuda.stream(self.stream):
+            s = self.t["status"].cpu().numpy()
         return A.PgStatus.from_buffer_copy(s.tobytes())
 
     def rebuild(self):
+        # the status resets below are torch ops: they must run on the stream the
+        # library's kernels run on, whichever stream the caller has current
+        with torch.cuda.stream(self.stream):
+            self._rebuild()
+
+    def _rebuild(self):
         by = C.byref
         self.p.guard = None
         A.call("pg_ensemble_bin", by(self.e), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
@@ -311,6 +318,7 @@ class Ensemble:
     def replica_state(self, r):
         """(pos, vel after the pending final kick is NOT applied, force) of replica r
         in uid order."""
+        self.stream.synchronize()
         a, b = int(self.first[r]), int(self.first[r] + self.sizes[r])
         uid = self.t["uid"][a:b].cpu().numpy()
         order = np.argsort(uid, kind="stable")
@@ -322,6 +330,7 @@ class Ensemble:
     def replica_pairs(self, r):
         """Verlet entries (uid_i, uid_j, sx, sy, sz) of replica r, uids counted from the
         replica's first particle."""
+        self.stream.synchronize()
         a, b = int(self.first[r]), int(self.first[r] + self.sizes[r])
         cnt = self.t["count"].cpu().numpy()[a:b]
         nbr = self.t["nbr"].cpu().numpy().astype(np.int64) & 0xFFFFFFFF

@@ -176,6 +176,7 @@ def test_ensemble_list_publishes_max_count_with_partial_warps():
     ens = Ensemble(reps, tpa=2, reach=1, policy="every", half=True)
     ens.rebuild()
     s = ens.read_status()
+    ens.synchronize()
     cnt = ens.t["count"][:total].cpu().numpy()
     assert s.max_neighbors == cnt.max()
 
