@@ -141,7 +141,7 @@ def run_ours(args, rank, world, dist):
 
     def kernel_times(eng, k):
         stream = eng.stream
-        eng.p.step = max(eng.ts - 1, 0)
+        eng.p.step = eng.device_step(max(eng.ts - 1, 0))
         out = []
         for _ in range(k):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -182,8 +182,9 @@ def run_ours(args, rank, world, dist):
 
         if force_events:
             eng.force = force_timed
-        l0 = lib.pg_kernel_launches()
-        c0 = dict(builds=eng.nbuilds, syncs=eng.host_syncs, rewinds=eng.rewinds, skipped=eng.skipped_steps)
+        l0 = lib.pg_kernel_launches() + eng.graph_kernels - eng.graph_captured
+        c0 = dict(builds=eng.nbuilds, syncs=eng.host_syncs, rewinds=eng.rewinds, skipped=eng.skipped_steps,
+                  replays=eng.graph_replays)
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.nvtx.range_push("timed")        # ncu --nvtx-include "timed/" selects these launches
         s0.record(stream)
@@ -191,12 +192,14 @@ def run_ours(args, rank, world, dist):
         s1.record(stream)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
-        launches = lib.pg_kernel_launches() - l0
+        # library kernels that ran: those launched one by one plus those of graph replays
+        launches = lib.pg_kernel_launches() + eng.graph_kernels - eng.graph_captured - l0
         eng.force = orig_force
         ms = s0.elapsed_time(s1)
         fms = [a.elapsed_time(b) for a, b in ev]
         counters = {"rebuilds": eng.nbuilds - c0["builds"], "host_syncs": eng.host_syncs - c0["syncs"],
-                    "rewinds": eng.rewinds - c0["rewinds"], "skipped_steps": eng.skipped_steps - c0["skipped"]}
+                    "rewinds": eng.rewinds - c0["rewinds"], "skipped_steps": eng.skipped_steps - c0["skipped"],
+                    "graph_replays": eng.graph_replays - c0["replays"]}
         return ms, fms, launches, counters
 
     prec, half = {"mixed-half": ("mixed", True), "mixed-full": ("mixed", False),
@@ -224,7 +227,10 @@ def run_ours(args, rank, world, dist):
     b_entry = 2 if eng.list.nbr16 else 4
     b_pos = 16 if (prec == "mixed" and eng.fixed_point) else 32     # fixed point: one int4
     b_force = n * (b_pos + 4 + b_f) + b_entry * pairs_total + (n * b_f if eng.list.half else 0)
-    kname = ("k_tile_lj" if eng.list.nbr16 else ("k_lj_mixed" if prec == "mixed" else "k_lj_fp64"))
+    # the mixed path's force pass: packed pair arithmetic on fixed-point positions
+    # (k_lj_packed), one pair at a time on compensated positions (k_lj_mixed)
+    kname = ("k_tile_lj" if eng.list.nbr16 else
+             (("k_lj_packed" if eng.fixed_point else "k_lj_mixed") if prec == "mixed" else "k_lj_fp64"))
     f_avg = statistics.mean(fms) if fms else float("nan")
     pk, pk_kind = peaks()
     achieved = b_force / (f_avg / 1e3) / 1e9
@@ -292,12 +298,15 @@ def run_ours(args, rank, world, dist):
 
     ferr = force_error() if prec == "mixed" else None
 
-    # plain FP64 path on the same workload: fixed every-20 schedule and exact guard
+    # plain FP64 path on the same workload, with rebuild schedules that keep the list
+    # valid (the exact guard read after every step, alone or with the reference's
+    # every-20 rule): at 1M atoms the guard trips every ~6 steps, so the reference's
+    # every-20 rule alone would miss pairs and is not a valid comparator
     fp64 = {}
-    k64 = max(10, args.steps // 10)
-    for half64, pol in ((True, "fixed"), (True, "guard"), (False, "fixed")):
+    k64 = max(100, args.steps)
+    for half64, pol in ((True, "guard"), (False, "guard"), (True, "fixed+guard")):
         e64 = make("fp64", half64, pol)
-        ms64, _, _, c64 = timed(e64, k64, min(args.warmup, 5), force_events=False)
+        ms64, _, _, c64 = timed(e64, k64, max(args.warmup, 3), force_events=False)
         f64ms = kernel_times(e64, 6)
         fp64[f"{'half' if half64 else 'full'}_{pol}"] = {
             "value": n * k64 / (ms64 / 1e3), "steps": k64, "force_ms": round(statistics.mean(f64ms), 4),
@@ -317,7 +326,7 @@ def run_ours(args, rank, world, dist):
     schedules = {}
     if prec == "mixed":
         ks = max(100, min(args.steps, 800))
-        for pol in (args.policy, "fixed+guard", "guard", "interval:7"):
+        for pol in (args.policy, "ema", "fixed+guard", "guard", "interval:7"):
             if pol in schedules:
                 continue
             es = make(prec, half, pol)
@@ -328,37 +337,35 @@ def run_ours(args, rank, world, dist):
                               "rewinds": cnt["rewinds"]}
             del es
 
-    # end to end through the public engine API from pinned host state
+    # end to end through the public engine API from pinned host buffers, on the state
+    # the timed loop ended with (downloaded once, untimed): every chunk uploads that
+    # state, advances `chunk` steps, and downloads positions, velocities and thermo
     chunk = min(100, args.steps)
-    nchunks = max(1, args.steps // chunk)
-    pad4 = lambda a: np.concatenate([a, np.zeros((len(a), 1))], axis=1)
-    host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
-            (("pos", pad4(st["pos"])), ("vel", pad4(st["vel"])), ("mass", st["mass"]),
-             ("type", st["type"]), ("uid", st["uid"]))}
+    nchunks = max(3, args.steps // chunk)
+    eng.settle()
+    eng.flush()
+    host = {k: eng.t[k][:n].cpu().pin_memory() for k in ("pos", "vel", "mass", "type", "uid")}
     out_pos = torch.empty((n, 4), dtype=torch.float64).pin_memory()
     out_vel = torch.empty((n, 4), dtype=torch.float64).pin_memory()
-    ee = make(prec, half, args.policy)
-    calibrate(ee)
-    ee.run(args.warmup)
     torch.cuda.synchronize()
     h2d = d2h = 0
     t0 = time.perf_counter()
     for _ in range(nchunks):
-        ee.upload(host["pos"], host["vel"], host["mass"], host["type"], host["uid"])
+        eng.upload(host["pos"], host["vel"], host["mass"], host["type"], host["uid"])
         h2d += sum(v.numel() * v.element_size() for v in host.values())
-        ee.run(chunk)
-        ee.flush()
-        out_pos.copy_(ee.t["pos"][:n], non_blocking=True)
-        out_vel.copy_(ee.t["vel"][:n], non_blocking=True)
-        ee.compute_thermo()
+        eng.run(chunk)
+        eng.flush()
+        out_pos.copy_(eng.t["pos"][:n], non_blocking=True)
+        out_vel.copy_(eng.t["vel"][:n], non_blocking=True)
+        eng.compute_thermo()
         d2h += 2 * n * 32 + 24
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
     e2e = {"value": n * chunk * nchunks / el, "unit": UNIT, "h2d_bytes_per_step": h2d // (chunk * nchunks),
-           "d2h_bytes_per_step": d2h // (chunk * nchunks),
-           "definition": f"public engine API: per call upload the full particle state from pinned host, "
-                         f"advance {chunk} MD steps, download positions+velocities and thermo"}
-    del ee
+           "d2h_bytes_per_step": d2h // (chunk * nchunks), "chunks": nchunks,
+           "definition": f"public engine API on the state the timed loop ended with: per call upload the full "
+                         f"particle state from pinned host, advance {chunk} MD steps (the first a rebuild), "
+                         f"download positions+velocities and thermo; {nchunks} calls"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -417,14 +424,14 @@ def run_ensemble(args, rank, world, dist):
     reps = [lattice.trimmed_fcc(**c) for c in cfgs]
     natoms = sum(len(r["mass"]) for r in reps)
     steps = args.steps
-    (tpa, block, reach), table = autotune(reps)
-    ens = Ensemble(reps, tpa=tpa, block=block, reach=reach)
+    (tpa, block, reach, half), table = autotune(reps)
+    ens = Ensemble(reps, tpa=tpa, block=block, reach=reach, half=half)
     ens.run(args.warmup)
     ens.synchronize()
     clocks = ClockSampler(dev.index or 0)
     clocks.start()
     lib = A.load()
-    l0 = lib.pg_kernel_launches()
+    l0 = lib.pg_kernel_launches() + ens.graph_kernels - ens.graph_captured
     b0, s0 = ens.nbuilds, ens.host_syncs
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(ens.stream)
@@ -433,7 +440,8 @@ def run_ensemble(args, rank, world, dist):
     ens.synchronize()
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
-    launches = lib.pg_kernel_launches() - l0
+    # library kernels that ran: launched one by one, plus those of graph replays
+    launches = lib.pg_kernel_launches() + ens.graph_kernels - ens.graph_captured - l0
     value = natoms * steps / (ms / 1e3)
     # one by one: every replica with the single-system mixed engine (guard policy)
     one_steps = args.one_by_one_steps
@@ -454,7 +462,7 @@ def run_ensemble(args, rank, world, dist):
                                "rho U[0.6,0.9], T U[0.7,1.5], rc 2.5, skin 0.3, dt 0.005, mixed, "
                                f"{'half' if ens.half else 'full'} lists, guard rebuilds, CUDA-graph chunks",
                    "replicas": len(reps), "atoms": natoms,
-                   "autotuned": {"tpa": tpa, "block": block, "reach": reach}},
+                   "autotuned": {"tpa": tpa, "block": block, "reach": reach, "half_lists": half}},
         "autotune_table": table,
         "one_by_one": {"value": one_value, "steps": one_steps, "seconds": one_s,
                        "definition": f"each replica alone through LJEngine (mixed, {'half' if ens.half else 'full'} "
@@ -491,6 +499,26 @@ def granular_workload(count, seed=7):
     return box, state, consts
 
 
+def dense_workload(count, seed=7):
+    """The dense DEM workload: `count` spheres, radii U[0.4, 0.6] mm, 2500 kg/m^3, on
+    an fcc lattice of 1 mm nearest-neighbour distance (a compressed packing: about 6
+    of the 12 neighbours overlap), periodic in x and y, between a plane at z = 0
+    (normal +z) and a plane at the top (normal -z), at rest under gravity.  The same
+    contact model and time step as the granular workload."""
+    import math
+    from pairs_gb300 import lattice
+    st, box = lattice.dem_compressed_fcc(count, 4e-4, 6e-4, 2500, 1e-3, seed=seed)
+    planes = dict(pos=np.array([[0.0, 0.0, 0.0], [0.0, 0.0, box[2]]]), vel=np.zeros((2, 3)), mass=np.ones(2),
+                  radius=np.zeros(2), type=np.zeros(2, np.int32), uid=np.array([count + 1, count + 2], np.int32),
+                  flags=np.array([13, 13], np.int32), shape=np.ones(2, np.int32),
+                  normal=np.array([[0.0, 0.0, 1.0], [0.0, 0.0, -1.0]]))
+    state = {k: np.concatenate([st[k] if k in st else np.zeros((count, 3)), planes[k]]) for k in planes}
+    e, nu = 0.7, 0.22
+    consts = dict(dt=1e-6, kappa=2.0 * (1.0 - nu) / (2.0 - nu), ln_e=math.log(e), tc=5e-4, drho=2500.0,
+                  gravity=9.81, mu=0.5, kn=1e5)
+    return box, state, consts
+
+
 def run_dem(args, rank, world, dist):
     """Granular DEM workload on one GB300: mixed precision (FP64 contact geometry,
     FP32 contact model, FP64 integration) against the FP64 path, particle-steps/s."""
@@ -500,7 +528,10 @@ def run_dem(args, rank, world, dist):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     count = args.dem_spheres
-    box, state, c = granular_workload(count)
+    dense = args.workload == "dem-dense"
+    builder = dense_workload if dense else granular_workload
+    box, state, c = builder(count)
+    nplanes = int((np.asarray(state["shape"]) != 0).sum())
     prm = lambda: dem_params(c["dt"], c["kappa"], c["ln_e"], c["tc"], c["drho"], c["gravity"], [0.0], [c["mu"]],
                              kn=c["kn"])
     lib = A.load()
@@ -518,8 +549,22 @@ def run_dem(args, rank, world, dist):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         ncont = int(eng.sets[0]["ccount"][:eng.n].sum().item())
-        out = dict(value=(count + 1) * steps / (ms / 1e3), ms_per_step=ms / steps, steps=steps,
-                   rebuilds=eng.nbuilds - b0, launches=lib.pg_kernel_launches() - l0, contacts_at_end=ncont)
+        # the contact kernel on its own (CUDA events on the engine's stream), on the
+        # state the run ended with
+        fev = []
+        eng.d.guard = None                      # time every pass, whatever the guard says
+        for _ in range(5):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(eng.stream)
+            eng._force(eng.ts)
+            b.record(eng.stream)
+            fev.append((a, b))
+        torch.cuda.synchronize()
+        force_ms = statistics.median([a.elapsed_time(b) for a, b in fev[1:]])
+        out = dict(value=(count + nplanes) * steps / (ms / 1e3), ms_per_step=ms / steps, steps=steps,
+                   rebuilds=eng.nbuilds - b0, launches=lib.pg_kernel_launches() - l0, contacts_at_end=ncont,
+                   contacts_per_sphere=round(ncont / count, 3), contact_kernel_ms=round(force_ms, 4),
+                   contact_capacity=eng.ccap)
         del eng
         torch.cuda.empty_cache()
         return out
@@ -533,11 +578,13 @@ def run_dem(args, rank, world, dist):
     if not args.no_cpu_baseline:
         from oracle import dem as odem
         n_cpu = 20000
-        cbox, cstate, _ = granular_workload(n_cpu)
+        cbox, cstate, _ = builder(n_cpu)
         spheres = {k: cstate[k][:n_cpu] for k in ("uid", "type", "mass", "radius", "pos", "vel")}
         p = dict(dt=c["dt"], kappa=c["kappa"], ln_e=c["ln_e"], tc=c["tc"], rho_p=2500, rho_f=0,
                  gravity=c["gravity"], mu=c["mu"], cell=1.01 * 1.2e-3)
-        sim = odem.Sim(cbox, [[n_cpu + 1, 0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 13]], p, spheres=spheres, kn=c["kn"])
+        planes = [[int(cstate["uid"][k]), 0, 1.0] + list(cstate["pos"][k]) + list(cstate["normal"][k]) + [13]
+                  for k in range(n_cpu, len(cstate["uid"]))]
+        sim = odem.Sim(cbox, planes, p, spheres=spheres, kn=c["kn"])
         sim.run(5)
         k = 100
         t0 = time.perf_counter()
@@ -547,13 +594,17 @@ def run_dem(args, rank, world, dist):
                "sample": f"{k} steps of a {n_cpu}-sphere version of the workload with oracle/dem_oracle.c "
                          "(the reference's DEM program restated: every step rebins and scans 27 cells)"}
     line = {
-        "metric": "particle-steps/s of the granular DEM workload on 1 GB300", "value": mixed["value"],
+        "metric": f"particle-steps/s of the {'dense' if dense else 'granular'} DEM workload on 1 GB300",
+        "value": mixed["value"],
         "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": mixed["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 geometry + f32 contact model / f64 integrate",
-        "data": "synthetic (seeded random non-overlapping spheres, at rest)",
+        "data": ("synthetic (seeded radii on an fcc lattice of 1 mm nearest-neighbour distance: a "
+                 "compressed packing, at rest)" if dense else
+                 "synthetic (seeded random non-overlapping spheres, at rest)"),
         "config": {"workload": f"{count} spheres r U[0.4,0.6] mm, 2500 kg/m^3, box {box[0]*1e3:.1f} x "
-                               f"{box[1]*1e3:.1f} x {box[2]*1e3:.1f} mm periodic x,y, plane z=0, gravity, kn 1e5 N/m, "
+                               f"{box[1]*1e3:.1f} x {box[2]*1e3:.1f} mm periodic x,y, "
+                               f"{'planes z=0 and z=top' if dense else 'plane z=0'}, gravity, kn 1e5 N/m, "
                                "e 0.7, kt = kappa kn (nu 0.22), Coulomb mu 0.5 with history, dt 1e-6 s",
                    "spheres": count},
         "mixed": mixed, "fp64": fp64, "speedup_mixed_vs_fp64": mixed["value"] / fp64["value"],
@@ -607,7 +658,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble", "dem"], default="lj64")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble", "dem", "dem-dense"], default="lj64")
     ap.add_argument("--dem-spheres", type=int, default=1000000, help="dem workload: number of spheres")
     ap.add_argument("--replicas", type=int, default=512, help="ensemble workload: number of replicas")
     ap.add_argument("--one-by-one-steps", type=int, default=100,
@@ -635,7 +686,7 @@ def main():
         run_reference(args, rank, world, dist)
     elif args.workload == "ensemble":
         run_ensemble(args, rank, world, dist)
-    elif args.workload == "dem":
+    elif args.workload in ("dem", "dem-dense"):
         run_dem(args, rank, world, dist)
     else:
         run_ours(args, rank, world, dist)

@@ -327,7 +327,7 @@ int pg_bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells,
  * workspace pg_bin_particles takes.  This entry point takes the same inputs and
  * outputs and no workspace: its scratch is a fixed array inside the library's own
  * device image, which every GPU that loads the library holds until the process
- * exits (about 5.3 MB).  It calls no allocator.
+ * exits (about 12.8 MB).  It calls no allocator.
  *
  * Limit: at most PG_NOALLOC_MAX_PARTICLES particles and PG_NOALLOC_MAX_CELLS cells;
  * larger inputs return PG_ERR_LIMIT before any work is queued.

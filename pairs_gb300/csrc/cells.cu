@@ -196,10 +196,75 @@ __global__ void k_split_positions(pg_box box, pg_particles p) {
     if(p.pos_fx != nullptr) { st_i4(p.pos_fx, i, fx_position(box, x.x, x.y, x.z, type)); }
 }
 
+// The permutation applied to every per-particle array in two passes: gather into the
+// staging area (new[k] = old[perm[k]], all arrays in one pass over perm), then copy
+// back, refreshing the FP32 position layouts (pos_fx, pos_hi/pos_lo) from the new
+// positions on the way when a box is given.  Absent arrays (null) are skipped.
+struct StageView {
+    D4 *pos, *vel;
+    double *mass;
+    int32_t *type, *uid, *flags, *cell;
+};
+
+__host__ __device__ inline StageView stage_view(char *stage, int n) {
+    StageView v;
+    v.pos = reinterpret_cast<D4 *>(stage);
+    v.vel = v.pos + n;
+    v.mass = reinterpret_cast<double *>(v.vel + n);
+    v.type = reinterpret_cast<int32_t *>(v.mass + n);
+    v.uid = v.type + n;
+    v.flags = v.uid + n;
+    v.cell = v.flags + n;
+    return v;
+}
+
+__global__ void k_gather_all(int n, const int32_t *perm, pg_particles p, const int32_t *cell, StageView v) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= n) { return; }
+    const int s = perm[k];
+    v.pos[k] = ld_d4_plain(p.pos, s);
+    if(p.vel != nullptr) { v.vel[k] = ld_d4_plain(p.vel, s); }
+    if(p.mass != nullptr) { v.mass[k] = p.mass[s]; }
+    if(p.type != nullptr) { v.type[k] = p.type[s]; }
+    if(p.uid != nullptr) { v.uid[k] = p.uid[s]; }
+    if(p.flags != nullptr) { v.flags[k] = p.flags[s]; }
+    v.cell[k] = cell[s];
+}
+
+__global__ void k_copy_back_all(int n, pg_particles p, int32_t *cell, StageView v, pg_box box, int split) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= n) { return; }
+    const D4 x = v.pos[k];
+    st_d4(p.pos, k, x);
+    if(p.vel != nullptr) { st_d4(p.vel, k, v.vel[k]); }
+    if(p.mass != nullptr) { p.mass[k] = v.mass[k]; }
+    int type = 0;
+    if(p.type != nullptr) { type = v.type[k]; p.type[k] = type; }
+    if(p.uid != nullptr) { p.uid[k] = v.uid[k]; }
+    if(p.flags != nullptr) { p.flags[k] = v.flags[k]; }
+    cell[k] = v.cell[k];
+    if(split) {
+        if(p.pos_hi != nullptr) {
+            const double q = box.quantum, iq = 1.0 / q;
+            float4 h, l;
+            split_pos(x.x, iq, q, h.x, l.x);
+            split_pos(x.y, iq, q, h.y, l.y);
+            split_pos(x.z, iq, q, h.z, l.z);
+            h.w = __int_as_float(type);
+            l.w = 0.0f;
+            st_f4(p.pos_hi, hl(p, k), h);
+            st_f4(p.pos_lo, hl(p, k), l);
+        }
+        if(p.pos_fx != nullptr) { st_i4(p.pos_fx, k, fx_position(box, x.x, x.y, x.z, type)); }
+    }
+}
+
 // workspace layout for pg_bin_particles (all offsets 256-byte aligned)
+constexpr size_t kStageBytes = 32 + 32 + 8 + 4 + 4 + 4 + 4;   // pos, vel, mass, type, uid, flags, cell
+
 struct BinWs {
     int32_t *count, *start, *cursor, *block_sums, *perm;
-    char *stage;                      // staging for one gathered array (32 B/particle)
+    char *stage;                      // staging of every gathered array (kStageBytes per particle)
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
@@ -215,7 +280,7 @@ static size_t bin_ws_layout(int32_t n, int32_t ncells, char *base, BinWs *w) {
     tmp.cursor = (int32_t *) take(nc * 4);
     tmp.block_sums = (int32_t *) take(nb * 4);
     tmp.perm = (int32_t *) take((size_t) n * 4);
-    tmp.stage = take((size_t) n * 32);
+    tmp.stage = take((size_t) n * kStageBytes);
     if(w) { *w = tmp; }
     return off;
 }
@@ -242,10 +307,11 @@ int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cud
 }
 
 // Everything after the count pass: exclusive scan of the counts (ncells cells plus
-// the trailing bucket), scatter, per-cell order by uid, gather of every per-particle
-// array of p and of cells->particle_cell, and the cell bookkeeping.
+// the trailing bucket), scatter, per-cell order by uid, the permutation of every
+// per-particle array of p and of cells->particle_cell, and the cell bookkeeping.
+// With a box, the FP32 position layouts of p are refreshed from the new positions.
 int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_cells *cells, pg_status *status,
-               cudaStream_t st, int32_t **perm_out) {
+               cudaStream_t st, int32_t **perm_out, const pg_box *split_box) {
     BinWs w;
     bin_ws_layout(n, ncells, (char *) ws.ptr, &w);
     if(perm_out) { *perm_out = w.perm; }
@@ -259,17 +325,12 @@ int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_c
     if(p->uid != nullptr) {
         k_sort_cells<<<blocks_for(ntot), kBlock, 0, st>>>(ntot, w.start, w.perm, p->uid, status); note_launch();
     }
-    // permute every per-particle array through the staging buffer
-    struct Arr { void *ptr; int bytes; } arrs[] = {
-        {p->pos, 32}, {p->vel, 32}, {p->mass, 8}, {p->type, 4}, {p->uid, 4}, {p->flags, 4},
-        {cells->particle_cell, 4},
-    };
-    for(const Arr &a : arrs) {
-        if(a.ptr == nullptr) { continue; }
-        int rc = gather_array(n, w.perm, a.ptr, w.stage, a.bytes, st);
-        if(rc) { return rc; }
-        cudaMemcpyAsync(a.ptr, w.stage, (size_t) n * a.bytes, cudaMemcpyDeviceToDevice, st);
-    }
+    const StageView v = stage_view(w.stage, n);
+    k_gather_all<<<blocks_for(n), kBlock, 0, st>>>(n, w.perm, *p, cells->particle_cell, v); note_launch();
+    pg_box box = {};
+    if(split_box != nullptr) { box = *split_box; }
+    k_copy_back_all<<<blocks_for(n), kBlock, 0, st>>>(n, *p, cells->particle_cell, v, box, split_box != nullptr ? 1 : 0);
+    note_launch();
     // cell bookkeeping for the sorted order
     cudaMemcpyAsync(cells->cell_start, w.start, (size_t) (ntot + 1) * 4, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(cells->cell_count, w.count, (size_t) ntot * 4, cudaMemcpyDeviceToDevice, st);
@@ -304,12 +365,8 @@ int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_worksp
         for(int d = 0; d < 3; d++) { inv.v[d] = 1.0 / cells->cell_len[d]; }
         k_bin_count<<<blocks_for(n), kBlock, 0, st>>>(*box, *p, *cells, inv, count, status); note_launch();
     }
-    rc = bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out);
-    if(rc || n == 0) { return rc; }
-    if((p->pos_hi != nullptr && p->pos_lo != nullptr) || p->pos_fx != nullptr) {
-        k_split_positions<<<blocks_for(n), kBlock, 0, st>>>(*box, *p); note_launch();
-    }
-    return launch_status();
+    const bool split = (p->pos_hi != nullptr && p->pos_lo != nullptr) || p->pos_fx != nullptr;
+    return bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out, split ? box : nullptr);
 }
 
 int split_positions(const pg_box *box, pg_particles *p, cudaStream_t st) {

@@ -22,7 +22,7 @@ namespace pg {
 
 int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cudaStream_t st);
 int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_cells *cells, pg_status *status,
-               cudaStream_t st, int32_t **perm_out);
+               cudaStream_t st, int32_t **perm_out, const pg_box *split_box);
 
 constexpr float kEnsBand = 1.0e-4f;
 
@@ -528,7 +528,7 @@ int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_work
     EnsArgs a = {};
     a.e = *e; a.p = *p; a.cells = *cells; a.status = status;
     if(n > 0) { k_ens_count<<<blocks_for(n), kBlock, 0, st>>>(a, count); note_launch(); }
-    rc = bin_finish(n, e->ncells, ws, p, cells, status, st, nullptr);
+    rc = bin_finish(n, e->ncells, ws, p, cells, status, st, nullptr, nullptr);
     if(rc || n == 0) { return rc; }
     a.p = *p;
     k_ens_split<<<blocks_for(n), kBlock, 0, st>>>(a); note_launch();

@@ -27,11 +27,13 @@ bool grid_ok(const pg_cells *cells);
 // Size of the binning workspace for the limits above, following the layout of
 // bin_particles' workspace: cell counts, starts and cursors for ncells + 2 entries,
 // the scan's block sums, the permutation (4 B per particle) and the gather staging
-// buffer (32 B per particle), each rounded up to 256 bytes.
+// area (88 B per particle: every per-particle array at once), each rounded up to 256
+// bytes.  The call below checks bin_workspace_bytes against this size, so a change
+// of the layout cannot leave the array too small.
 constexpr size_t round256(size_t x) { return (x + 255) & ~(size_t) 255; }
 constexpr size_t noalloc_bytes(size_t n, size_t ncells) {
     return round256((ncells + 2) * 4) + round256((ncells + 3) * 4) + round256((ncells + 2) * 4) +
-           round256(((ncells + 2 + 1023) / 1024 + 1) * 4) + round256(n * 4) + round256(n * 32);
+           round256(((ncells + 2 + 1023) / 1024 + 1) * 4) + round256(n * 4) + round256(n * 88);
 }
 constexpr size_t kNoAllocBytes = noalloc_bytes(PG_NOALLOC_MAX_PARTICLES, PG_NOALLOC_MAX_CELLS);
 

@@ -52,7 +52,7 @@ class LJEngine:
                  dt=0.005, ntypes=1, epsilon=None, sigma6=None, precision="fp64", half=False,
                  sync="exact", every=20, neighbor_capacity=100, policy="fixed", device="cuda",
                  capacity=None, fused=True, tiles=None, tile_tpa=2, tile_atoms=224, cell_reach=1,
-                 cell_reach_x=None, fixed_point=None):
+                 cell_reach_x=None, fixed_point=None, graphs=True):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -61,12 +61,17 @@ class LJEngine:
         self.sync = {"exact": A.PG_SYNC_EXACT, "reference": A.PG_SYNC_REFERENCE}[sync]
         if self.sync == A.PG_SYNC_REFERENCE and self.precision != A.PG_FP64:
             raise ValueError("reference image sync is defined for the FP64 path only")
-        if policy not in ("fixed", "guard", "fixed+guard", "learned") and not str(policy).startswith("interval:"):
+        if policy not in ("fixed", "guard", "fixed+guard", "learned", "ema") and not str(policy).startswith("interval:"):
             raise ValueError(f"unknown rebuild policy {policy!r}")
-        if (policy == "learned" or str(policy).startswith("interval:")) and sync == "reference":
+        if (policy in ("learned", "ema") or str(policy).startswith("interval:")) and sync == "reference":
             raise ValueError("speculative rebuild policies need exact image sync")
         self.policy = policy
         self.fused = fused
+        self.graphs = bool(graphs)
+        self._graphs = {}
+        self.graph_replays = 0
+        self.graph_kernels = 0          # kernels run by graph replays
+        self.graph_captured = 0         # kernels the library counted while capturing
         pos = np.asarray(state["pos"], dtype=np.float64)
         n = len(pos)
         box = np.asarray(state["box"], dtype=np.float64)
@@ -253,10 +258,13 @@ class LJEngine:
         if policy == "learned":
             from .schedule import LearnedSchedule
             self.schedule = LearnedSchedule(self)
+        elif policy == "ema":
+            from .schedule import EMASchedule
+            self.schedule = EMASchedule(self)
 
     @property
     def speculative(self):
-        return self.policy == "learned" or str(self.policy).startswith("interval:")
+        return self.policy in ("learned", "ema") or str(self.policy).startswith("interval:")
 
     # ------------------------------------------------------------------ buffers
 
@@ -280,6 +288,7 @@ class LJEngine:
         self.list.tile_capacity = self.TILE_LIMIT
 
     def _alloc_list(self, max_nb):
+        self._graphs = {}                   # captured graphs hold the old list's address
         self.list.max_neighbors = max_nb
         self.t.pop("nbr", None)
         self.t.pop("nbr16", None)
@@ -352,7 +361,7 @@ class LJEngine:
                 self.list.steps_since_build = 0
                 then()
             st = self._wait_status()
-            guard = st.guard_tripped if guard is None else guard
+            guard = self._guard_abs(st.guard_tripped) if guard is None else guard
             if st.nonfinite:
                 raise A.PairsError("non-finite particle position met while binning")
             if st.overflow & 4:
@@ -390,24 +399,24 @@ class LJEngine:
         by = C.byref
         if self.precision == A.PG_MIXED:
             A.call("pg_integrate_mixed", by(self.box), by(self.p), self.dt, kicks, 1, self.half_skin2,
-                   self.ts, self.status_ptr, self.sh)
+                   self.device_step(self.ts), self.status_ptr, self.sh)
             return
         if self.sync == A.PG_SYNC_REFERENCE:
             self._rotate_ring()
         name = "pg_final_initial_integrate" if kicks == 2 else "pg_initial_integrate"
-        A.call(name, by(self.box), by(self.p), self.dt, self.precision, self.half_skin2, self.ts, self.sync,
-               self.status_ptr, self.sh)
+        A.call(name, by(self.box), by(self.p), self.dt, self.precision, self.half_skin2, self.device_step(self.ts),
+               self.sync, self.status_ptr, self.sh)
 
     def flush(self):
         """Apply a deferred final half step (velocities at full step)."""
         if not self._pending_final:
             return
         self._pending_final = False
-        self.p.step = max(self.ts - 1, 0)
+        self.p.step = self.device_step(max(self.ts - 1, 0))
         by = C.byref
         if self.precision == A.PG_MIXED:
-            A.call("pg_integrate_mixed", by(self.box), by(self.p), self.dt, 1, 0, self.half_skin2, self.ts,
-                   self.status_ptr, self.sh)
+            A.call("pg_integrate_mixed", by(self.box), by(self.p), self.dt, 1, 0, self.half_skin2,
+                   self.device_step(self.ts), self.status_ptr, self.sh)
         else:
             A.call("pg_final_integrate", by(self.box), by(self.p), self.dt, self.precision, self.sh)
 
@@ -424,17 +433,26 @@ class LJEngine:
         self.settle()
         if self.nbuilds == 0:
             self.rebuild()
-        self.p.step = self.ts - 1 if self.ts > 0 else 0
+        self.p.step = self.device_step(self.ts - 1 if self.ts > 0 else 0)
         self.force(energy=True)
         e = self.t["energy"].cpu().numpy()
         return float(e[0]), float(e[1])
 
     # ------------------------------------------------------------------ schedule
 
+    def device_step(self, ts):
+        """Step number the kernels see for time step ts: counted from the start of the
+        current rebuild cycle, so that a captured chunk of steps replays unchanged in
+        any cycle.  The guard word holds such numbers too."""
+        return ts - self._cycle_start
+
+    def _guard_abs(self, g):
+        return g if g == INT32_MAX else g + self._cycle_start
+
     def guard_step(self):
         """Step at which the guard tripped since the last build (INT32_MAX if none)."""
         self.host_syncs += 1
-        return int(self.t["status"][4].item())
+        return self._guard_abs(int(self.t["status"][4].item()))
 
     def guard_tripped(self):
         return self.guard_step() != INT32_MAX
@@ -500,7 +518,8 @@ class LJEngine:
                 r = sch.predicted()                 # read back with the rebuild's status
             else:
                 r, slot = sch.predicted_steps()
-                sch.pending.append((slot, ts))
+                if slot is not None:
+                    sch.pending.append((slot, ts))
             sch.history.append((ts, r))
             self.next_rebuild = ts + max(1, int(math.floor(r * sch.margin)))
 
@@ -508,7 +527,7 @@ class LJEngine:
         """One iteration of the reference's time loop.  The final half step of a time
         step is deferred and fused with the next step's initial half step."""
         ts = self.ts
-        self.p.step = ts
+        self.p.step = self.device_step(ts)
         if ts > 0:
             self.advance(2 if self._pending_final else 1)
             self._pending_final = False
@@ -530,7 +549,7 @@ class LJEngine:
         """Second half of a time step (after the integration pass): rebuild if asked,
         force, defer the final half step, thermo."""
         ts = self.ts
-        self.p.step = ts
+        self.p.step = self.device_step(ts)
         if built:
             pass                                        # the rebuild queued the force pass
         elif rebuild:
@@ -568,10 +587,75 @@ class LJEngine:
 
     def run(self, nsteps, thermo_every=0):
         """Advance until nsteps more time steps are done (a speculative policy may
-        step back to a guard trip and redo steps)."""
+        step back to a guard trip and redo steps).  Under a trained speculative policy
+        the plain steps between two rebuild points replay as one captured CUDA graph."""
         target = self.ts + nsteps
         while self.ts < target:
-            self.step(thermo_every)
+            k = self._plain_run(target, thermo_every)
+            if k >= 2:
+                self._replay_plain(k)
+            else:
+                self.step(thermo_every)
+
+    # ------------------------------------------------------------------ CUDA graphs
+
+    def _plain_run(self, target, thermo_every):
+        """Number of plain steps (no rebuild point, no thermo, no host read) that can
+        run from the current step, or 0."""
+        if not (self.graphs and self.speculative and self.fused and not self.tiles):
+            return 0
+        if self.schedule is not None and not self.schedule.trained:
+            return 0
+        if thermo_every or not self._pending_final or self.ts <= self._cycle_start:
+            return 0
+        return max(0, min(self.next_rebuild, target) - self.ts)
+
+    def _plain_launches(self, r0, k, stream_handle):
+        """The kernels of k plain steps with device steps r0 .. r0 + k - 1: the fused
+        final + initial half kicks with the drift and the guard, then the force pass."""
+        saved = self.sh
+        self.sh = stream_handle
+        try:
+            for r in range(r0, r0 + k):
+                self.p.step = r
+                if self.precision == A.PG_MIXED:
+                    A.call("pg_integrate_mixed", C.byref(self.box), C.byref(self.p), self.dt, 2, 1, self.half_skin2,
+                           r, self.status_ptr, self.sh)
+                else:
+                    A.call("pg_final_initial_integrate", C.byref(self.box), C.byref(self.p), self.dt, self.precision,
+                           self.half_skin2, r, self.sync, self.status_ptr, self.sh)
+                self.force()
+        finally:
+            self.sh = saved
+
+    def _replay_plain(self, k):
+        """Run k plain steps as one graph replay.  The graph of a (first device step,
+        length) pair is captured on first use; it holds the buffers' addresses, so a
+        list regrow drops every graph.  Its kernels read the guard word like any other
+        launch, so steps after a trip are skipped on the device as before."""
+        r0 = self.device_step(self.ts)
+        entry = self._graphs.get((r0, k))
+        if entry is None:
+            g = torch.cuda.CUDAGraph()
+            cap = torch.cuda.Stream(device=self.dev)
+            cap.wait_stream(self.stream)
+            lib = A.load()
+            l0 = lib.pg_kernel_launches()
+            with torch.cuda.graph(g, stream=cap):
+                self._plain_launches(r0, k, C.c_void_p(cap.cuda_stream))
+            # kernels per replay (the library counts launches when they are issued)
+            entry = (g, lib.pg_kernel_launches() - l0)
+            self.graph_captured += entry[1]         # counted at capture, run by the replays
+            self.stream.wait_stream(cap)
+            self._graphs[(r0, k)] = entry
+        with torch.cuda.stream(self.stream):
+            entry[0].replay()
+        self.graph_replays += 1
+        self.graph_kernels += entry[1]
+        self.since_build += k
+        self.list.steps_since_build = self.since_build
+        self.p.step = r0 + k - 1
+        self.ts += k
 
     def upload(self, pos, vel, mass=None, type=None, uid=None):
         """Replace the particle state with host arrays (n x 4 or n x 3 FP64 pos/vel,
@@ -588,6 +672,7 @@ class LJEngine:
             if src is not None:
                 t[key][:n].copy_(src, non_blocking=True)
         self.ts = 0
+        self._cycle_start = 0
         self._pending_final = False
 
     # ------------------------------------------------------------------ readback

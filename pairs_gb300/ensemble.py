@@ -65,6 +65,8 @@ class Ensemble:
         self._cycle = 6
         self._build_ts = 0
         self._graphs = {}
+        self.graph_kernels = 0                 # kernels run by graph replays
+        self.graph_captured = 0                # kernels the library counted while capturing
         self.stream = torch.cuda.Stream(device=self.dev)
         self.sh = C.c_void_p(self.stream.cuda_stream)
 
@@ -134,9 +136,14 @@ class Ensemble:
 
     # ------------------------------------------------------------------ layout
 
-    def configure(self, tpa, block, reach):
-        """Set the force kernel's threads per atom / block size and the cell size
-        (cells of >= r_list / reach); takes effect at the next rebuild."""
+    def configure(self, tpa, block, reach, half=None):
+        """Set the force kernel's threads per atom / block size, the cell size (cells
+        of >= r_list / reach) and, if given, the list layout (half or full); takes
+        effect at the next rebuild."""
+        if half is not None:
+            self.half = bool(half)
+            self.list.half = int(self.half)
+            self.e.half = int(self.half)
         self.tpa, self.block, self.reach = int(tpa), int(block), int(reach)
         self.e.tpa, self.e.block = self.tpa, self.block
         reps = (A.PgReplica * self.nrep)()
@@ -252,15 +259,20 @@ class Ensemble:
         if not self.graphs:
             self._chunk_launches(k)
             return
-        g = self._graphs.get(k)
-        if g is None:
+        entry = self._graphs.get(k)
+        if entry is None:
             # first use of this length: capture it (the launches of the capture are
             # not executed; the replay below runs them)
             g = torch.cuda.CUDAGraph()
+            lib = A.load()
+            l0 = lib.pg_kernel_launches()
             with torch.cuda.graph(g, stream=self.stream):
                 self._chunk_launches(k)
-            self._graphs[k] = g
-        g.replay()
+            entry = (g, lib.pg_kernel_launches() - l0)
+            self.graph_captured += entry[1]         # counted at capture, run by the replays
+            self._graphs[k] = entry
+        entry[0].replay()
+        self.graph_kernels += entry[1]
 
     def run(self, nsteps):
         """Advance every replica by nsteps time steps."""
@@ -350,16 +362,19 @@ class Ensemble:
                         axis=1).astype(np.int32)
 
 
-def autotune(replicas, candidates=None, steps=6, **kw):
-    """Time (tpa, block, reach) candidates on this ensemble: per candidate one list
-    build and `steps` force passes (CUDA events); score = force time + build time /
-    expected steps between rebuilds.  Returns (best, table)."""
+def autotune(replicas, candidates=None, steps=6, cycle=5.0, **kw):
+    """Time layout candidates (tpa, block, reach, half) on this ensemble: threads per
+    atom, block size, cell size (cells of >= r_list / reach) and list layout (half
+    lists with reactions, or full lists).  Per candidate one list build and `steps`
+    force passes (CUDA events); score = force time + build time / `cycle`, the steps
+    between rebuilds (any replica's trip rebuilds all: about every 5 steps at 512
+    replicas).  Returns (best, table)."""
     if candidates is None:
-        candidates = [(t, b, r) for r in (1, 2) for t in (1, 2, 4, 8) for b in (128, 256)]
+        candidates = [(t, b, r, h) for h in (True, False) for r in (1, 2) for t in (1, 2, 4, 8) for b in (128, 256)]
     ens = Ensemble(replicas, graphs=False, **kw)
     table = []
-    for tpa, block, reach in candidates:
-        ens.configure(tpa, block, reach)
+    for tpa, block, reach, half in candidates:
+        ens.configure(tpa, block, reach, half=half)
         with torch.cuda.stream(ens.stream):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(ens.stream)
@@ -375,9 +390,9 @@ def autotune(replicas, candidates=None, steps=6, **kw):
         ens.synchronize()
         build = e0.elapsed_time(e1)
         force = float(np.median([a.elapsed_time(b) for a, b in f[1:]]))
-        score = force + build / 8.0
-        table.append(dict(tpa=tpa, block=block, reach=reach, force_ms=force, build_ms=build, score=score))
+        score = force + build / cycle
+        table.append(dict(tpa=tpa, block=block, reach=reach, half=half, force_ms=force, build_ms=build, score=score))
     best = min(table, key=lambda r: r["score"])
     del ens
     torch.cuda.empty_cache()
-    return (best["tpa"], best["block"], best["reach"]), table
+    return (best["tpa"], best["block"], best["reach"], best["half"]), table

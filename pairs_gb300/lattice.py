@@ -288,3 +288,31 @@ def dem_random_packing(count, box, rmin, rmax, density, seed=7, spacing=None):
     return dict(pos=pos, vel=np.zeros((count, 3)), mass=mass, radius=r, type=np.zeros(count, np.int32),
                 uid=np.arange(1, count + 1, dtype=np.int32), flags=np.zeros(count, np.int32),
                 shape=np.zeros(count, np.int32))
+
+
+def dem_compressed_fcc(count, rmin, rmax, density, nearest, seed=7):
+    """`count` spheres on the sites of an fcc lattice whose nearest-neighbour distance is
+    `nearest`, radii uniform in [rmin, rmax] (numpy PCG64 with `seed`), at rest: a
+    compressed packing in which a pair of neighbours overlaps whenever r_i + r_j >
+    nearest (with radii U[0.4, 0.6] mm and nearest = 1 mm, half of the 12 neighbours).
+    The lattice has n x n x 2n unit cells (n the smallest that holds `count`), filled
+    from the bottom; sites start half a nearest distance above z = 0.  Returns the
+    state (mass 4/3 pi r^3 density, uid 1..count) and the box (x, y periodic lengths
+    and the height of the highest site plus half a nearest distance)."""
+    a = nearest * math.sqrt(2.0)
+    n = int(math.ceil((count / 8.0) ** (1.0 / 3.0)))
+    basis = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.0], [0.5, 0.0, 0.5], [0.0, 0.5, 0.5]])
+    k = np.arange(2 * n * n * n)
+    ix, iy, iz = k % n, (k // n) % n, k // (n * n)
+    cells = np.stack([ix, iy, iz], axis=1).astype(np.float64)
+    sites = (cells[:, None, :] + basis[None, :, :]).reshape(-1, 3)
+    sites = sites[np.lexsort((sites[:, 0], sites[:, 1], sites[:, 2]))][:count] * a
+    sites[:, 2] += 0.5 * nearest
+    g = np.random.default_rng(seed)
+    r = g.uniform(rmin, rmax, count)
+    mass = (4.0 / 3.0) * math.pi * r * r * r * density
+    box = (n * a, n * a, float(sites[:, 2].max()) + 0.5 * nearest)
+    state = dict(pos=sites, vel=np.zeros((count, 3)), mass=mass, radius=r, type=np.zeros(count, np.int32),
+                 uid=np.arange(1, count + 1, dtype=np.int32), flags=np.zeros(count, np.int32),
+                 shape=np.zeros(count, np.int32))
+    return state, box

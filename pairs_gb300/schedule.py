@@ -191,3 +191,65 @@ class LearnedSchedule:
         self.features_into(slot)
         self.predict_log(slot)
         return math.exp(float(self.result[0].item())), slot
+
+
+class EMASchedule:
+    """Policy "ema": the trivial predictor the learned schedule is measured against.
+
+    It predicts the next cycle's length (steps from a list build to the first guard
+    trip) as an exponential moving average of the lengths seen so far, with no GPU
+    work at all.  A cycle that ended at a proactive rebuild before any trip only
+    bounds its length from below, so such a cycle can raise the average but never
+    lower it.  Stepping, speculation, rewinds and the exact FP64 guard are the
+    learned policy's; only the prediction differs.
+    """
+
+    samples_per_cycle = 0
+
+    def __init__(self, engine, alpha=0.3, margin=1.2, warmup_cycles=3):
+        self.e = engine
+        self.alpha = alpha
+        # a step past the trip costs only its skipped launches, a rebuild before the
+        # trip a whole list build: the margin leans towards running past the trip
+        self.margin = margin
+        self.warmup_cycles = warmup_cycles
+        self.ema = None
+        self.cycles = 0
+        self.trained = False
+        self.pending = []
+        self.history = []
+        self._next = None
+        self._start = None
+
+    def sample_at_build(self, predict):
+        self._next = 0
+        return 0
+
+    def open_cycle(self, step):
+        self._start = step
+        self._next = None
+
+    def record(self, step):
+        pass
+
+    def close_cycle(self, trip_step, end_step):
+        if self._start is None:
+            return
+        if trip_step is not None:
+            length = max(trip_step - self._start, 1)
+            self.ema = length if self.ema is None else (1 - self.alpha) * self.ema + self.alpha * length
+        else:
+            length = max(end_step - self._start, 1)
+            blend = length if self.ema is None else (1 - self.alpha) * self.ema + self.alpha * length
+            self.ema = blend if self.ema is None else max(self.ema, blend)
+        self.cycles += 1
+
+    def train(self, *args, **kw):
+        self.trained = self.ema is not None
+        return None
+
+    def predicted(self):
+        return self.ema
+
+    def predicted_steps(self):
+        return self.ema, None

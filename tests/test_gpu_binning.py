@@ -208,7 +208,7 @@ def test_near_cutoff_queue_overflow_loses_no_force(half):
     eng.run(40)
     eng.settle()
     eng.rebuild()
-    eng.p.step = eng.ts
+    eng.p.step = eng.device_step(eng.ts)
     eng.force(energy=True)
     torch.cuda.synchronize()
     queued = int(eng.t["ws"][:4].view(torch.int32).item())
