@@ -584,7 +584,7 @@ def run_dem(args, rank, world, dist):
                  gravity=c["gravity"], mu=c["mu"], cell=1.01 * 1.2e-3)
         planes = [[int(cstate["uid"][k]), 0, 1.0] + list(cstate["pos"][k]) + list(cstate["normal"][k]) + [13]
                   for k in range(n_cpu, len(cstate["uid"]))]
-        sim = odem.Sim(cbox, planes, p, spheres=spheres, kn=c["kn"])
+        sim = odem.Sim(cbox, planes, p, spheres=spheres, kn=c["kn"], ccap=64 if dense else 20)
         sim.run(5)
         k = 100
         t0 = time.perf_counter()

@@ -28,22 +28,20 @@ constexpr int kFeat = 4;   // f0, f1, f2, valid
 
 // ---------------------------------------------------------------- features
 
-// kCellLanes lanes per cell, chosen by the host from the mean occupancy: a warp per
-// cell of ~19 particles (8 lanes measured slower there: 34.5 vs 31 us at 1M atoms),
-// half a warp for cells of ~10 (55 us with a warp per cell at 1M atoms in 110k cells)
-template<int kCellLanes>
-__global__ void k_cell_features(pg_particles p, pg_cells cells, int precision, float since, float dt,
-                                float inv_half_skin, float *feat) {
-    const int cell = (blockIdx.x * blockDim.x + threadIdx.x) / kCellLanes;
-    const int lane = threadIdx.x % kCellLanes;
-    const bool live = cell < cells.ncells;
-    const int b = live ? cells.cell_start[cell] : 0, cnt = live ? cells.cell_count[cell] : 0;
-    float vmax = 0.0f, fsum = 0.0f;
-    for(int k = lane; k < cnt; k += kCellLanes) {
-        const int i = b + k;
+// One thread per particle (particles are stored in cell order, so a warp spans a few
+// cells): each lane adds its particle's |F|/m to its cell with an atomic, and the
+// lanes of a cell take the largest |v|^2 together (redux over the lanes that share the
+// cell) before one of them publishes it.  The accumulators live in the feature rows
+// themselves (zeroed first); k_cell_finish turns them into the features.  (A kernel
+// with 16 lanes per cell of ~10 particles took 39 us at 1M atoms in 110k cells.)
+__global__ void __launch_bounds__(256) k_cell_accum(pg_particles p, pg_cells cells, int precision, float *feat) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = i < p.n ? cells.particle_cell[i] : -1;
+    const bool live = c >= 0 && c < cells.ncells;
+    float vv = 0.0f, fm = 0.0f;
+    if(live) {
         const D4 v = ld_d4(p.vel, i);
-        const float vv = (float) (v.x * v.x + v.y * v.y + v.z * v.z);
-        vmax = fmaxf(vmax, vv);
+        vv = (float) (v.x * v.x + v.y * v.y + v.z * v.z);
         float fx, fy, fz;
         if(precision == PG_MIXED) {
             const float4 f = ld_f4(p.force32, i);
@@ -52,19 +50,29 @@ __global__ void k_cell_features(pg_particles p, pg_cells cells, int precision, f
             const D4 f = ld_d4(p.force, i);
             fx = (float) f.x; fy = (float) f.y; fz = (float) f.z;
         }
-        fsum += sqrtf(fx * fx + fy * fy + fz * fz) / (float) p.mass[i];
+        fm = sqrtf(fx * fx + fy * fy + fz * fz) / (float) p.mass[i];
     }
-    for(int o = kCellLanes / 2; o > 0; o >>= 1) {
-        vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o, kCellLanes));
-        fsum += __shfl_xor_sync(0xffffffffu, fsum, o, kCellLanes);
+    const unsigned group = __match_any_sync(0xffffffffu, c);
+    // |v|^2 >= 0: its bit pattern orders like the value
+    const int vmax = __reduce_max_sync(group, __float_as_int(vv));
+    if(live) {
+        float *f = feat + (size_t) c * kFeat;
+        atomicAdd(f + 1, fm);
+        if((threadIdx.x & 31) == (unsigned) (__ffs(group) - 1)) { atomicMax(reinterpret_cast<int *>(f), vmax); }
     }
-    if(live && lane == 0) {
-        float *f = feat + (size_t) cell * kFeat;
-        f[0] = sqrtf(vmax) * dt * inv_half_skin;
-        f[1] = cnt > 0 ? fsum / cnt * dt * dt * inv_half_skin : 0.0f;
-        f[2] = since * (1.0f / 20.0f);
-        f[3] = cnt > 0 ? 1.0f : 0.0f;
-    }
+}
+
+__global__ void __launch_bounds__(256) k_cell_finish(pg_cells cells, float since, float dt, float inv_half_skin,
+                                                     float *feat) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if(c >= cells.ncells) { return; }
+    float *f = feat + (size_t) c * kFeat;
+    const int cnt = cells.cell_count[c];
+    const float vmax = __int_as_float(*reinterpret_cast<const int *>(f));
+    f[0] = sqrtf(vmax) * dt * inv_half_skin;
+    f[1] = cnt > 0 ? f[1] / cnt * dt * dt * inv_half_skin : 0.0f;
+    f[2] = since * (1.0f / 20.0f);
+    f[3] = cnt > 0 ? 1.0f : 0.0f;
 }
 
 // ---------------------------------------------------------------- forward
@@ -339,15 +347,11 @@ int cell_features(const pg_particles *p, const pg_cells *cells, int precision, i
                   double half_skin, float *feat, cudaStream_t st) {
     if(!p || !cells || !feat || !p->vel || !p->mass) { return PG_ERR_ARGUMENT; }
     if(precision == PG_MIXED ? !p->force32 : !p->force) { return PG_ERR_ARGUMENT; }
-    const int threads = 256;
-    const double mean = cells->ncells > 0 ? (double) p->n / cells->ncells : 0.0;
-    const int lanes = mean <= 6.0 ? 8 : (mean <= 14.0 ? 16 : 32);
-    const int blocks = (int) (((int64_t) cells->ncells * lanes + threads - 1) / threads);
+    if(!cells->particle_cell || !cells->cell_count || cells->ncells <= 0) { return PG_ERR_ARGUMENT; }
     const float ts = (float) since, fdt = (float) dt, ihs = (float) (1.0 / half_skin);
-    if(lanes == 8) { k_cell_features<8><<<blocks, threads, 0, st>>>(*p, *cells, precision, ts, fdt, ihs, feat); }
-    else if(lanes == 16) { k_cell_features<16><<<blocks, threads, 0, st>>>(*p, *cells, precision, ts, fdt, ihs, feat); }
-    else { k_cell_features<32><<<blocks, threads, 0, st>>>(*p, *cells, precision, ts, fdt, ihs, feat); }
-    note_launch();
+    cudaMemsetAsync(feat, 0, (size_t) cells->ncells * kFeat * sizeof(float), st);
+    if(p->n > 0) { k_cell_accum<<<blocks_for(p->n), 256, 0, st>>>(*p, *cells, precision, feat); note_launch(); }
+    k_cell_finish<<<blocks_for(cells->ncells), 256, 0, st>>>(*cells, ts, fdt, ihs, feat); note_launch();
     return launch_status();
 }
 

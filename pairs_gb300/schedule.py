@@ -29,13 +29,16 @@ from . import _capi as A
 
 class LearnedSchedule:
     def __init__(self, engine, warmup_cycles=6, samples_per_cycle=4, margin=1.1, temperature=0.05, lr=3e-3,
-                 train_steps=300, seed=0, max_samples=64, top_cells=256, online_every=32, online_steps=1,
+                 train_steps=300, seed=0, max_samples=64, top_cells=256, online_every=128, online_steps=1,
                  online_recent=16):
         self.e = engine
         lib = A.load()
         self.np = lib.pg_mlp_param_count()
         self.ncells_all = engine.cells.ncells
         self.ncells = min(top_cells, self.ncells_all)       # cells per sample: the fastest ones
+        # one Adam step on the 16 newest samples every `online_every` cycles keeps the
+        # network following the run; each costs ~0.5 ms at 1M atoms, so every 128 cycles
+        # (every 32 cost 16 us per cycle, a quarter of the schedule's own work)
         self.online_every = online_every
         self.online_steps = online_steps
         self.online_recent = online_recent
