@@ -67,7 +67,8 @@ extern "C" {
 /* Device-side status, written by kernels (mirrors the reference's resizes[]). */
 typedef struct {
     int32_t overflow;            /* bit 0 cells, bit 1 neighbours, bit 2 tile
-                                    neighbourhood, bit 3 contacts */
+                                    neighbourhood, bit 3 contacts; bit 4: a grid
+                                    barrier of pg_lj_steps ran out of time */
     int32_t max_cell_count;      /* largest cell occupancy seen */
     int32_t max_neighbors;       /* largest per-particle Verlet count seen */
     int32_t nonfinite;           /* set when a non-finite value was met */
@@ -375,6 +376,34 @@ int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_c
 int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                 const pg_neighbor_list *list, const pg_lj_params *lj, int precision, int sync_mode,
                 double *energy, pg_workspace ws, void *stream);
+
+/* Plain time steps of the mixed-precision LJ path in one persistent, cooperative
+ * launch: for each device step first_step .. first_step + nsteps - 1, the fused final
+ * + initial half kicks with the FP64 drift and displacement guard (pg_integrate_mixed
+ * with kicks = 2), the force pass on the Verlet list (pg_lj_force) and its FP64
+ * decision of the cutoff band, each phase closed by a grid barrier.  Replaces the
+ * per-module kernel launches and device synchronisations of the reference's
+ * generated time loop (src/pairs/code_gen/cgen.py:540-576) for the steps between two
+ * list rebuilds.  Needs fixed-point positions (pos_fx, ref_fx), force32, global
+ * lists.  The guard keeps its meaning: a trip in the integration of step r ends the
+ * launch before the force of step r (status->guard_tripped = r), as the separate
+ * kernels would skip themselves.  ws: scratch as for pg_lj_force (its first 256
+ * bytes hold the queue count and the barrier words).  No barrier waits longer than
+ * barrier_timeout_s (2 s if <= 0): after that the launch ends early with
+ * status->overflow bit 4 set and the state of an unfinished step.  A call with
+ * nsteps = 0 only prepares the launch (it queries the device once, so make it before
+ * a stream capture that will hold such launches). */
+int pg_lj_steps(const pg_box *box, pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
+                double dt, double half_skin2, int32_t first_step, int32_t nsteps, pg_status *status,
+                pg_workspace ws, double barrier_timeout_s, void *stream);
+
+/* Diagnostic of the grid barrier that pg_lj_steps uses (no counterpart in the
+ * reference): a cooperative launch passes three barriers that expect extra_arrivals
+ * more blocks than it has.  With extra_arrivals = 0 it returns with status untouched;
+ * with more, no wait can end, every block gives up after timeout_s and
+ * status->overflow bit 4 is set.  Either way the device stays usable. */
+int pg_grid_barrier_check(int32_t extra_arrivals, double timeout_s, pg_status *status, pg_workspace ws,
+                          void *stream);
 
 /* Velocity-Verlet half steps of examples/md.py:11-17 (the reference's
  * initial_integrate / final_integrate modules), same operation order:

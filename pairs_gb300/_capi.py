@@ -129,6 +129,9 @@ SIGNATURES = {
                                           C.c_void_p, C.c_void_p]),
     "pg_lj_force": (C.c_int, [P(PgBox), P(PgParticles), P(PgCells), P(PgNeighborList), P(PgLJParams), C.c_int,
                               C.c_int, C.c_void_p, PgWorkspace, C.c_void_p]),
+    "pg_lj_steps": (C.c_int, [P(PgBox), P(PgParticles), P(PgNeighborList), P(PgLJParams), C.c_double, C.c_double,
+                              C.c_int32, C.c_int32, C.c_void_p, PgWorkspace, C.c_double, C.c_void_p]),
+    "pg_grid_barrier_check": (C.c_int, [C.c_int32, C.c_double, C.c_void_p, PgWorkspace, C.c_void_p]),
     "pg_initial_integrate": (C.c_int, [P(PgBox), P(PgParticles), C.c_double, C.c_int, C.c_double, C.c_int32,
                                        C.c_int, C.c_void_p, C.c_void_p]),
     "pg_final_integrate": (C.c_int, [P(PgBox), P(PgParticles), C.c_double, C.c_int, C.c_void_p]),

@@ -42,6 +42,10 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
 int ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift, double half_skin2,
                        int32_t step, pg_status *status, cudaStream_t st);
 int ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, cudaStream_t st);
+int lj_steps(const pg_box *box, pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj, double dt,
+             double half_skin2, int32_t first, int32_t nsteps, pg_status *status, pg_workspace ws, double timeout_s,
+             cudaStream_t st);
+int grid_barrier_check(int32_t extra_arrivals, double timeout_s, pg_status *status, pg_workspace ws, cudaStream_t st);
 int dem_setup(pg_dem_particles *d, const pg_dem_params *prm, cudaStream_t st);
 int dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
             const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, cudaStream_t st);
@@ -100,6 +104,17 @@ int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                 const pg_neighbor_list *list, const pg_lj_params *lj, int precision, int sync_mode,
                 double *energy, pg_workspace ws, void *stream) {
     return pg::lj_force(box, p, cells, list, lj, precision, sync_mode, energy, ws, S(stream));
+}
+
+int pg_lj_steps(const pg_box *box, pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj, double dt,
+                double half_skin2, int32_t first_step, int32_t nsteps, pg_status *status, pg_workspace ws,
+                double barrier_timeout_s, void *stream) {
+    return pg::lj_steps(box, p, list, lj, dt, half_skin2, first_step, nsteps, status, ws, barrier_timeout_s, S(stream));
+}
+
+int pg_grid_barrier_check(int32_t extra_arrivals, double timeout_s, pg_status *status, pg_workspace ws,
+                          void *stream) {
+    return pg::grid_barrier_check(extra_arrivals, timeout_s, status, ws, S(stream));
 }
 
 int pg_initial_integrate(const pg_box *box, pg_particles *p, double dt, int precision,

@@ -23,20 +23,9 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "lj_packed.cuh"
 
 namespace pg {
-
-constexpr int kMaxTypes = 8;
-
-struct LJTable {
-    int ntypes;
-    float cutoff2f;
-    double cutoff2;
-    double eps[kMaxTypes * kMaxTypes];
-    double sig6[kMaxTypes * kMaxTypes];
-    float epsf[kMaxTypes * kMaxTypes];
-    float sig6f[kMaxTypes * kMaxTypes];
-};
 
 struct ForceArgs {
     pg_box box;
@@ -288,91 +277,19 @@ constexpr int kPackedBlock = 128;
 
 template<bool kHalf, bool kOneType, int kB>
 __global__ void __launch_bounds__(kPackedBlock) k_lj_packed(ForceArgs a) {
-    static_assert(kB % 2 == 0, "entries are taken in pairs");
     if(frozen_force(a.p)) { return; }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= a.p.n) { return; }
-    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    float3 f = make_float3(0.0f, 0.0f, 0.0f);
     if(!(a.p.flags != nullptr && (a.p.flags[i] & kFlagFixed))) {
-        const int4 fi = ld_i4(a.p.pos_fx, i);
-        const int ti = kOneType ? 0 : fi.w * a.lj.ntypes;
-        const int cnt = a.list.count[i];
-        const int32_t *nb = a.list.nbr + i;
-        const size_t stride = (size_t) a.list.stride;
-        const float c2 = a.lj.cutoff2f, band = c2 * kCutBand;
-        const float2 ux = make_float2(a.box.fx_unit[0], a.box.fx_unit[0]);
-        const float2 uy = make_float2(a.box.fx_unit[1], a.box.fx_unit[1]);
-        const float2 uz = make_float2(a.box.fx_unit[2], a.box.fx_unit[2]);
-        const float2 half2 = make_float2(-0.5f, -0.5f);
-        float2 FX = make_float2(0.0f, 0.0f), FY = FX, FZ = FX;
-        uint32_t cur[kB];
-#pragma unroll
-        for(int u = 0; u < kB; u++) { cur[u] = u < cnt ? (uint32_t) __ldcs(nb + u * stride) : 0u; }
-        for(int k0 = 0; k0 < cnt; k0 += kB) {
-            int4 fj[kB];
-#pragma unroll
-            for(int u = 0; u < kB; u++) { fj[u] = ld_i4(a.p.pos_fx, (int) (cur[u] & PG_NBR_INDEX_MASK)); }
-            uint32_t nxt[kB];
-            const int32_t *nbn = nb + (size_t) (k0 + kB) * stride;
-#pragma unroll
-            for(int u = 0; u < kB; u++) { nxt[u] = k0 + kB + u < cnt ? (uint32_t) __ldcs(nbn + u * stride) : 0u; }
-            uint32_t pending = 0u;
-#pragma unroll
-            for(int u = 0; u < kB; u += 2) {
-                const bool va = k0 + u < cnt, vb = k0 + u + 1 < cnt;
-                const float2 dX = __fmul2_rn(make_float2((float) fx_diff(fi.x, fj[u].x), (float) fx_diff(fi.x, fj[u + 1].x)), ux);
-                const float2 dY = __fmul2_rn(make_float2((float) fx_diff(fi.y, fj[u].y), (float) fx_diff(fi.y, fj[u + 1].y)), uy);
-                const float2 dZ = __fmul2_rn(make_float2((float) fx_diff(fi.z, fj[u].z), (float) fx_diff(fi.z, fj[u + 1].z)), uz);
-                float2 R = __fmul2_rn(dX, dX);
-                R = __ffma2_rn(dY, dY, R);
-                R = __ffma2_rn(dZ, dZ, R);
-                const bool na = fabsf(R.x - c2) < band, nb2 = fabsf(R.y - c2) < band;
-                const bool ia = va && R.x < c2 && !na, ib = vb && R.y < c2 && !nb2;
-                float2 sig6, eps48;
-                if(kOneType) {
-                    sig6 = make_float2(a.lj.sig6f[0], a.lj.sig6f[0]);
-                    eps48 = make_float2(48.0f * a.lj.epsf[0], 48.0f * a.lj.epsf[0]);
-                } else {
-                    const int ta = ti + fj[u].w, tb = ti + fj[u + 1].w;
-                    sig6 = make_float2(a.lj.sig6f[ta], a.lj.sig6f[tb]);
-                    eps48 = make_float2(48.0f * a.lj.epsf[ta], 48.0f * a.lj.epsf[tb]);
-                }
-                const float2 S2 = make_float2(rcp_approx(R.x), rcp_approx(R.y));
-                const float2 S6 = __fmul2_rn(__fmul2_rn(S2, S2), __fmul2_rn(S2, sig6));
-                float2 F = __fmul2_rn(__fmul2_rn(S6, __fadd2_rn(S6, half2)), __fmul2_rn(S2, eps48));
-                F.x = ia ? F.x : 0.0f;
-                F.y = ib ? F.y : 0.0f;
-                FX = __ffma2_rn(dX, F, FX);
-                FY = __ffma2_rn(dY, F, FY);
-                FZ = __ffma2_rn(dZ, F, FZ);
-                if(kHalf) {
-                    const float2 nF = make_float2(-F.x, -F.y);
-                    const float2 rX = __fmul2_rn(dX, nF), rY = __fmul2_rn(dY, nF), rZ = __fmul2_rn(dZ, nF);
-                    if(ia && (cur[u] >> PG_NBR_INDEX_BITS) == 0u) {
-                        red_add_v4(a.p.force32 + 4 * (size_t) (cur[u] & PG_NBR_INDEX_MASK), rX.x, rY.x, rZ.x);
-                    }
-                    if(ib && (cur[u + 1] >> PG_NBR_INDEX_BITS) == 0u) {
-                        red_add_v4(a.p.force32 + 4 * (size_t) (cur[u + 1] & PG_NBR_INDEX_MASK), rX.y, rY.y, rZ.y);
-                    }
-                }
-                if(va && na) { pending |= 1u << u; }
-                if(vb && nb2) { pending |= 2u << u; }
-            }
-            if(pending != 0u) {
-#pragma unroll
-                for(int u = 0; u < kB; u++) {
-                    if(pending & (1u << u)) { cut_push(a, i, cur[u]); }
-                }
-            }
-#pragma unroll
-            for(int u = 0; u < kB; u++) { cur[u] = nxt[u]; }
-        }
-        fx = FX.x + FX.y; fy = FY.x + FY.y; fz = FZ.x + FZ.y;
+        f = packed_pairs<kHalf, kOneType, kB, false>(i, ld_i4(a.p.pos_fx, i), a.list.nbr + i, a.list.count[i],
+                                                      (size_t) a.list.stride, a.p.pos_fx, a.p.force32, a.box, a.lj,
+                                                      a.cut_count, a.cut_rec, a.cut_capacity);
     }
     if(kHalf) {
-        red_add_v4(a.p.force32 + 4 * (size_t) i, fx, fy, fz);
+        red_add_v4(a.p.force32 + 4 * (size_t) i, f.x, f.y, f.z);
     } else {
-        st_f4(a.p.force32, i, make_float4(fx, fy, fz, 0.0f));
+        st_f4(a.p.force32, i, make_float4(f.x, f.y, f.z, 0.0f));
     }
 }
 

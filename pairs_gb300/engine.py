@@ -26,6 +26,7 @@ import torch
 from . import _capi as A
 
 INT32_MAX = 2 ** 31 - 1
+BARRIER_TIMEOUT = 16                # pg_status.overflow bit 4 (pg_lj_steps)
 
 
 def _ptr(t):
@@ -52,7 +53,7 @@ class LJEngine:
                  dt=0.005, ntypes=1, epsilon=None, sigma6=None, precision="fp64", half=False,
                  sync="exact", every=20, neighbor_capacity=100, policy="fixed", device="cuda",
                  capacity=None, fused=True, tiles=None, tile_tpa=2, tile_atoms=224, cell_reach=1,
-                 cell_reach_x=None, fixed_point=None, graphs=True):
+                 cell_reach_x=None, fixed_point=None, graphs=True, persistent=None):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -69,6 +70,7 @@ class LJEngine:
         self.fused = fused
         self.graphs = bool(graphs)
         self._graphs = {}
+        self._deferred = []             # schedule bookkeeping run once the next chunk is queued
         self.graph_replays = 0
         self.graph_kernels = 0          # kernels run by graph replays
         self.graph_captured = 0         # kernels the library counted while capturing
@@ -253,6 +255,19 @@ class LJEngine:
         self.stream = torch.cuda.current_stream(self.dev)
         self.sh = C.c_void_p(self.stream.cuda_stream)
         A.call("pg_split_positions", C.byref(self.box), C.byref(self.p), self.sh)
+        # plain steps between rebuild points as one persistent launch (pg_lj_steps) in the
+        # graph chunks: mixed precision on fixed-point positions with global lists.
+        # Opt-in: at 1M atoms the chunk graph of separate kernels measured 0.345 ms/step
+        # against 0.397 for the persistent launch (three grid barriers per step, and far
+        # fewer loads in flight in its grid-stride phases than in a 1M-thread launch)
+        can_persist = self.precision == A.PG_MIXED and self.fixed_point and not self.tiles
+        if persistent and not can_persist:
+            raise ValueError("persistent steps need the mixed path with fixed-point positions and global lists")
+        self.persistent = bool(persistent) and can_persist
+        if self.persistent:
+            # queries the device once (outside any stream capture)
+            A.call("pg_lj_steps", C.byref(self.box), C.byref(self.p), C.byref(self.list), C.byref(self.lj), self.dt,
+                   self.half_skin2, 0, 0, self.status_ptr, self.ws, 0.0, self.sh)
         if self.speculative:
             self.p.guard = t["status"].data_ptr() + 4 * 4         # &status->guard_tripped
         if policy == "learned":
@@ -340,13 +355,14 @@ class LJEngine:
         if pre_bin is not None:
             pre_bin()
         st_dev = self.t["status"]
-        st_dev[0:3].zero_()                             # overflow, max_cell_count, max_neighbors
+        st_dev[0:1].bitwise_and_(BARRIER_TIMEOUT)       # overflow (a barrier timeout stays to be seen)
+        st_dev[1:3].zero_()                             # max_cell_count, max_neighbors
         A.call("pg_bin_particles", by(self.box), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
         guard = None
         first = True
         while True:
             if not first:
-                st_dev[0] = 0
+                st_dev[0:1].bitwise_and_(BARRIER_TIMEOUT)
                 st_dev[2] = 0
             first = False
             if self.tiles:
@@ -364,6 +380,8 @@ class LJEngine:
             guard = self._guard_abs(st.guard_tripped) if guard is None else guard
             if st.nonfinite:
                 raise A.PairsError("non-finite particle position met while binning")
+            if st.overflow & BARRIER_TIMEOUT:
+                raise A.PairsError("a grid barrier of the persistent steps ran out of time: the state is unfinished")
             if st.overflow & 4:
                 # a tile neighbourhood is larger than a block's shared memory: make
                 # tiles shorter, or give up tiles for this system
@@ -505,6 +523,23 @@ class LJEngine:
         if self.policy.startswith("interval:"):
             self.next_rebuild = ts + max(1, int(self.policy.split(":")[1]))
             return
+        if self.policy == "learned" and sch.trained and sch._next is not None:
+            # the new cycle's prediction came back with the rebuild's status: choose the
+            # next rebuild now, and leave the cycle bookkeeping (labels, calibration, the
+            # periodic training step) until the next chunk is queued on the GPU
+            raw, r = sch.raw_prediction()
+            self.next_rebuild = ts + max(1, int(math.floor(r * sch.margin)))
+            end = ts + 1 if tripped_at is None else None
+
+            def bookkeeping():
+                if ts > 0:
+                    sch.close_cycle(tripped_at, end)
+                sch.open_cycle(ts)
+                sch.note_prediction(raw)
+                sch.history.append((ts, r))
+
+            self._deferred.append(bookkeeping)
+            return
         if ts > 0:
             sch.close_cycle(tripped_at, ts + 1 if tripped_at is None else None)
         predicted = sch.trained and sch._next is not None
@@ -523,9 +558,14 @@ class LJEngine:
             sch.history.append((ts, r))
             self.next_rebuild = ts + max(1, int(math.floor(r * sch.margin)))
 
+    def _flush_deferred(self):
+        while self._deferred:
+            self._deferred.pop(0)()
+
     def step(self, thermo_every=0):
         """One iteration of the reference's time loop.  The final half step of a time
         step is deferred and fused with the next step's initial half step."""
+        self._flush_deferred()
         ts = self.ts
         self.p.step = self.device_step(ts)
         if ts > 0:
@@ -572,6 +612,7 @@ class LJEngine:
     def settle(self):
         """Speculative policies: make sure no guard trip is pending, so the state is
         the exact one at the current step (redo steps from a trip if needed)."""
+        self._flush_deferred()
         if not self.speculative or self.ts == 0:
             return
         target = self.ts
@@ -596,6 +637,7 @@ class LJEngine:
                 self._replay_plain(k)
             else:
                 self.step(thermo_every)
+        self._flush_deferred()
 
     # ------------------------------------------------------------------ CUDA graphs
 
@@ -616,6 +658,11 @@ class LJEngine:
         saved = self.sh
         self.sh = stream_handle
         try:
+            if self.persistent:
+                self.p.step = r0 + k - 1
+                A.call("pg_lj_steps", C.byref(self.box), C.byref(self.p), C.byref(self.list), C.byref(self.lj),
+                       self.dt, self.half_skin2, r0, k, self.status_ptr, self.ws, 0.0, self.sh)
+                return
             for r in range(r0, r0 + k):
                 self.p.step = r
                 if self.precision == A.PG_MIXED:
@@ -650,6 +697,7 @@ class LJEngine:
             self._graphs[(r0, k)] = entry
         with torch.cuda.stream(self.stream):
             entry[0].replay()
+        self._flush_deferred()                      # host bookkeeping while the chunk runs
         self.graph_replays += 1
         self.graph_kernels += entry[1]
         self.since_build += k

@@ -29,7 +29,7 @@ from . import _capi as A
 
 class LearnedSchedule:
     def __init__(self, engine, warmup_cycles=6, samples_per_cycle=4, margin=1.1, temperature=0.05, lr=3e-3,
-                 train_steps=300, seed=0, max_samples=64, top_cells=256, online_every=128, online_steps=1,
+                 train_steps=300, seed=0, max_samples=64, top_cells=256, online_every=32, online_steps=1,
                  online_recent=16):
         self.e = engine
         lib = A.load()
@@ -37,9 +37,16 @@ class LearnedSchedule:
         self.ncells_all = engine.cells.ncells
         self.ncells = min(top_cells, self.ncells_all)       # cells per sample: the fastest ones
         # one Adam step on the 16 newest samples every `online_every` cycles keeps the
-        # network following the run; each costs ~0.5 ms at 1M atoms, so every 128 cycles
-        # (every 32 cost 16 us per cycle, a quarter of the schedule's own work)
+        # network following the run (~0.5 ms at 1M atoms; every 128 cycles instead of 32
+        # left the first cycles' bias in place: 69 rebuilds in 400 steps against 61)
         self.online_every = online_every
+        # online calibration of the network's output: an average of log(observed /
+        # predicted) cycle length, added to every prediction, takes out what bias the
+        # training has not (the network is first trained on the run's first cycles)
+        self.calib_rate = 0.3
+        self.bias = 0.0
+        self._open_pred = None            # raw log prediction for the open cycle
+        self._open_start = None
         self.online_steps = online_steps
         self.online_recent = online_recent
         self.warmup_cycles = warmup_cycles
@@ -142,13 +149,44 @@ class LearnedSchedule:
         if self._next is not None:
             self.pending.append((self._next, step))
             self._next = None
+        self._open_start = step
+        self._open_pred = None
+
+    def _calibrated(self, raw_log):
+        self._open_pred = raw_log
+        return math.exp(raw_log + self.bias)
 
     def predicted(self):
         """Predicted steps of the new cycle (after the rebuild's status read)."""
-        return math.exp(float(self.result_host[0]))
+        return self._calibrated(float(self.result_host[0]))
+
+    def raw_prediction(self):
+        """The network's log prediction for the new cycle, as read with the rebuild's
+        status, and the calibrated number of steps (the bias as of the last closed
+        cycle).  note_prediction() later records it for the cycle's calibration."""
+        raw = float(self.result_host[0])
+        return raw, math.exp(raw + self.bias)
+
+    def note_prediction(self, raw_log):
+        self._open_pred = raw_log
+
+    def _calibrate(self, trip_step, end_step):
+        """Move the bias towards log(observed / predicted) of the cycle that closes: a
+        trip gives the length, a cycle ended before any trip only a lower bound (which
+        can raise the bias, never lower it)."""
+        if self._open_pred is None or self._open_start is None:
+            return
+        if trip_step is not None:
+            err = math.log(max(trip_step - self._open_start, 1)) - self._open_pred
+            self.bias += self.calib_rate * (err - self.bias)
+        else:
+            err = math.log(max(end_step - self._open_start, 1)) - self._open_pred
+            if err > self.bias:
+                self.bias += self.calib_rate * (err - self.bias)
 
     def close_cycle(self, trip_step, end_step):
         """Label the open cycle: tripped at trip_step (exact), or censored at end_step."""
+        self._calibrate(trip_step, end_step)
         for slot, step in self.pending:
             if trip_step is not None:
                 r = max(trip_step - step, 1)
@@ -193,7 +231,7 @@ class LearnedSchedule:
         slot = self._slot()
         self.features_into(slot)
         self.predict_log(slot)
-        return math.exp(float(self.result[0].item())), slot
+        return self._calibrated(float(self.result[0].item())), slot
 
 
 class EMASchedule:

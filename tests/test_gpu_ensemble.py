@@ -141,7 +141,10 @@ def test_guard_schedule_keeps_the_pair_set(half):
         sim = olj.Sim(dict(st, pos=pos, vel=vel), every=1, exact_sync=True)
         sim.step()
         _, _, f_ref = sim.state()
-        assert rms_rel(f, f_ref) < 1e-5
+        # a pair missing from the list would change a force by |F(rc)| = 0.039, ~2e-3
+        # of the RMS force; FP32 sums (reactions by atomics, in any order) stay within
+        # ~1.6e-5 of it at the largest (measured up to 1.6e-5 at 1M atoms)
+        assert rms_rel(f, f_ref) < 2e-5
 
 
 def test_thermo_matches_oracle_temperature():

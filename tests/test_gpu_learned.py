@@ -125,6 +125,35 @@ def test_learned_schedule_gain_over_guard_every_step():
     assert l["builds"] <= 1.6 * g["builds"], runs
 
 
+def test_learned_schedule_time_per_step_at_32cube():
+    """fcc 32^3, mixed precision, half lists, 400 timed steps after calibration (CUDA
+    events on the engine's stream).  What the learned schedule buys: no host read per
+    step (the guard policy reads the guard after every step and cannot replay chunks as
+    graphs), so it must be faster than the guard.  Against the EMA of past cycle lengths
+    (no GPU work at all), which predicts this stationary liquid's cycles as well, it
+    pays only its own per-cycle work and stays within a few percent."""
+    from pairs_gb300.engine import LJEngine
+    st = lattice.copper_fcc_lattice(32, 32, 32)
+    ms = {}
+    for policy in ("guard", "ema", "learned"):
+        eng = LJEngine(st, precision="mixed", half=True, sync="exact", policy=policy)
+        k = 0
+        while eng.schedule is not None and not eng.schedule.trained and k < 2000:
+            eng.step()
+            k += 1
+        eng.run(max(0, 150 - k))
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(eng.stream)
+        eng.run(400)
+        b.record(eng.stream)
+        torch.cuda.synchronize()
+        ms[policy] = a.elapsed_time(b) / 400
+        del eng
+    assert ms["learned"] < ms["guard"], ms
+    assert ms["learned"] < 1.10 * ms["ema"], ms
+
+
 @pytest.mark.parametrize("half", [True, False])
 def test_cell_features_match_a_host_computation(half):
     """pg_cell_features against numpy on the engine's own cells: per cell max|v| dt /
