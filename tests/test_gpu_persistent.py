@@ -60,7 +60,7 @@ def test_persistent_chunks_follow_the_separate_kernels(half, policy):
     assert np.abs(a["pos"] - b["pos"]).max() < tol
     assert np.abs(a["vel"] - b["vel"]).max() < tol * 100
     rms = np.sqrt((b["frc"] ** 2).mean())
-    assert np.abs(a["frc"] - b["frc"]).max() / rms < (1e-6 if not half else 1e-5)
+    assert np.abs(a["frc"] - b["frc"]).max() / rms < (1e-6 if not half else 5e-5)
     # one cooperative launch per replayed chunk, against four kernels per step
     assert a["kernels"] == a["replays"]
     assert b["kernels"] > 4 * b["replays"]
