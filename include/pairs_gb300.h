@@ -569,6 +569,26 @@ int pg_dem_force(const pg_box *box, const pg_dem_particles *d, const pg_cells *c
 int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, int precision, double half_skin2, int32_t step,
                  pg_status *status, void *stream);
 
+/* ---- VTK output (runtime/vtk.hpp:11-86, replaces the host loops of vtk_write_data) */
+
+/* Workspace of pg_vtk_format_rows / pg_vtk_pack_rows for `rows` rows: a 96-byte slot
+ * per row, then the int32 row lengths (the last 4 * rows bytes); -1 for rows < 0. */
+int64_t pg_vtk_workspace_bytes(int32_t rows);
+
+/* Formats row k of one section for particle order[k] (order NULL: k) into its slot and
+ * its length into the length array: section 0 "x y z\n" of pos[i] (double4) and section
+ * 2 "m\n" of mass[i], each number as printf("%.8f") prints it (exact conversion, ties to
+ * even); section 1 "1 index[k]\n" (index NULL: k).  A length of -1 marks a value that
+ * %.8f with at most 11 integer digits cannot hold (|x| >= 9.2e10, NaN, infinity).  The
+ * caller leaves infinite shapes out of `order` and gives in index[k] the row's index
+ * among all particles (vtk.hpp:36-40, 57-60). */
+int pg_vtk_format_rows(int section, int32_t rows, const int32_t *order, const double *pos, const double *mass,
+                       const int32_t *index, pg_workspace ws, void *stream);
+
+/* Copies the formatted rows to out + offsets[k] (offsets: the exclusive scan of the
+ * lengths, int64, device memory), giving the section's text. */
+int pg_vtk_pack_rows(int32_t rows, pg_workspace ws, const int64_t *offsets, char *out, void *stream);
+
 /* cudaStreamSynchronize, returning PG_OK or PG_ERR_CUDA. */
 int pg_stream_sync(void *stream);
 

@@ -142,6 +142,10 @@ SIGNATURES = {
     "pg_compute_thermo": (C.c_int, [P(PgBox), P(PgParticles), C.c_void_p, PgWorkspace, C.c_void_p]),
     "pg_split_positions": (C.c_int, [P(PgBox), P(PgParticles), C.c_void_p]),
     "pg_permute": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "pg_vtk_workspace_bytes": (C.c_int64, [C.c_int32]),
+    "pg_vtk_format_rows": (C.c_int, [C.c_int, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     PgWorkspace, C.c_void_p]),
+    "pg_vtk_pack_rows": (C.c_int, [C.c_int32, PgWorkspace, C.c_void_p, C.c_void_p, C.c_void_p]),
     "pg_stream_sync": (C.c_int, [C.c_void_p]),
     "pg_mlp_param_count": (C.c_int, []),
     "pg_cell_features": (C.c_int, [P(PgParticles), P(PgCells), C.c_int, C.c_int32, C.c_double, C.c_double,

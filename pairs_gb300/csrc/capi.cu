@@ -46,6 +46,10 @@ int lj_steps(const pg_box *box, pg_particles *p, const pg_neighbor_list *list, c
              double half_skin2, int32_t first, int32_t nsteps, pg_status *status, pg_workspace ws, double timeout_s,
              cudaStream_t st);
 int grid_barrier_check(int32_t extra_arrivals, double timeout_s, pg_status *status, pg_workspace ws, cudaStream_t st);
+int64_t vtk_workspace_bytes(int32_t rows);
+int vtk_format_rows(int what, int32_t rows, const int32_t *order, const double *pos, const double *mass,
+                    const int32_t *index, pg_workspace ws, cudaStream_t st);
+int vtk_pack_rows(int32_t rows, pg_workspace ws, const int64_t *offset, char *out, cudaStream_t st);
 int dem_setup(pg_dem_particles *d, const pg_dem_params *prm, cudaStream_t st);
 int dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
             const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, cudaStream_t st);
@@ -233,6 +237,17 @@ int pg_mlp_backward(const float *params, const float *features, const float *out
 int pg_mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, float beta1, float beta2,
                 float eps, int32_t t, float grad_scale, void *stream) {
     return pg::mlp_adam(params, grads, m1, m2, lr, beta1, beta2, eps, t, grad_scale, S(stream));
+}
+
+int64_t pg_vtk_workspace_bytes(int32_t rows) { return pg::vtk_workspace_bytes(rows); }
+
+int pg_vtk_format_rows(int section, int32_t rows, const int32_t *order, const double *pos, const double *mass,
+                       const int32_t *index, pg_workspace ws, void *stream) {
+    return pg::vtk_format_rows(section, rows, order, pos, mass, index, ws, S(stream));
+}
+
+int pg_vtk_pack_rows(int32_t rows, pg_workspace ws, const int64_t *offsets, char *out, void *stream) {
+    return pg::vtk_pack_rows(rows, ws, offsets, out, S(stream));
 }
 
 int pg_stream_sync(void *stream) {

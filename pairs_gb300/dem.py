@@ -507,6 +507,11 @@ class DEMEngine:
 
     # ------------------------------------------------------------------ readout
 
+    def vtk_fields(self):
+        """Device tensors (pos n x 4, mass, flags, uid) for the device VTK writer."""
+        cur = lambda k: (self.t[k] if k in self.t else self.sets[0][k])[:self.n]
+        return cur("pos"), cur("mass"), cur("flags"), cur("uid")
+
     def _host(self, name, width=None):
         src = self.t[name] if name in self.t else self.sets[0][name]
         a = src[:self.n].cpu().numpy()

@@ -740,6 +740,14 @@ class LJEngine:
             frc = self.t["force32"][:n, :3].cpu().numpy().astype(np.float64)[order]
         return pos, vel, frc
 
+    def vtk_fields(self):
+        """Device tensors (pos n x 4, mass, flags, uid) of the state at the current
+        step, for the device VTK writer."""
+        self.settle()
+        self.flush()
+        n, t = self.n, self.t
+        return t["pos"][:n], t["mass"][:n], t["flags"][:n], t["uid"][:n]
+
     def _uid_order(self):
         uid = self.t["uid"][: self.n].cpu().numpy()
         return np.argsort(uid, kind="stable")

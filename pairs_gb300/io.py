@@ -8,8 +8,13 @@ read_particle_data  runtime/read_from_file.hpp:121-203: CSV, one particle per li
                     infinite, fixed or global; its shape is set to `shape_id`.
 write_vtk           runtime/vtk.hpp:11-86: legacy VTK ASCII unstructured grid of the
                     positions (vertices) with the mass as point data, 8 decimals,
-                    infinite particles left out, file <name>_<timestep>.vtk.
+                    infinite particles left out, file <name>_<timestep>.vtk.  The rows
+                    are formatted on the device (pg_vtk_format_rows / pg_vtk_pack_rows)
+                    and only the text comes back; format_vtk is the host restatement
+                    the device text is tested against.
 """
+import ctypes as C
+
 import numpy as np
 
 from .types import Flags, Types
@@ -89,17 +94,20 @@ def read_particle_data(sim, filename, prop_names, shape_id):
 
 
 def format_vtk(pos, mass, flags=None):
-    """Legacy VTK text of the particles (vtk.hpp:11-86 layout)."""
+    """Legacy VTK text of the particles (vtk.hpp:11-86 layout): infinite particles left
+    out, CELLS rows "1 i" with i the particle's index among all particles
+    (vtk.hpp:57-60 writes i - start, so an infinite particle leaves a gap)."""
     keep = np.ones(len(pos), dtype=bool) if flags is None else (np.asarray(flags) & Flags.Infinite) == 0
     p = np.asarray(pos)[keep]
     m = np.asarray(mass)[keep]
+    idx = np.nonzero(keep)[0]
     n = len(p)
     out = ["# vtk DataFile Version 2.0\n", "Particle data\n", "ASCII\n", "DATASET UNSTRUCTURED_GRID\n",
            f"POINTS {n} double\n"]
     out += ["%.8f %.8f %.8f\n" % tuple(r) for r in p]
     out.append("\n\n")
     out.append(f"CELLS {n} {n * 2}\n")
-    out += [f"1 {k}\n" for k in range(n)]
+    out += [f"1 {k}\n" for k in idx]
     out.append("\n\n")
     out.append(f"CELL_TYPES {n}\n")
     out += ["1\n"] * n
@@ -110,11 +118,61 @@ def format_vtk(pos, mass, flags=None):
     return "".join(out)
 
 
+def device_vtk_text(pos, mass, flags=None, uid=None):
+    """The text of format_vtk, formatted on the device from device tensors: pos
+    (n x 4 FP64), mass (n, FP64), flags (n, int32; infinite particles left out) and
+    uid (n, int32; rows in uid order, as the host arrays of engine.state()).  One
+    thread formats one row into a fixed-width slot, a scan of the row lengths gives
+    the offsets and a second kernel packs the rows; the host adds the header lines.
+    Returns bytes; raises PairsError for a value that %.8f cannot hold (|x| >= 9.2e10,
+    NaN, infinity)."""
+    import torch
+    from . import _capi as A
+    lib = A.load()
+    dev = pos.device
+    n = pos.shape[0]
+    order = torch.argsort(uid.long(), stable=True) if uid is not None else torch.arange(n, device=dev)
+    index = torch.arange(n, dtype=torch.int32, device=dev)     # row k's index among all particles
+    if flags is not None:
+        keep = (flags[order] & int(Flags.Infinite)) == 0
+        order, index = order[keep], index[keep]
+    order = order.to(torch.int32).contiguous()
+    index = index.contiguous()
+    rows = int(order.numel())
+    pos, mass = pos.contiguous(), mass.to(torch.float64).contiguous()
+    wsb = int(lib.pg_vtk_workspace_bytes(rows))
+    ws = torch.empty(max(wsb, 16), dtype=torch.uint8, device=dev)
+    w = A.PgWorkspace(ws.data_ptr(), ws.numel())
+    lens = ws[wsb - 4 * rows: wsb].view(torch.int32)    # the row lengths end the workspace
+    sh = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    ptr = lambda x: C.c_void_p(x.data_ptr())
+
+    def section(what):
+        if rows == 0:
+            return b""
+        A.call("pg_vtk_format_rows", what, rows, ptr(order), ptr(pos), ptr(mass), ptr(index), w, sh)
+        ln = lens.to(torch.int64)
+        if bool((ln < 0).any()):
+            raise A.PairsError("VTK output: a position or mass outside the range of %.8f")
+        off = torch.cumsum(ln, 0) - ln
+        total = int(ln.sum())
+        out = torch.empty(total, dtype=torch.uint8, device=dev)
+        A.call("pg_vtk_pack_rows", rows, w, ptr(off), ptr(out), sh)
+        return out.cpu().numpy().tobytes()
+
+    head = (b"# vtk DataFile Version 2.0\nParticle data\nASCII\nDATASET UNSTRUCTURED_GRID\n"
+            + f"POINTS {rows} double\n".encode())
+    parts = [head, section(0), b"\n\n", f"CELLS {rows} {rows * 2}\n".encode(), section(1), b"\n\n",
+             f"CELL_TYPES {rows}\n".encode(), b"1\n" * rows, b"\n\n",
+             f"POINT_DATA {rows}\nSCALARS mass double\nLOOKUP_TABLE default\n".encode(), section(2), b"\n\n"]
+    return b"".join(parts)
+
+
 def write_vtk(sim, engine, timestep):
-    st = engine.state()
-    if isinstance(st, dict):                      # DEM engine: arrays by name
-        pos, mass, flags = st["pos"], st["mass"], st["flags"]
-    else:
-        pos, mass, flags = st[0], engine.masses(), engine.flags()
-    with open(f"{sim.vtk_file}_{timestep}.vtk", "w") as f:
-        f.write(format_vtk(pos, mass, flags))
+    """<file>_local_<timestep>.vtk, the reference's file of the local particles
+    (sim/vtk.py:20).  Its second file, <file>_ghost_<timestep>.vtk, lists the copies its
+    border exchange made; this engine makes none (periodic images are formed inside the
+    pair kernels), so that file is not written."""
+    pos, mass, flags, uid = engine.vtk_fields()
+    with open(f"{sim.vtk_file}_local_{timestep}.vtk", "wb") as f:
+        f.write(device_vtk_text(pos, mass, flags, uid))

@@ -329,12 +329,21 @@ class Simulation:
         return eng
 
     def _run_dem(self, eng, nsteps):
-        """DEM time loop: the engine advances in chunks between VTK frames."""
+        """DEM time loop: the engine advances in chunks between VTK frames.  The frame of
+        step ts is written after that step, at the end of the time-step body
+        (sim/simulation.py:422-423)."""
         from .io import write_vtk
-        freq = self.vtk_frequency if self.vtk_file is not None else 0
+        vtk = self.vtk_file is not None
+        freq = self.vtk_frequency if vtk else 0
         while eng.ts < nsteps:
-            if self.vtk_file is not None and (freq == 0 or eng.ts % freq == 0):
-                write_vtk(self, eng, eng.ts)
-            nxt = nsteps if not freq else min(nsteps, (eng.ts // freq + 1) * freq)
-            eng.run(nxt - eng.ts)
+            if not vtk:
+                end = nsteps
+            elif freq == 0:
+                end = eng.ts + 1
+            else:
+                end = min(nsteps, -(-eng.ts // freq) * freq + 1)   # just past the next frame step
+            eng.run(end - eng.ts)
+            ts = eng.ts - 1
+            if vtk and (freq == 0 or ts % freq == 0):
+                write_vtk(self, eng, ts)
         return eng

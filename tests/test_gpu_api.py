@@ -47,8 +47,8 @@ def test_vtk_output(tmp_path):
     psim.vtk_output(str(tmp_path / "md"), frequency=5)
     psim.run(verbose=False)
     files = sorted(os.listdir(tmp_path))
-    assert files == ["md_0.vtk", "md_10.vtk", "md_5.vtk"]
-    txt = open(tmp_path / "md_5.vtk").read()
+    assert files == ["md_local_0.vtk", "md_local_10.vtk", "md_local_5.vtk"]
+    txt = open(tmp_path / "md_local_5.vtk").read()
     assert "POINTS 256 double" in txt
 
 
