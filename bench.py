@@ -137,7 +137,9 @@ def run_ours(args, rank, world, dist):
     def make(precision, half, policy):
         return LJEngine(st, precision=precision, half=half, sync="exact", every=20, policy=policy,
                         device=str(dev), tiles=tiles if precision == "mixed" else None, tile_tpa=args.tile_tpa,
-                        fixed_point={"auto": None, "on": True, "off": False}[args.fixed_point])
+                        fixed_point={"auto": None, "on": True, "off": False}[args.fixed_point],
+                        pair_lists={"auto": None, "on": True, "off": False}[args.pair_lists]
+                        if precision == "mixed" and half else None)
 
     def kernel_times(eng, k):
         stream = eng.stream
@@ -218,7 +220,23 @@ def run_ours(args, rank, world, dist):
     # state (same stream, CUDA events around each launch)
     eng.settle()
     fms = kernel_times(eng, 20)
-    pairs_total = int(eng.t["count"][:n].sum().item())
+    pairs_total, entries_total = eng.list_size()
+
+    def build_times(eng, k):
+        """The Verlet build alone (the last binning's cells, current positions), CUDA
+        events around each call; the list it leaves is valid for these positions."""
+        out = []
+        for _ in range(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(eng.stream)
+            A.call("pg_build_neighbor_lists", C.byref(eng.box), C.byref(eng.p), C.byref(eng.cells),
+                   C.byref(eng.list), eng.r_list2, eng.status_ptr, eng.sh)
+            b.record(eng.stream)
+            out.append((a, b))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in out[1:]]
+
+    build_ms = statistics.median(build_times(eng, 6))
     # algorithmic bytes of one force launch: own position (16 fixed point, 32 FP32 hi+lo
     # or FP64 x,y,z,pad), neighbour count (4), force write (16 FP32 / 32 FP64), one Verlet
     # entry per pair (4 bytes global, 2 bytes tile-local); a half list adds one
@@ -227,9 +245,12 @@ def run_ours(args, rank, world, dist):
     b_entry = 2 if eng.list.nbr16 else 4
     b_pos = 16 if (prec == "mixed" and eng.fixed_point) else 32     # fixed point: one int4
     b_force = n * (b_pos + 4 + b_f) + b_entry * pairs_total + (n * b_f if eng.list.half else 0)
-    # the mixed path's force pass: packed pair arithmetic on fixed-point positions
-    # (k_lj_packed), one pair at a time on compensated positions (k_lj_mixed)
-    kname = ("k_tile_lj" if eng.list.nbr16 else
+    # (pairs_total: the Verlet pairs; a pair-cluster list holds them in fewer entries,
+    # entries_total, whose bytes are reported beside as list_bytes)
+    # the mixed path's force pass: pair-cluster lists (k_pc_lj), packed pair arithmetic
+    # on fixed-point positions (k_lj_packed), one pair at a time on compensated
+    # positions (k_lj_mixed)
+    kname = ("k_tile_lj" if eng.list.nbr16 else "k_pc_lj" if eng.pair_lists else
              (("k_lj_packed" if eng.fixed_point else "k_lj_mixed") if prec == "mixed" else "k_lj_fp64"))
     f_avg = statistics.mean(fms) if fms else float("nan")
     pk, pk_kind = peaks()
@@ -238,7 +259,9 @@ def run_ours(args, rank, world, dist):
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_kind": pk_kind,
                 "traffic": traffic, "kernel": "%s (%s)" % (kname, args.variant),
-                "kernel_ms": round(f_avg, 4), "algorithmic_bytes": b_force, "list_entries": pairs_total}
+                "kernel_ms": round(f_avg, 4), "algorithmic_bytes": b_force, "list_pairs": pairs_total,
+                "list_entries": entries_total, "list_bytes": b_entry * entries_total,
+                "build_ms": round(build_ms, 4)}
     if traffic is not None and traffic_atoms != n:
         roofline["traffic_scaled_from_atoms"] = traffic_atoms
     schedule = dict(counters, policy=args.policy, calibration_steps=calib_steps,
@@ -380,7 +403,8 @@ def run_ours(args, rank, world, dist):
                                f"rc 2.5, skin 0.3, dt 0.005, {args.variant}, rebuild policy {args.policy} "
                                "(exact FP64 displacement guard)",
                    "atoms": n, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (Verlet list %.0f MB)" % (pairs_total * 4 / 1e6)},
+                   "l2": "inputs larger than L2 (per step: Verlet list %.0f MB, FP64 positions and "
+                         "velocities %.0f MB)" % (b_entry * entries_total / 1e6, 64 * n / 1e6)},
         "roofline": roofline, "schedule": schedule,
         "energy_drift_1000": {"headline": drift_headline, "fp64_guard": drift64, "steps": args.drift_steps},
         "force_error_vs_fp64": ferr,
@@ -674,6 +698,8 @@ def main():
                     help="mixed path, full lists: 16-bit shared-memory tile lists or global lists (auto = off)")
     ap.add_argument("--tile-tpa", type=int, default=2, choices=[1, 2, 4],
                     help="threads per atom of the tile force kernel")
+    ap.add_argument("--pair-lists", choices=["auto", "on", "off"], default="auto",
+                    help="pair-cluster half lists on the mixed fixed-point path (auto: the engine's default)")
     ap.add_argument("--fixed-point", choices=["auto", "on", "off"], default="auto",
                     help="FP32 position layout: fixed point (2^32 units per box length, one 16-byte record "
                          "per partner) or compensated hi/lo pairs (auto = fixed point where the box allows)")

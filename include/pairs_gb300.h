@@ -173,6 +173,7 @@ typedef struct {
     int32_t *tile_table;         /* [ntiles * PG_TILE_RECORD_WORDS] */
     int32_t tile_tpa;            /* threads per particle in the tile force kernel: 1, 2, 4 */
     int32_t pad_;
+    int32_t *pair_table;         /* [stride] or NULL: pair-cluster half lists (below) */
 } pg_neighbor_list;
 
 /* Lennard-Jones parameters per type pair (examples/md.py:5-8, feature tables). */
@@ -310,8 +311,8 @@ int64_t pg_workspace_bytes(int32_t n, int32_t ncells);
 
 /* Wrap particles that left a periodic box back in (x < lo -> x + len, x > hi ->
  * x - len, as the reference's exchange, sim/comm.py:101-151), bin them into the
- * cell grid, and permute every per-particle array into cell order (stable within a
- * cell by uid).  Replaces build_cell_lists + partition_cell_lists
+ * cell grid, and permute every per-particle array into cell order (within a cell by
+ * z, then uid; cells are numbered z fastest, so each z column of cells is sorted by z).  Replaces build_cell_lists + partition_cell_lists
  * (sim/cell_lists.py:90-171) and the exchange half of the halo code.
  * The grid must have dims[d] >= 1 and a positive, finite cell_len[d] on every axis
  * and ncells = dims[0]*dims[1]*dims[2]; anything else returns PG_ERR_ARGUMENT before
@@ -353,7 +354,19 @@ int pg_bin_particles_noalloc(const pg_box *box, pg_particles *p, pg_cells *cells
  * fl(x_j + s*len), delta, (dx*dx + dy*dy) + dz*dz, no fused multiply-add.  Also
  * records pos_ref (and ref_hi/ref_lo or ref_fx) for the displacement guard.  The FP32
  * screen reads pos_fx when it is set and the box allows it (every axis periodic with
- * at least 2 reach + 2 cells), else pos_hi/pos_lo. */
+ * at least 2 reach + 2 cells), else pos_hi/pos_lo.
+ *
+ * Pair-cluster half lists (list->pair_table not NULL; half lists on fixed-point
+ * positions, PG_MIXED forces): the list is kept per cluster of two consecutive
+ * particles of one cell (the last particle of an odd cell alone).  pair_table[t] of
+ * cluster slot t is the first particle's index, bit 30 set when particle index + 1 is
+ * the second member, or -1 for a free slot; stride must be at least
+ * pg_pair_slots(n, ncells).  nbr[k * stride + t] is the partner index in bits 0-29,
+ * bit 30 set when the pair (first member, partner) is stored, bit 31 for the second
+ * member; count[t] entries.  The pair set is the per-particle half list's, each pair
+ * stored once by the member whose partner lies above it in x (minimum image; pairs
+ * through a periodic image too), and the force applies every pair's reaction. */
+int64_t pg_pair_slots(int32_t n, int32_t ncells);
 int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                             pg_neighbor_list *list, double r_list2, pg_status *status,
                             void *stream);
@@ -372,7 +385,10 @@ int pg_build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_c
  * with half lists), so 256 + 8 * ceil(0.004 * n) bytes leaves a wide margin, and
  * pg_workspace_bytes(n, ncells) always does.  A queue that overflows loses no
  * force: the second kernel then walks every list again for the band's pairs, which
- * costs about one more force pass. */
+ * costs about one more force pass.  Pair-cluster lists (list->pair_table, see
+ * pg_build_neighbor_lists) take the mixed path on fixed-point positions with a half
+ * list; one thread walks a cluster's list and computes both members' pairs in the two
+ * lanes of packed FP32 instructions. */
 int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
                 const pg_neighbor_list *list, const pg_lj_params *lj, int precision, int sync_mode,
                 double *energy, pg_workspace ws, void *stream);
@@ -385,7 +401,7 @@ int pg_lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells,
  * per-module kernel launches and device synchronisations of the reference's
  * generated time loop (src/pairs/code_gen/cgen.py:540-576) for the steps between two
  * list rebuilds.  Needs fixed-point positions (pos_fx, ref_fx), force32, global
- * lists.  The guard keeps its meaning: a trip in the integration of step r ends the
+ * per-particle lists (no tile or pair-cluster lists).  The guard keeps its meaning: a trip in the integration of step r ends the
  * launch before the force of step r (status->guard_tripped = r), as the separate
  * kernels would skip themselves.  ws: scratch as for pg_lj_force (its first 256
  * bytes hold the queue count and the barrier words).  No barrier waits longer than

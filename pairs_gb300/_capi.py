@@ -62,7 +62,8 @@ class PgNeighborList(C.Structure):
     _fields_ = [("stride", C.c_int32), ("max_neighbors", C.c_int32), ("half", C.c_int32),
                 ("nbr", C.c_void_p), ("count", C.c_void_p), ("steps_since_build", C.c_int32),
                 ("nbr16", C.c_void_p), ("tile_z", C.c_int32), ("tile_capacity", C.c_int32),
-                ("tile_table", C.c_void_p), ("tile_tpa", C.c_int32), ("pad_", C.c_int32)]
+                ("tile_table", C.c_void_p), ("tile_tpa", C.c_int32), ("pad_", C.c_int32),
+                ("pair_table", C.c_void_p)]
 
 
 TILE_RECORD_WORDS = 180
@@ -142,6 +143,7 @@ SIGNATURES = {
     "pg_compute_thermo": (C.c_int, [P(PgBox), P(PgParticles), C.c_void_p, PgWorkspace, C.c_void_p]),
     "pg_split_positions": (C.c_int, [P(PgBox), P(PgParticles), C.c_void_p]),
     "pg_permute": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "pg_pair_slots": (C.c_int64, [C.c_int32, C.c_int32]),
     "pg_vtk_workspace_bytes": (C.c_int64, [C.c_int32]),
     "pg_vtk_format_rows": (C.c_int, [C.c_int, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      PgWorkspace, C.c_void_p]),

@@ -46,6 +46,7 @@ int lj_steps(const pg_box *box, pg_particles *p, const pg_neighbor_list *list, c
              double half_skin2, int32_t first, int32_t nsteps, pg_status *status, pg_workspace ws, double timeout_s,
              cudaStream_t st);
 int grid_barrier_check(int32_t extra_arrivals, double timeout_s, pg_status *status, pg_workspace ws, cudaStream_t st);
+int64_t pair_slots(int32_t n, int32_t ncells);
 int64_t vtk_workspace_bytes(int32_t rows);
 int vtk_format_rows(int what, int32_t rows, const int32_t *order, const double *pos, const double *mass,
                     const int32_t *index, pg_workspace ws, cudaStream_t st);
@@ -238,6 +239,8 @@ int pg_mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, flo
                 float eps, int32_t t, float grad_scale, void *stream) {
     return pg::mlp_adam(params, grads, m1, m2, lr, beta1, beta2, eps, t, grad_scale, S(stream));
 }
+
+int64_t pg_pair_slots(int32_t n, int32_t ncells) { return pg::pair_slots(n, ncells); }
 
 int64_t pg_vtk_workspace_bytes(int32_t rows) { return pg::vtk_workspace_bytes(rows); }
 

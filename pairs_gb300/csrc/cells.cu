@@ -134,10 +134,16 @@ __global__ void k_scatter(int n, const int32_t *particle_cell, const int32_t *st
     perm[start[c] + atomicAdd(&cursor[c], 1)] = i;
 }
 
-// Order each cell's particles by uid (insertion sort; cells hold ~20 particles),
-// so the result does not depend on the atomic order of the scatter.
+// Order each cell's particles by z, then uid (insertion sort; cells hold ~10-20
+// particles), so the result does not depend on the atomic order of the scatter.  The
+// cells of a z column are consecutive, so a column's particles are then sorted by z
+// as a whole: the list builds take the candidates of a column within a z window.
+__device__ __forceinline__ bool z_uid_less(double za, int ua, double zb, int ub) {
+    return za < zb || (za == zb && ua < ub);
+}
+
 __global__ void k_sort_cells(int ncells_total, const int32_t *start, int32_t *perm,
-                             const int32_t *uid, pg_status *status) {
+                             const int32_t *uid, const double *pos, pg_status *status) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     int cnt = 0;
     if(c < ncells_total) {
@@ -146,8 +152,14 @@ __global__ void k_sort_cells(int ncells_total, const int32_t *start, int32_t *pe
         for(int k = b + 1; k < e; k++) {
             const int v = perm[k];
             const int key = uid[v];
+            const double z = pos[4 * (size_t) v + 2];
             int m = k - 1;
-            while(m >= b && uid[perm[m]] > key) { perm[m + 1] = perm[m]; m--; }
+            while(m >= b) {
+                const int w = perm[m];
+                if(!z_uid_less(z, key, pos[4 * (size_t) w + 2], uid[w])) { break; }
+                perm[m + 1] = w;
+                m--;
+            }
             perm[m + 1] = v;
         }
     }
@@ -323,7 +335,8 @@ int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_c
     if(n == 0) { return launch_status(); }
     k_scatter<<<blocks_for(n), kBlock, 0, st>>>(n, cells->particle_cell, w.start, w.cursor, w.perm); note_launch();
     if(p->uid != nullptr) {
-        k_sort_cells<<<blocks_for(ntot), kBlock, 0, st>>>(ntot, w.start, w.perm, p->uid, status); note_launch();
+        k_sort_cells<<<blocks_for(ntot), kBlock, 0, st>>>(ntot, w.start, w.perm, p->uid, p->pos, status);
+        note_launch();
     }
     const StageView v = stage_view(w.stage, n);
     k_gather_all<<<blocks_for(n), kBlock, 0, st>>>(n, w.perm, *p, cells->particle_cell, v); note_launch();

@@ -423,6 +423,8 @@ constexpr int kFixupBlocks = 2 * kSMs;
 
 int tile_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list, const pg_cells *cells,
                   const LJTableF &lj, double *energy, cudaStream_t st);
+int pc_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list, const LJTable &lj,
+                double *energy, int32_t *cut_count, int2 *cut_rec, int cut_capacity, cudaStream_t st);
 
 int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, const pg_neighbor_list *list,
              const pg_lj_params *lj, int precision, int sync_mode, double *energy, pg_workspace ws, cudaStream_t st) {
@@ -453,6 +455,8 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, co
     }
     const bool half = list->half != 0, one = lj->ntypes == 1, en = energy != nullptr;
     const bool tile = precision == PG_MIXED && list->nbr16 != nullptr;
+    const bool pairs = list->pair_table != nullptr;
+    if(pairs && (precision != PG_MIXED || !fixed_point || !half || tile)) { return PG_ERR_ARGUMENT; }
     if(tile && (!cells || !p->pos_hi || !p->pos_lo)) { return PG_ERR_ARGUMENT; }
     if(!tile && !list->nbr) { return PG_ERR_ARGUMENT; }
     if(en) { cudaMemsetAsync(energy, 0, 2 * sizeof(double), st); }
@@ -481,6 +485,7 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, co
         pick_fp64(half, one, en)<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch();
         return launch_status();
     }
+    if(pairs) { return pc_lj_force(box, p, list, a.lj, energy, a.cut_count, a.cut_rec, a.cut_capacity, st); }
     const MixedKernels k = pick_mixed(half, one, en, fixed_point);
     k.main<<<blocks_for(p->n, k.block), k.block, 0, st>>>(a); note_launch();
     k.fixup<<<kFixupBlocks, kBlock, 0, st>>>(a); note_launch();

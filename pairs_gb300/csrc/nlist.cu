@@ -166,7 +166,7 @@ static int axis_reach(const pg_cells *cells, int d) {
 }
 
 // the fixed-point screen is exact for every candidate (see k_build_list)
-static bool fixed_point_screen(const pg_box *box, const pg_particles *p, const pg_cells *cells) {
+bool fixed_point_screen(const pg_box *box, const pg_particles *p, const pg_cells *cells) {
     if(p->pos_fx == nullptr || p->ref_fx == nullptr) { return false; }
     for(int d = 0; d < 3; d++) {
         // a candidate lies within reach + 1 cells of the particle: below half a box
@@ -177,6 +177,8 @@ static bool fixed_point_screen(const pg_box *box, const pg_particles *p, const p
 
 int tile_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                double r_list2, pg_status *status, cudaStream_t st);
+int pc_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list, double r_list2,
+             pg_status *status, cudaStream_t st);
 bool grid_ok(const pg_cells *cells);
 
 int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cells *cells,
@@ -187,7 +189,9 @@ int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cell
     if(!p->pos || (!fx && (!p->pos_hi || !p->pos_lo)) || !p->pos_ref || !list->nbr || !list->count) {
         return PG_ERR_ARGUMENT;
     }
-    if(list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS)) { return PG_ERR_ARGUMENT; }
+    if(list->pair_table == nullptr && (list->stride < p->n || p->n >= (1 << PG_NBR_INDEX_BITS))) {
+        return PG_ERR_ARGUMENT;
+    }
     if(cells->reach > 2 || cells->reach_x < 0 || cells->reach_x > 2) { return PG_ERR_ARGUMENT; }
     for(int d = 0; d < 3; d++) {
         const int rr = axis_reach(cells, d);
@@ -197,6 +201,10 @@ int build_neighbor_lists(const pg_box *box, const pg_particles *p, const pg_cell
         // the periodic box must exceed r_list (2 r_list along an axis of reach 2, whose
         // offsets would otherwise reach the same image twice)
         if(box->periodic[d] && box->len[d] * box->len[d] <= (rr == 1 ? 1.0 : 4.0) * r_list2) { return PG_ERR_ARGUMENT; }
+    }
+    if(list->pair_table != nullptr) {
+        list->steps_since_build = 0;
+        return pc_build(box, p, cells, list, r_list2, status, st);
     }
     ListArgs a;
     a.box = *box; a.p = *p; a.cells = *cells; a.list = *list; a.r_list2 = r_list2;

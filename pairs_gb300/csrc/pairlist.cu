@@ -1,0 +1,468 @@
+// Pair-cluster half lists: the mixed path's Verlet list and LJ force on fixed-point
+// positions, with the list walked by pairs of particles.
+//
+// The per-particle half list (nlist.cu, lj.cu) spends its time in the L1 data pipe:
+// every entry is one scattered 16-byte partner gather and, inside the cutoff, one
+// scattered 16-byte reaction reduction.  Two particles of the same cell have nearly the
+// same neighbourhood (the union of two r_list spheres 1 sigma apart is 1.27 spheres), so
+// here the two share one list: a cluster is a pair of consecutive particles of one cell
+// (a, b = a + 1; the last particle of an odd cell alone), and each entry of the
+// cluster's list is a partner j with one bit per member saying whether that member
+// stores the pair (j, member).  Per entry the partner is gathered once and one reaction
+// reduction carries the sum of both members' pair forces; the two members' pair
+// arithmetic is the two lanes of Blackwell's packed f32x2 instructions.
+//
+// The pair set is the reference's (sim/neighbor_lists.py:21-48): a pair of particles
+// closer than r_list, decided by the same FP32 screen and FP64 band test as the
+// per-particle build (nlist.cu), each pair stored once.  Which member stores a pair is
+// geometric: the one whose partner lies above it in x (minimum-image separation; ties
+// y, z, index).  Pairs through a periodic image follow the same rule, so every pair,
+// image or not, is stored once and applies its reaction (the reference computes an
+// image pair from both sides with no reaction, sim/interaction.py:107-113; the force
+// on each particle is the same sum).  Stored above means the stencil is the cells at
+// 0..reach_x cells above in x (half-width x cells), 3 x 3 in y and z.
+//
+// Cluster slots need no scan: cell c with first particle s_c and n_c particles owns
+// slots ceil((s_c + c) / 2) + m, m < ceil(n_c / 2).  Consecutive cells' slot ranges are
+// disjoint (the base grows by at least ceil(n_c / 2) from one cell to the next), and
+// at most (n + ncells) / 2 + 2 slots are used; free slots hold -1.
+#include <math.h>
+
+#include "common.cuh"
+#include "lj_packed.cuh"
+
+namespace pg {
+
+constexpr int32_t kPcHasB = 1 << 30;                 // table record: a second member
+constexpr uint32_t kPcIndexMask = (1u << 30) - 1u;   // table record / entry: particle index
+constexpr uint32_t kPcMaskA = 1u << 30;              // entry: the pair (j, first member)
+constexpr uint32_t kPcMaskB = 1u << 31;              // entry: the pair (j, second member)
+constexpr float kPcScreenBand = 1.0e-4f;             // the build's FP64 band (as nlist.cu)
+constexpr int kPcBlock = 128;
+constexpr int kPcBatch = 4;
+
+int64_t pair_slots(int32_t n, int32_t ncells) {
+    return n < 0 || ncells < 0 ? -1 : ((int64_t) n + ncells) / 2 + 2;
+}
+
+// ------------------------------------------------------------------ cluster table
+
+__global__ void k_pc_table(pg_cells cells, int32_t *table) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if(c >= cells.ncells) { return; }
+    const int s = cells.cell_start[c], n = cells.cell_count[c];
+    const int base = (int) (((int64_t) s + c + 1) >> 1);
+    for(int m = 0; 2 * m < n; m++) {
+        table[base + m] = (s + 2 * m) | (2 * m + 1 < n ? kPcHasB : 0);
+    }
+}
+
+// ------------------------------------------------------------------ build
+
+struct PcBuildArgs {
+    pg_box box;
+    pg_particles p;
+    pg_cells cells;
+    pg_neighbor_list list;
+    double r_list2;
+    float r2_lo, r2_hi;          // screening band, box units squared when kCubic
+};
+
+// The FP64 decision of a candidate in the screening band: the reference's separately
+// rounded rsq to the stencil's image of the partner (as nlist.cu).
+__device__ __noinline__ bool pc_exact(const PcBuildArgs &a, int i, int j, int sx, int sy, int sz) {
+    const D4 xi = ld_d4_rare(a.p.pos, i), xj = ld_d4_rare(a.p.pos, j);
+    const double dx = __dsub_rn(xi.x, ref_image(xj.x, sx, a.box.len[0]));
+    const double dy = __dsub_rn(xi.y, ref_image(xj.y, sy, a.box.len[1]));
+    const double dz = __dsub_rn(xi.z, ref_image(xj.z, sz, a.box.len[2]));
+    return ref_rsq(dx, dy, dz) < a.r_list2;
+}
+
+// Fixed-point z of particle j as an ordering key along its cell column: the coordinate
+// in units (0 .. 2^32), except in the column's top cell, where a particle rounded onto
+// the box's upper face (z_fx = 2^32 mod 2^32 = 0) counts as 2^32, so that the keys of
+// a column's particles, sorted by z within each cell (pg_bin_particles), ascend.
+__device__ __forceinline__ int64_t z_key(uint32_t zfx, bool top_cell) {
+    return (int64_t) zfx + (top_cell && zfx < 0x80000000u ? (int64_t) 1 << 32 : 0);
+}
+
+// One thread per cluster slot: both members' candidates from the stencil of their
+// cell, one list entry per partner stored by either member.  Also records the guard's
+// reference positions of the members.
+//
+// The stencil is walked by z columns: cells (cx + ox, cy + oy, cz - reach .. cz +
+// reach) are one contiguous range of particles sorted by z (or two or three ranges
+// where the column wraps around a periodic z face, each with its image shift).  A
+// partner within r_list lies within r_list in z, so each range is entered at the
+// first particle of the window [z_min - r_list, z_max + r_list] of the two members and
+// left at its end (both found by binary search on the z keys): about 2 r_list of each
+// column instead of its 3 cells, and about the same count for every thread of a warp.
+// Measured at 1M atoms: 0.653 ms per build against 0.685 ms leaving the window at the
+// first key past it and 0.76 ms scanning whole cells.
+template<bool kCubic>
+__global__ void __launch_bounds__(kBlock) k_pc_build(PcBuildArgs a, int64_t r_units, pg_status *status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if(t >= a.list.stride) { return; }
+    const int rec = a.list.pair_table[t];
+    const int cap = a.list.max_neighbors;
+    int cnt = 0;
+    if(rec >= 0) {
+        const int ia = rec & (int) kPcIndexMask;
+        const bool has_b = (rec & kPcHasB) != 0;
+        const int ib = has_b ? ia + 1 : ia;
+        const int4 fa = ld_i4(a.p.pos_fx, ia), fb = ld_i4(a.p.pos_fx, ib);
+        st_d4(a.p.pos_ref, ia, ld_d4(a.p.pos, ia));
+        st_i4(a.p.ref_fx, ia, fa);
+        if(has_b) {
+            st_d4(a.p.pos_ref, ib, ld_d4(a.p.pos, ib));
+            st_i4(a.p.ref_fx, ib, fb);
+        }
+        const bool use_a = !(a.p.flags != nullptr && (a.p.flags[ia] & kFlagFixed));
+        const bool use_b = has_b && !(a.p.flags != nullptr && (a.p.flags[ib] & kFlagFixed));
+        const int ci = a.cells.particle_cell[ia];
+        if((use_a || use_b) && ci < a.cells.ncells) {
+            const int dz_ = a.cells.dims[2], dy_ = a.cells.dims[1], dx_ = a.cells.dims[0];
+            const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
+            const int rr = a.cells.reach > 1 ? a.cells.reach : 1;
+            const int rx = a.cells.reach_x > 0 ? a.cells.reach_x : rr;
+            const float unit2 = kCubic ? a.box.fx_unit[0] * a.box.fx_unit[0] : 1.0f;
+            const float r2_lo = a.r2_lo / unit2, r2_hi = a.r2_hi / unit2;
+            const int stride = a.list.stride;
+            int32_t *wp = a.list.nbr + t;
+            // the members' z window (keys of their own cell; b follows a in z order)
+            const bool own_top = cz == dz_ - 1;
+            const int64_t za = z_key((uint32_t) fa.z, own_top), zb = z_key((uint32_t) fb.z, own_top);
+            const int64_t w_lo = (za < zb ? za : zb) - r_units, w_hi = (za < zb ? zb : za) + r_units;
+            // column ranges: the unwrapped cells, then the cells wrapped below / above
+            const int z_lo = cz - rr < 0 ? 0 : cz - rr, z_hi = cz + rr > dz_ - 1 ? dz_ - 1 : cz + rr;
+            // one candidate j (position fj) of the stencil cell at x offset ox, image (sx, sy, sz)
+            auto candidate = [&](int j, int4 fj, int ox, int sx, int sy, int sz) {
+                float ax = (float) fx_diff(fa.x, fj.x), ay = (float) fx_diff(fa.y, fj.y);
+                float az = (float) fx_diff(fa.z, fj.z);
+                float bx = (float) fx_diff(fb.x, fj.x), by = (float) fx_diff(fb.y, fj.y);
+                float bz = (float) fx_diff(fb.z, fj.z);
+                if(!kCubic) {
+                    ax *= a.box.fx_unit[0]; ay *= a.box.fx_unit[1]; az *= a.box.fx_unit[2];
+                    bx *= a.box.fx_unit[0]; by *= a.box.fx_unit[1]; bz *= a.box.fx_unit[2];
+                }
+                // a partner in a higher x slab lies above; in the own slab the separation
+                // decides (exactly one side of a pair keeps it)
+                bool ka = use_a && j != ia && (ox > 0 || partner_above(ax, ay, az, ia, j));
+                bool kb = use_b && j != ib && (ox > 0 || partner_above(bx, by, bz, ib, j));
+                if(ka) {
+                    const float r2 = ax * ax + ay * ay + az * az;
+                    ka = r2 < r2_lo || (r2 <= r2_hi && pc_exact(a, ia, j, sx, sy, sz));
+                }
+                if(kb) {
+                    const float r2 = bx * bx + by * by + bz * bz;
+                    kb = r2 < r2_lo || (r2 <= r2_hi && pc_exact(a, ib, j, sx, sy, sz));
+                }
+                if(ka || kb) {
+                    if(cnt < cap) {
+                        *wp = (int32_t) ((uint32_t) j | (ka ? kPcMaskA : 0u) | (kb ? kPcMaskB : 0u));
+                        wp += stride;
+                    }
+                    cnt++;
+                }
+            };
+            for(int ox = 0; ox <= rx; ox++) {
+                int nx = cx + ox, sx = 0;
+                if(nx >= dx_) { nx -= dx_; sx = 1; }
+                for(int oy = -rr; oy <= rr; oy++) {
+                    int ny = cy + oy, sy = 0;
+                    if(ny < 0) { ny += dy_; sy = -1; } else if(ny >= dy_) { ny -= dy_; sy = 1; }
+                    const int col = (nx * dy_ + ny) * dz_;
+                    for(int seg = 0; seg < 3; seg++) {
+                        int c0, c1, sz;
+                        if(seg == 0) { c0 = z_lo; c1 = z_hi; sz = 0; }
+                        else if(seg == 1) { c0 = cz - rr + dz_; c1 = dz_ - 1; sz = -1; }   // wrapped below
+                        else { c0 = 0; c1 = cz + rr - dz_; sz = 1; }                          // wrapped above
+                        if(c0 > c1) { continue; }
+                        const int b = a.cells.cell_start[col + c0];
+                        const int e = a.cells.cell_start[col + c1] + a.cells.cell_count[col + c1];
+                        const bool top = c1 == dz_ - 1;
+                        const int64_t shift = (int64_t) sz * ((int64_t) 1 << 32);
+                        // the window's particles [lo, hi): first key + shift >= w_lo, first > w_hi
+                        const int ts = top ? a.cells.cell_start[col + dz_ - 1] : e;
+                        int lo = b, hi = e;
+                        while(lo < hi) {
+                            const int mid = (lo + hi) >> 1;
+                            const int64_t k = z_key((uint32_t) __ldg(a.p.pos_fx + 4 * (size_t) mid + 2), mid >= ts) + shift;
+                            if(k < w_lo) { lo = mid + 1; } else { hi = mid; }
+                        }
+                        int end = e;
+                        for(int l = lo; l < end;) {
+                            const int mid = (l + end) >> 1;
+                            const int64_t k = z_key((uint32_t) __ldg(a.p.pos_fx + 4 * (size_t) mid + 2), mid >= ts) + shift;
+                            if(k <= w_hi) { l = mid + 1; } else { end = mid; }
+                        }
+                        // two candidates per iteration: their loads and arithmetic overlap
+                        int j = lo;
+                        for(; j + 1 < end; j += 2) {
+                            const int4 f0 = ld_i4(a.p.pos_fx, j), f1 = ld_i4(a.p.pos_fx, j + 1);
+                            candidate(j, f0, ox, sx, sy, sz);
+                            candidate(j + 1, f1, ox, sx, sy, sz);
+                        }
+                        if(j < end) { candidate(j, ld_i4(a.p.pos_fx, j), ox, sx, sy, sz); }
+                    }
+                }
+            }
+        }
+    }
+    a.list.count[t] = cnt < cap ? cnt : cap;
+    publish_count(cnt, cap, status);
+}
+
+// ------------------------------------------------------------------ force
+
+struct PcForceArgs {
+    pg_box box;
+    pg_particles p;
+    pg_neighbor_list list;
+    LJTable lj;
+    double *energy;
+    int32_t *cut_count;          // pairs within the cutoff band, queued (particle, partner)
+    int2 *cut_rec;
+    int cut_capacity;
+};
+
+__device__ __forceinline__ void pc_block_energy(double pe, double vir, double *energy) {
+    __shared__ double s[2][kPcBlock / 32];
+    pe = warp_sum(pe);
+    vir = warp_sum(vir);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if(lane == 0) { s[0][w] = pe; s[1][w] = vir; }
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for(int k = 0; k < kPcBlock / 32; k++) { x += s[0][k]; y += s[1][k]; }
+        atomicAdd(&energy[0], x);
+        atomicAdd(&energy[1], y);
+    }
+}
+
+// The pair forces of one cluster slot.  Lane x of every packed value is the first
+// member's pair with the entry's partner, lane y the second's.  Each pair rounds as
+// in the per-particle kernels (the squared distance in the order of pair_rsq, the
+// factor 48 sr6 (sr6 - 1/2) sr2 eps in FP32, examples/md.py:5-8); a pair within
+// kCutBand of rc^2 is queued for the FP64 decision of k_pc_fixup.
+template<bool kOneType, bool kEnergy>
+__global__ void __launch_bounds__(kPcBlock) k_pc_lj(PcForceArgs a) {
+    if(frozen_force(a.p)) { return; }
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int rec = t < a.list.stride ? a.list.pair_table[t] : -1;
+    double pe = 0.0, vir = 0.0;
+    if(rec >= 0) {
+        const int ia = rec & (int) kPcIndexMask;
+        const bool has_b = (rec & kPcHasB) != 0;
+        const int ib = has_b ? ia + 1 : ia;
+        const int4 fa = ld_i4(a.p.pos_fx, ia), fb = ld_i4(a.p.pos_fx, ib);
+        const int ta = kOneType ? 0 : fa.w * a.lj.ntypes, tb = kOneType ? 0 : fb.w * a.lj.ntypes;
+        const int cnt = a.list.count[t];
+        const int32_t *nb = a.list.nbr + t;
+        const size_t stride = (size_t) a.list.stride;
+        const float c2 = a.lj.cutoff2f, band = c2 * kCutBand;
+        const float2 ux = make_float2(a.box.fx_unit[0], a.box.fx_unit[0]);
+        const float2 uy = make_float2(a.box.fx_unit[1], a.box.fx_unit[1]);
+        const float2 uz = make_float2(a.box.fx_unit[2], a.box.fx_unit[2]);
+        const float2 half2 = make_float2(-0.5f, -0.5f);
+        float2 FX = make_float2(0.0f, 0.0f), FY = FX, FZ = FX;
+        uint32_t cur[kPcBatch];
+#pragma unroll
+        for(int u = 0; u < kPcBatch; u++) { cur[u] = u < cnt ? (uint32_t) __ldcs(nb + u * stride) : 0u; }
+        for(int k0 = 0; k0 < cnt; k0 += kPcBatch) {
+            int4 fj[kPcBatch];
+#pragma unroll
+            for(int u = 0; u < kPcBatch; u++) { fj[u] = ld_i4(a.p.pos_fx, (int) (cur[u] & kPcIndexMask)); }
+            uint32_t nxt[kPcBatch];
+            const int32_t *nbn = nb + (size_t) (k0 + kPcBatch) * stride;
+#pragma unroll
+            for(int u = 0; u < kPcBatch; u++) {
+                nxt[u] = k0 + kPcBatch + u < cnt ? (uint32_t) __ldcs(nbn + u * stride) : 0u;
+            }
+            uint32_t pend_a = 0u, pend_b = 0u;
+#pragma unroll
+            for(int u = 0; u < kPcBatch; u++) {
+                const bool valid = k0 + u < cnt;
+                const bool ma = valid && (cur[u] & kPcMaskA) != 0u, mb = valid && (cur[u] & kPcMaskB) != 0u;
+                const float2 dX = __fmul2_rn(make_float2((float) fx_diff(fa.x, fj[u].x), (float) fx_diff(fb.x, fj[u].x)), ux);
+                const float2 dY = __fmul2_rn(make_float2((float) fx_diff(fa.y, fj[u].y), (float) fx_diff(fb.y, fj[u].y)), uy);
+                const float2 dZ = __fmul2_rn(make_float2((float) fx_diff(fa.z, fj[u].z), (float) fx_diff(fb.z, fj[u].z)), uz);
+                float2 R = __fmul2_rn(dX, dX);
+                R = __ffma2_rn(dY, dY, R);
+                R = __ffma2_rn(dZ, dZ, R);
+                const bool na = fabsf(R.x - c2) < band, nbd = fabsf(R.y - c2) < band;
+                const bool ina = ma && R.x < c2 && !na, inb = mb && R.y < c2 && !nbd;
+                float2 sig6, eps48;
+                if(kOneType) {
+                    sig6 = make_float2(a.lj.sig6f[0], a.lj.sig6f[0]);
+                    eps48 = make_float2(48.0f * a.lj.epsf[0], 48.0f * a.lj.epsf[0]);
+                } else {
+                    const int pa = ta + fj[u].w, pb = tb + fj[u].w;
+                    sig6 = make_float2(a.lj.sig6f[pa], a.lj.sig6f[pb]);
+                    eps48 = make_float2(48.0f * a.lj.epsf[pa], 48.0f * a.lj.epsf[pb]);
+                }
+                const float2 S2 = make_float2(rcp_approx(R.x), rcp_approx(R.y));
+                const float2 S6 = __fmul2_rn(__fmul2_rn(S2, S2), __fmul2_rn(S2, sig6));
+                float2 F = __fmul2_rn(__fmul2_rn(S6, __fadd2_rn(S6, half2)), __fmul2_rn(S2, eps48));
+                F.x = ina ? F.x : 0.0f;
+                F.y = inb ? F.y : 0.0f;
+                FX = __ffma2_rn(dX, F, FX);
+                FY = __ffma2_rn(dY, F, FY);
+                FZ = __ffma2_rn(dZ, F, FZ);
+                if(ina || inb) {
+                    const float2 px = __fmul2_rn(dX, F), py = __fmul2_rn(dY, F), pz = __fmul2_rn(dZ, F);
+                    red_add_v4(a.p.force32 + 4 * (size_t) (cur[u] & kPcIndexMask), -(px.x + px.y), -(py.x + py.y),
+                               -(pz.x + pz.y));
+                    if(kEnergy) {
+                        const int pa = kOneType ? 0 : ta + fj[u].w, pb = kOneType ? 0 : tb + fj[u].w;
+                        if(ina) {
+                            pe += 4.0 * (double) a.lj.epsf[pa] * ((double) S6.x * (double) S6.x - (double) S6.x);
+                            vir += (double) (R.x * F.x);
+                        }
+                        if(inb) {
+                            pe += 4.0 * (double) a.lj.epsf[pb] * ((double) S6.y * (double) S6.y - (double) S6.y);
+                            vir += (double) (R.y * F.y);
+                        }
+                    }
+                }
+                if(ma && na) { pend_a |= 1u << u; }
+                if(mb && nbd) { pend_b |= 1u << u; }
+            }
+            if((pend_a | pend_b) != 0u) {
+#pragma unroll
+                for(int u = 0; u < kPcBatch; u++) {
+                    const int j = (int) (cur[u] & kPcIndexMask);
+                    if(pend_a & (1u << u)) { cut_queue_push(a.cut_count, a.cut_rec, a.cut_capacity, ia, (uint32_t) j); }
+                    if(pend_b & (1u << u)) { cut_queue_push(a.cut_count, a.cut_rec, a.cut_capacity, ib, (uint32_t) j); }
+                }
+            }
+#pragma unroll
+            for(int u = 0; u < kPcBatch; u++) { cur[u] = nxt[u]; }
+        }
+        red_add_v4(a.p.force32 + 4 * (size_t) ia, FX.x, FY.x, FZ.x);
+        if(has_b) { red_add_v4(a.p.force32 + 4 * (size_t) ib, FX.y, FY.y, FZ.y); }
+    }
+    if(kEnergy) { pc_block_energy(pe, vir, a.energy); }
+}
+
+// One pair of the cutoff band, decided by the FP64 path's own test on the image of the
+// partner nearest the particle (the image the reference's ghost carries; the pair is
+// far closer than half a box), then applied as the main pass would have: the FP32 force
+// on the particle and its reaction on the partner.
+template<bool kOneType, bool kEnergy>
+__device__ void pc_fixup_pair(const PcForceArgs &a, int i, int j) {
+    const D4 xi = ld_d4_rare(a.p.pos, i), xj = ld_d4_rare(a.p.pos, j);
+    const double di[3] = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
+    int s[3];
+    for(int d = 0; d < 3; d++) {
+        const double h = 0.5 * a.box.len[d];
+        s[d] = di[d] > h ? 1 : (di[d] < -h ? -1 : 0);
+    }
+    const double dx = __dsub_rn(xi.x, ref_image(xj.x, s[0], a.box.len[0]));
+    const double dy = __dsub_rn(xi.y, ref_image(xj.y, s[1], a.box.len[1]));
+    const double dz = __dsub_rn(xi.z, ref_image(xj.z, s[2], a.box.len[2]));
+    if(!(ref_rsq(dx, dy, dz) < a.lj.cutoff2)) { return; }
+    const int4 fi = ld_i4(a.p.pos_fx, i), fj = ld_i4(a.p.pos_fx, j);
+    const float ex = __fmul_rn((float) fx_diff(fi.x, fj.x), a.box.fx_unit[0]);
+    const float ey = __fmul_rn((float) fx_diff(fi.y, fj.y), a.box.fx_unit[1]);
+    const float ez = __fmul_rn((float) fx_diff(fi.z, fj.z), a.box.fx_unit[2]);
+    const float rsq = pair_rsq(ex, ey, ez);
+    const int tij = kOneType ? 0 : fi.w * a.lj.ntypes + fj.w;
+    const float s2 = rcp_approx(rsq);
+    const float s6 = __fmul_rn(__fmul_rn(s2, s2), __fmul_rn(s2, a.lj.sig6f[tij]));
+    const float f = __fmul_rn(__fmul_rn(s6, __fadd_rn(s6, -0.5f)), __fmul_rn(s2, 48.0f * a.lj.epsf[tij]));
+    red_add_v4(a.p.force32 + 4 * (size_t) i, ex * f, ey * f, ez * f);
+    red_add_v4(a.p.force32 + 4 * (size_t) j, -(ex * f), -(ey * f), -(ez * f));
+    if(kEnergy) {
+        atomicAdd(&a.energy[0], 4.0 * (double) a.lj.epsf[tij] * ((double) s6 * (double) s6 - (double) s6));
+        atomicAdd(&a.energy[1], (double) (rsq * f));
+    }
+}
+
+// The band pairs the main pass left out: the queued records, or, when more pairs fell
+// in the band than the queue holds, every cluster list walked again with the main
+// pass's screen arithmetic (which finds exactly the pairs it left out).
+template<bool kOneType, bool kEnergy>
+__global__ void __launch_bounds__(kBlock) k_pc_fixup(PcForceArgs a) {
+    if(frozen_force(a.p)) { return; }
+    const int queued = *a.cut_count;
+    const int first = blockIdx.x * blockDim.x + threadIdx.x, step = gridDim.x * blockDim.x;
+    if(queued <= a.cut_capacity) {
+        for(int r = first; r < queued; r += step) {
+            const int2 q = a.cut_rec[r];
+            pc_fixup_pair<kOneType, kEnergy>(a, q.x, q.y);
+        }
+        return;
+    }
+    const float c2 = a.lj.cutoff2f, band = c2 * kCutBand;
+    for(int t = first; t < a.list.stride; t += step) {
+        const int rec = a.list.pair_table[t];
+        if(rec < 0) { continue; }
+        const int ia = rec & (int) kPcIndexMask;
+        const int ib = (rec & kPcHasB) != 0 ? ia + 1 : ia;
+        const int4 fa = ld_i4(a.p.pos_fx, ia), fb = ld_i4(a.p.pos_fx, ib);
+        const int cnt = a.list.count[t];
+        for(int k = 0; k < cnt; k++) {
+            const uint32_t e = (uint32_t) a.list.nbr[(size_t) k * a.list.stride + t];
+            const int j = (int) (e & kPcIndexMask);
+            const int4 fj = ld_i4(a.p.pos_fx, j);
+            for(int m = 0; m < 2; m++) {
+                if(!(e & (m == 0 ? kPcMaskA : kPcMaskB))) { continue; }
+                const int4 fm = m == 0 ? fa : fb;
+                const float ex = __fmul_rn((float) fx_diff(fm.x, fj.x), a.box.fx_unit[0]);
+                const float ey = __fmul_rn((float) fx_diff(fm.y, fj.y), a.box.fx_unit[1]);
+                const float ez = __fmul_rn((float) fx_diff(fm.z, fj.z), a.box.fx_unit[2]);
+                if(fabsf(pair_rsq(ex, ey, ez) - c2) < band) { pc_fixup_pair<kOneType, kEnergy>(a, m == 0 ? ia : ib, j); }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+bool fixed_point_screen(const pg_box *box, const pg_particles *p, const pg_cells *cells);
+
+int pc_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list, double r_list2,
+             pg_status *status, cudaStream_t st) {
+    if(!list->half || !fixed_point_screen(box, p, cells)) { return PG_ERR_ARGUMENT; }
+    if((int64_t) list->stride < pair_slots(p->n, cells->ncells) || p->n >= (1 << 30)) { return PG_ERR_ARGUMENT; }
+    PcBuildArgs a;
+    a.box = *box; a.p = *p; a.cells = *cells; a.list = *list; a.r_list2 = r_list2;
+    a.r2_lo = (float) r_list2 * (1.0f - kPcScreenBand);
+    a.r2_hi = (float) r_list2 * (1.0f + kPcScreenBand);
+    cudaMemsetAsync(list->pair_table, 0xff, (size_t) list->stride * sizeof(int32_t), st);
+    if(cells->ncells > 0) {
+        k_pc_table<<<blocks_for(cells->ncells), kBlock, 0, st>>>(*cells, list->pair_table); note_launch();
+    }
+    // the z window's half width in units, above r_list by the rounding of two coordinates
+    const int64_t r_units = (int64_t) ceil(sqrt(r_list2) * box->fx_scale[2]) + 4;
+    const bool cubic = box->fx_unit[0] == box->fx_unit[1] && box->fx_unit[1] == box->fx_unit[2];
+    if(cubic) { k_pc_build<true><<<blocks_for(list->stride), kBlock, 0, st>>>(a, r_units, status); }
+    else { k_pc_build<false><<<blocks_for(list->stride), kBlock, 0, st>>>(a, r_units, status); }
+    note_launch();
+    return launch_status();
+}
+
+constexpr int kPcFixupBlocks = 2 * kSMs;
+
+int pc_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list, const LJTable &lj,
+                double *energy, int32_t *cut_count, int2 *cut_rec, int cut_capacity, cudaStream_t st) {
+    if(!list->half || !p->pos_fx || !list->nbr || !list->count || !cut_count) { return PG_ERR_ARGUMENT; }
+    PcForceArgs a;
+    a.box = *box; a.p = *p; a.list = *list; a.lj = lj;
+    a.energy = energy; a.cut_count = cut_count; a.cut_rec = cut_rec; a.cut_capacity = cut_capacity;
+    const bool one = lj.ntypes == 1, en = energy != nullptr;
+    const int grid = blocks_for(list->stride, kPcBlock);
+    if(one) {
+        if(en) { k_pc_lj<true, true><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<true, true><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+        else { k_pc_lj<true, false><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<true, false><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+    } else {
+        if(en) { k_pc_lj<false, true><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<false, true><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+        else { k_pc_lj<false, false><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<false, false><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+    }
+    note_launch(2);
+    return launch_status();
+}
+
+}  // namespace pg

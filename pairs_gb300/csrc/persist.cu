@@ -288,7 +288,7 @@ int lj_steps(const pg_box *box, pg_particles *p, const pg_neighbor_list *list, c
              cudaStream_t st) {
     if(!box || !p || !list || !lj || !status || nsteps < 0) { return PG_ERR_ARGUMENT; }
     if(!p->pos || !p->vel || !p->mass || !p->force32 || !p->pos_fx || !p->ref_fx || !p->pos_ref || !list->nbr ||
-       !list->count || list->nbr16 != nullptr) {
+       !list->count || list->nbr16 != nullptr || list->pair_table != nullptr) {
         return PG_ERR_ARGUMENT;
     }
     if(lj->ntypes < 1 || lj->ntypes > kMaxTypes || (lj->ntypes > 1 && !p->type)) { return PG_ERR_ARGUMENT; }

@@ -53,7 +53,7 @@ class LJEngine:
                  dt=0.005, ntypes=1, epsilon=None, sigma6=None, precision="fp64", half=False,
                  sync="exact", every=20, neighbor_capacity=100, policy="fixed", device="cuda",
                  capacity=None, fused=True, tiles=None, tile_tpa=2, tile_atoms=224, cell_reach=1,
-                 cell_reach_x=None, fixed_point=None, graphs=True, persistent=None):
+                 cell_reach_x=None, fixed_point=None, graphs=True, persistent=None, pair_lists=None):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -213,6 +213,19 @@ class LJEngine:
         self.list = A.PgNeighborList()
         self.list.stride = cap
         self.list.half = int(bool(half))
+        # pair-cluster half lists (one list per two particles of a cell, pairlist.cu) on
+        # the mixed path with fixed-point positions; the per-particle half list's pair
+        # set, a partner gathered once and one reaction for both members
+        pc_ok = (self.precision == A.PG_MIXED and self.fixed_point and bool(half) and not tiles
+                 and not persistent)
+        if pair_lists and not pc_ok:
+            raise ValueError("pair-cluster lists need the mixed path, fixed-point positions and half lists, "
+                             "without tiles or persistent steps")
+        self.pair_lists = pc_ok if pair_lists is None else bool(pair_lists)
+        if self.pair_lists:
+            self.list.stride = int(A.load().pg_pair_slots(cap, ncells))
+            t["pair_table"] = torch.full((self.list.stride,), -1, dtype=torch.int32, device=self.dev)
+            self.list.pair_table = t["pair_table"].data_ptr()
         # tile lists are opt-in: on GB300 the global-list kernels, which gather partners
         # through L1, measured faster (1M atoms, full lists: 0.31 ms global vs 0.94 ms
         # tiles at 2 threads per atom)
@@ -260,7 +273,7 @@ class LJEngine:
         # Opt-in: at 1M atoms the chunk graph of separate kernels measured 0.345 ms/step
         # against 0.397 for the persistent launch (three grid barriers per step, and far
         # fewer loads in flight in its grid-stride phases than in a 1M-thread launch)
-        can_persist = self.precision == A.PG_MIXED and self.fixed_point and not self.tiles
+        can_persist = self.precision == A.PG_MIXED and self.fixed_point and not self.tiles and not self.pair_lists
         if persistent and not can_persist:
             raise ValueError("persistent steps need the mixed path with fixed-point positions and global lists")
         self.persistent = bool(persistent) and can_persist
@@ -312,10 +325,10 @@ class LJEngine:
             self.list.nbr16 = self.t["nbr16"].data_ptr()
             self.list.nbr = None
         else:
-            self.t["nbr"] = torch.zeros((max_nb, self.cap), dtype=torch.int32, device=self.dev)
+            self.t["nbr"] = torch.zeros((max_nb, self.list.stride), dtype=torch.int32, device=self.dev)
             self.list.nbr = self.t["nbr"].data_ptr()
             self.list.nbr16 = None
-        self.t["count"] = torch.zeros((self.cap,), dtype=torch.int32, device=self.dev)
+        self.t["count"] = torch.zeros((self.list.stride,), dtype=torch.int32, device=self.dev)
         self.list.count = self.t["count"].data_ptr()
 
     def _rotate_ring(self):
@@ -812,8 +825,48 @@ class LJEngine:
                         tables[i] = (gj, gc)
         return tables
 
+    def _cluster_pairs(self):
+        """Pair-cluster entries as (uid_i, uid_j, sx, sy, sz) rows, i the member that
+        stores the pair; the image is the partner's nearest to i at the last rebuild."""
+        stride = self.list.stride
+        table = self.t["pair_table"][:stride].cpu().numpy().astype(np.int64)
+        cnt = self.t["count"][:stride].cpu().numpy()
+        nbr = self.t["nbr"][:, :stride].cpu().numpy().astype(np.uint32)
+        uid = self.t["uid"][: self.n].cpu().numpy()
+        ref = self.t["pos_ref"][: self.n, :3].cpu().numpy()
+        kk = np.arange(nbr.shape[0])[:, None]
+        sel = (kk < cnt[None, :]).nonzero()
+        e = nbr[sel]
+        slot = sel[1]
+        first = table[slot] & ((1 << 30) - 1)
+        j = (e & ((1 << 30) - 1)).astype(np.int64)
+        rows = []
+        for member, bit in ((0, 1 << 30), (1, 1 << 31)):
+            m = (e & np.uint32(bit)) != 0
+            i = first[m] + member
+            d = ref[i] - ref[j[m]]
+            half = 0.5 * np.array([self.box.len[k] for k in range(3)])
+            img = np.where(d > half, 1, np.where(d < -half, -1, 0))
+            rows.append(np.concatenate([uid[i][:, None], uid[j[m]][:, None], img], axis=1))
+        return np.concatenate(rows).astype(np.int32)
+
+    def list_size(self):
+        """(pairs, entries) of the current Verlet list: a per-particle list stores one
+        pair per entry, a pair-cluster entry one or two (its member bits)."""
+        cnt = self.t["count"][: self.list.stride]
+        entries = int(cnt.sum().item())
+        if not self.pair_lists:
+            return entries, entries
+        nbr = self.t["nbr"][:, : self.list.stride]
+        valid = torch.arange(nbr.shape[0], device=self.dev)[:, None] < cnt[None, :]
+        e = nbr.to(torch.int64) & 0xFFFFFFFF
+        bits = ((e >> 30) & 1) + ((e >> 31) & 1)
+        return int(bits[valid].sum().item()), entries
+
     def pairs(self):
         """Verlet entries as (uid_i, uid_j, sx, sy, sz) rows (list order per particle)."""
+        if self.pair_lists:
+            return self._cluster_pairs()
         n = self.n
         cnt = self.t["count"][:n].cpu().numpy()
         if self.tiles:

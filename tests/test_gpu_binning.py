@@ -146,10 +146,14 @@ def test_engine_grid_matches_host_recount(cube, half):
     assert eng.t["cell_count"][nc].item() == 0
     assert np.array_equal(eng.t["cell_start"][: nc + 1].cpu().numpy(), np.concatenate([[0], np.cumsum(counts)]))
     assert np.array_equal(eng.t["particle_cell"][:n].cpu().numpy(), flat)
-    # stable within a cell by uid
+    # within a cell by z, then uid: every z column of cells is sorted by z
     uid = eng.t["uid"][:n].cpu().numpy()
     same = flat[1:] == flat[:-1]
-    assert np.all(uid[1:][same] > uid[:-1][same])
+    z = pos[:, 2]
+    assert np.all((z[1:][same] > z[:-1][same]) | ((z[1:][same] == z[:-1][same]) & (uid[1:][same] > uid[:-1][same])))
+    column = flat // dims[2]
+    run = column[1:] == column[:-1]
+    assert np.all(z[1:][run] >= z[:-1][run])
 
 
 @pytest.mark.parametrize("half,precision", [(False, "fp64"), (True, "mixed"), (False, "mixed")])

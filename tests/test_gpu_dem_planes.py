@@ -9,6 +9,12 @@ plane at the top (normal -z): half spaces as general shapes in the pair loop
 after some steps (with its contact history), one GPU step equals one oracle step:
 forces, torques, velocities to 1e-12 of their RMS, positions and orientations to
 round-off, and the same contact records.
+
+Lattice sites lie on the periodic faces x = 0 and y = 0, so spheres with contacts cross
+those faces every few steps.  The reference then packs a leaving sphere's history after
+its slot was refilled (sim/comm.py:101-151), and the sphere takes over its filler's
+contacts; the GPU path moves each sphere's own records with it.  The oracle runs in
+that corrected mode here (history_fixed), as the two modes differ for these spheres.
 """
 import math
 
@@ -34,7 +40,7 @@ def setup():
     p = dict(dt=1e-6, kappa=2.0 * (1.0 - nu) / (2.0 - nu), ln_e=math.log(e), tc=5e-4, rho_p=2500, rho_f=0,
              gravity=9.81, mu=0.5, cell=1.01 * 1.2e-3)
     spheres = {k: st[k] for k in ("uid", "type", "mass", "radius", "pos", "vel")}
-    sim = odem.Sim(box, planes, p, spheres=spheres, kn=KN, ccap=64)
+    sim = odem.Sim(box, planes, p, spheres=spheres, kn=KN, ccap=64, history_fixed=True)
     return sim, p, box
 
 

@@ -263,7 +263,7 @@ def test_half_list_counts_are_balanced_within_warps():
     the full list's interior pairs plus its image pairs."""
     from pairs_gb300.engine import LJEngine
     st = lattice.copper_fcc_lattice(16, 16, 16)
-    e = LJEngine(st, precision="mixed", half=True, policy="guard")
+    e = LJEngine(st, precision="mixed", half=True, policy="guard", pair_lists=False)
     e.run(40)
     e.settle()
     e.rebuild()
