@@ -238,15 +238,15 @@ def run_ours(args, rank, world, dist):
 
     build_ms = statistics.median(build_times(eng, 6))
     # algorithmic bytes of one force launch: own position (16 fixed point, 32 FP32 hi+lo
-    # or FP64 x,y,z,pad), neighbour count (4), force write (16 FP32 / 32 FP64), one Verlet
-    # entry per pair (4 bytes global, 2 bytes tile-local); a half list adds one
-    # reaction write per particle (b_F)
+    # or FP64 x,y,z,pad), neighbour count (4 per particle; a pair-cluster list reads a
+    # count and a table word per cluster slot), force write (16 FP32 / 32 FP64), each
+    # stored list entry once (4 bytes global, 2 bytes tile-local; a pair-cluster entry
+    # carries one or two pairs); a half list adds one reaction write per particle (b_F)
     b_f = 16 if prec == "mixed" else 32
     b_entry = 2 if eng.list.nbr16 else 4
     b_pos = 16 if (prec == "mixed" and eng.fixed_point) else 32     # fixed point: one int4
-    b_force = n * (b_pos + 4 + b_f) + b_entry * pairs_total + (n * b_f if eng.list.half else 0)
-    # (pairs_total: the Verlet pairs; a pair-cluster list holds them in fewer entries,
-    # entries_total, whose bytes are reported beside as list_bytes)
+    b_count = 8 * eng.list.stride if eng.pair_lists else 4 * n
+    b_force = n * (b_pos + b_f) + b_count + b_entry * entries_total + (n * b_f if eng.list.half else 0)
     # the mixed path's force pass: pair-cluster lists (k_pc_lj), packed pair arithmetic
     # on fixed-point positions (k_lj_packed), one pair at a time on compensated
     # positions (k_lj_mixed)

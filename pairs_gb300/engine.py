@@ -825,17 +825,23 @@ class LJEngine:
                         tables[i] = (gj, gc)
         return tables
 
+    def _cluster_rows(self):
+        """Valid entries of a pair-cluster list as a (rows, slots) mask, and the count
+        per slot."""
+        cnt = self.t["count"][: self.list.stride]
+        k = torch.arange(self.list.max_neighbors, device=self.dev)[:, None]
+        return k < cnt[None, :], cnt
+
     def _cluster_pairs(self):
         """Pair-cluster entries as (uid_i, uid_j, sx, sy, sz) rows, i the member that
         stores the pair; the image is the partner's nearest to i at the last rebuild."""
         stride = self.list.stride
         table = self.t["pair_table"][:stride].cpu().numpy().astype(np.int64)
-        cnt = self.t["count"][:stride].cpu().numpy()
+        valid, _ = self._cluster_rows()
         nbr = self.t["nbr"][:, :stride].cpu().numpy().astype(np.uint32)
         uid = self.t["uid"][: self.n].cpu().numpy()
         ref = self.t["pos_ref"][: self.n, :3].cpu().numpy()
-        kk = np.arange(nbr.shape[0])[:, None]
-        sel = (kk < cnt[None, :]).nonzero()
+        sel = valid.cpu().numpy().nonzero()
         e = nbr[sel]
         slot = sel[1]
         first = table[slot] & ((1 << 30) - 1)
@@ -850,15 +856,22 @@ class LJEngine:
             rows.append(np.concatenate([uid[i][:, None], uid[j[m]][:, None], img], axis=1))
         return np.concatenate(rows).astype(np.int32)
 
+    def list_counts(self):
+        """Stored entries per list row owner (a particle, or a pair-cluster slot) as a
+        numpy array."""
+        if not self.pair_lists:
+            return self.t["count"][: self.n].cpu().numpy()
+        return self.t["count"][: self.list.stride].cpu().numpy()
+
     def list_size(self):
         """(pairs, entries) of the current Verlet list: a per-particle list stores one
         pair per entry, a pair-cluster entry one or two (its member bits)."""
-        cnt = self.t["count"][: self.list.stride]
-        entries = int(cnt.sum().item())
         if not self.pair_lists:
+            entries = int(self.t["count"][: self.list.stride].sum().item())
             return entries, entries
+        valid, cnt = self._cluster_rows()
+        entries = int(cnt.sum().item())
         nbr = self.t["nbr"][:, : self.list.stride]
-        valid = torch.arange(nbr.shape[0], device=self.dev)[:, None] < cnt[None, :]
         e = nbr.to(torch.int64) & 0xFFFFFFFF
         bits = ((e >> 30) & 1) + ((e >> 31) & 1)
         return int(bits[valid].sum().item()), entries

@@ -167,7 +167,7 @@ def test_lj_list_publishes_max_count_with_partial_warps(half, precision):
     eng.settle()
     eng.rebuild()
     s = eng.read_status()
-    cnt = eng.t["count"][: eng.n].cpu().numpy()
+    cnt = eng.list_counts()
     assert s.max_neighbors == cnt.max()
     assert s.overflow == 0
 

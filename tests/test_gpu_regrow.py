@@ -33,7 +33,7 @@ def test_tiny_neighbor_capacity_regrows_to_the_same_pair_set(precision, half):
     small.rebuild()
     big.rebuild()
     assert small.list.max_neighbors > 4
-    cnt = small.t["count"][: small.n].cpu().numpy()
+    cnt = small.list_counts()
     assert cnt.max() <= small.list.max_neighbors
     assert np.array_equal(canonical_pairs(small.pairs()), canonical_pairs(big.pairs()))
     small.force()
