@@ -368,14 +368,24 @@ __global__ void __launch_bounds__(kBlock) k_lj_cutoff_fixup(ForceArgs a) {
 using KernelFn = void (*)(ForceArgs);
 
 // zero the force array before a half-list pass, and the mixed path's near-cutoff queue
-// (skipped like the pass when frozen)
+// (skipped like the pass when frozen).  Each thread clears kZeroPer consecutive 16-byte
+// records after one read of the guard word (one record per thread: 12.5 us at 1M atoms,
+// the stores waiting on each thread's guard load).
+constexpr int kZeroPer = 4;
+
 __global__ void k_zero_force(pg_particles p, int fp64, int32_t *cut_count) {
     if(frozen_force(p)) { return; }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i == 0 && cut_count != nullptr) { *cut_count = 0; }
-    if(i >= p.n) { return; }
-    if(fp64) { st_d4(p.force, i, make_d4(0.0, 0.0, 0.0, 0.0)); }
-    else { st_f4(p.force32, i, make_float4(0.0f, 0.0f, 0.0f, 0.0f)); }
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if(t == 0 && cut_count != nullptr) { *cut_count = 0; }
+    // 16-byte records: one per particle in FP32, two in FP64
+    const int64_t records = fp64 ? 2 * (int64_t) p.n : (int64_t) p.n;
+    float4 *base = fp64 ? reinterpret_cast<float4 *>(p.force) : reinterpret_cast<float4 *>(p.force32);
+    const int64_t first = (int64_t) blockIdx.x * blockDim.x * kZeroPer + threadIdx.x;
+#pragma unroll
+    for(int k = 0; k < kZeroPer; k++) {
+        const int64_t r = first + (int64_t) k * blockDim.x;
+        if(r < records) { base[r] = make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+    }
 }
 
 static KernelFn pick_fp64(bool half, bool one, bool en) {
@@ -468,7 +478,9 @@ int lj_force(const pg_box *box, const pg_particles *p, const pg_cells *cells, co
         a.cut_capacity = (int) std::min<int64_t>((ws.bytes - 256) / 8, INT32_MAX);
     }
     if(half && p->n > 0) {
-        k_zero_force<<<blocks_for(p->n), kBlock, 0, st>>>(*p, precision == PG_FP64, a.cut_count); note_launch();
+        const int64_t records = precision == PG_FP64 ? 2 * (int64_t) p->n : (int64_t) p->n;
+        k_zero_force<<<blocks_for(records, kBlock * kZeroPer), kBlock, 0, st>>>(*p, precision == PG_FP64, a.cut_count);
+        note_launch();
     } else if(queue) {
         cudaMemsetAsync(a.cut_count, 0, sizeof(int32_t), st);
     }

@@ -38,7 +38,11 @@ constexpr uint32_t kPcIndexMask = (1u << 30) - 1u;   // table record / entry: pa
 constexpr uint32_t kPcMaskA = 1u << 30;              // entry: the pair (j, first member)
 constexpr uint32_t kPcMaskB = 1u << 31;              // entry: the pair (j, second member)
 constexpr float kPcScreenBand = 1.0e-4f;             // the build's FP64 band (as nlist.cu)
-constexpr int kPcBlock = 128;
+// force pass: 192 threads, at most 64 registers (5 blocks, 960 threads per SM).  Measured
+// at 1M atoms (main pass + fixup): 0.1556 ms, against 0.1638 at 128 threads (8 blocks),
+// 0.1556 at 96 threads (10 blocks) or at 128 threads with 72 registers (7 blocks),
+// 0.1633 at 80 registers or at 64 threads; the resident warps' partner gathers share L1
+constexpr int kPcBlock = 192;
 constexpr int kPcBatch = 4;
 
 int64_t pair_slots(int32_t n, int32_t ncells) {
@@ -293,7 +297,7 @@ __device__ __forceinline__ void pc_block_energy(double pe, double vir, double *e
 // factor 48 sr6 (sr6 - 1/2) sr2 eps in FP32, examples/md.py:5-8); a pair within
 // kCutBand of rc^2 is queued for the FP64 decision of k_pc_fixup.
 template<bool kOneType, bool kEnergy>
-__global__ void __launch_bounds__(kPcBlock) k_pc_lj(PcForceArgs a) {
+__global__ void __launch_bounds__(kPcBlock, 5) k_pc_lj(PcForceArgs a) {
     if(frozen_force(a.p)) { return; }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int rec = t < a.list.stride ? a.list.pair_table[t] : -1;
