@@ -605,6 +605,37 @@ int pg_vtk_format_rows(int section, int32_t rows, const int32_t *order, const do
  * lengths, int64, device memory), giving the section's text. */
 int pg_vtk_pack_rows(int32_t rows, pg_workspace ws, const int64_t *offsets, char *out, void *stream);
 
+/* ---- particle CSV input on the device ---------------------------------------
+ * Replaces read_particle_data (runtime/read_from_file.hpp:33-116).  The caller copies
+ * the file's bytes to the device (text); the library indexes the lines, parses every
+ * field as std::stod (PG_CSV_REAL) or std::stoi (PG_CSV_INT) reads it, keeps a line's
+ * particle when its position (fields pos_field .. pos_field + 2) lies in [lo, hi - 1e-5)
+ * on every axis (runtime/domain/regular_6d_stencil.cpp:96-100; no filter when domain_lo
+ * is NULL) or its flags field (flags_field, or -1) has the infinite, fixed or global bit,
+ * and writes the kept rows in file order to table, column-major [nfields * max_rows]
+ * (integers as exact doubles).  Lines of white space only are skipped.  A real field is
+ * converted to the correctly rounded double (ties to even) for up to 19 significant
+ * digits and decimal exponents within +-27 (up to 15 digits: +-22 by one FP64 operation);
+ * other numbers are counted in result->inexact.  A missing field, a field without
+ * digits or an integer outside int32 sets result->bad_line (0-based, the first such
+ * line).  Either returns PG_ERR_ARGUMENT; more kept rows than max_rows return
+ * PG_ERR_LIMIT with result->rows the number needed.  Both calls synchronise the stream
+ * (they return counts to the host). */
+#define PG_CSV_REAL 0
+#define PG_CSV_INT  1
+typedef struct {
+    int32_t rows;                /* particles kept */
+    int32_t lines;               /* lines indexed (newlines + 1) */
+    int32_t bad_line;            /* first malformed line, or -1 */
+    int32_t inexact;             /* real fields outside the exact conversion range */
+} pg_csv_result;
+int64_t pg_csv_count_bytes(int64_t bytes);
+int pg_csv_count_lines(const char *text, int64_t bytes, int64_t *lines, pg_workspace ws, void *stream);
+int64_t pg_csv_workspace_bytes(int64_t bytes, int64_t lines, int32_t nfields);
+int pg_csv_parse(const char *text, int64_t bytes, int64_t lines, int32_t nfields, const int32_t *kinds,
+                 int32_t pos_field, int32_t flags_field, const double *domain_lo, const double *domain_hi,
+                 double *table, int32_t max_rows, pg_csv_result *result, pg_workspace ws, void *stream);
+
 /* cudaStreamSynchronize, returning PG_OK or PG_ERR_CUDA. */
 int pg_stream_sync(void *stream);
 

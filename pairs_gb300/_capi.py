@@ -114,8 +114,14 @@ class PgEnsemble(C.Structure):
                 ("pad_", C.c_int32)]
 
 
+class PgCsvResult(C.Structure):
+    _fields_ = [("rows", C.c_int32), ("lines", C.c_int32), ("bad_line", C.c_int32), ("inexact", C.c_int32)]
+
+
+PG_CSV_REAL, PG_CSV_INT = 0, 1
+
 STRUCTS = [PgStatus, PgBox, PgParticles, PgCells, PgNeighborList, PgLJParams, PgWorkspace, PgDemParticles,
-           PgContacts, PgDemParams, PgReplica, PgEnsemble]
+           PgContacts, PgDemParams, PgReplica, PgEnsemble, PgCsvResult]
 
 P = C.POINTER
 # name -> (restype, argtypes)
@@ -144,6 +150,12 @@ SIGNATURES = {
     "pg_split_positions": (C.c_int, [P(PgBox), P(PgParticles), C.c_void_p]),
     "pg_permute": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "pg_pair_slots": (C.c_int64, [C.c_int32, C.c_int32]),
+    "pg_csv_count_bytes": (C.c_int64, [C.c_int64]),
+    "pg_csv_count_lines": (C.c_int, [C.c_void_p, C.c_int64, P(C.c_int64), PgWorkspace, C.c_void_p]),
+    "pg_csv_workspace_bytes": (C.c_int64, [C.c_int64, C.c_int64, C.c_int32]),
+    "pg_csv_parse": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32, P(C.c_int32), C.c_int32, C.c_int32,
+                               P(C.c_double), P(C.c_double), C.c_void_p, C.c_int32, P(PgCsvResult), PgWorkspace,
+                               C.c_void_p]),
     "pg_vtk_workspace_bytes": (C.c_int64, [C.c_int32]),
     "pg_vtk_format_rows": (C.c_int, [C.c_int, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      PgWorkspace, C.c_void_p]),

@@ -51,6 +51,12 @@ int64_t vtk_workspace_bytes(int32_t rows);
 int vtk_format_rows(int what, int32_t rows, const int32_t *order, const double *pos, const double *mass,
                     const int32_t *index, pg_workspace ws, cudaStream_t st);
 int vtk_pack_rows(int32_t rows, pg_workspace ws, const int64_t *offset, char *out, cudaStream_t st);
+int64_t csv_count_bytes(int64_t bytes);
+int csv_count_lines(const char *text, int64_t bytes, int64_t *lines, pg_workspace ws, cudaStream_t st);
+int64_t csv_workspace_bytes(int64_t bytes, int64_t lines, int32_t nfields);
+int csv_parse(const char *text, int64_t bytes, int64_t lines, int32_t nfields, const int32_t *kinds, int32_t pos_field,
+              int32_t flags_field, const double *domain_lo, const double *domain_hi, double *table, int32_t max_rows,
+              pg_csv_result *result, pg_workspace ws, cudaStream_t st);
 int dem_setup(pg_dem_particles *d, const pg_dem_params *prm, cudaStream_t st);
 int dem_bin(const pg_box *box, pg_dem_particles *d, const pg_dem_particles *spare, const pg_contacts *c,
             const pg_contacts *spare_c, pg_cells *cells, pg_workspace ws, pg_status *status, cudaStream_t st);
@@ -78,6 +84,7 @@ int pg_struct_sizes(int64_t *out, int n) {
         (int64_t) sizeof(pg_cells), (int64_t) sizeof(pg_neighbor_list), (int64_t) sizeof(pg_lj_params),
         (int64_t) sizeof(pg_workspace), (int64_t) sizeof(pg_dem_particles), (int64_t) sizeof(pg_contacts),
         (int64_t) sizeof(pg_dem_params), (int64_t) sizeof(pg_replica), (int64_t) sizeof(pg_ensemble),
+        (int64_t) sizeof(pg_csv_result),
     };
     const int m = (int) (sizeof(sizes) / sizeof(sizes[0]));
     if(out == nullptr) { return m; }
@@ -251,6 +258,23 @@ int pg_vtk_format_rows(int section, int32_t rows, const int32_t *order, const do
 
 int pg_vtk_pack_rows(int32_t rows, pg_workspace ws, const int64_t *offsets, char *out, void *stream) {
     return pg::vtk_pack_rows(rows, ws, offsets, out, S(stream));
+}
+
+int64_t pg_csv_count_bytes(int64_t bytes) { return pg::csv_count_bytes(bytes); }
+
+int pg_csv_count_lines(const char *text, int64_t bytes, int64_t *lines, pg_workspace ws, void *stream) {
+    return pg::csv_count_lines(text, bytes, lines, ws, S(stream));
+}
+
+int64_t pg_csv_workspace_bytes(int64_t bytes, int64_t lines, int32_t nfields) {
+    return pg::csv_workspace_bytes(bytes, lines, nfields);
+}
+
+int pg_csv_parse(const char *text, int64_t bytes, int64_t lines, int32_t nfields, const int32_t *kinds,
+                 int32_t pos_field, int32_t flags_field, const double *domain_lo, const double *domain_hi,
+                 double *table, int32_t max_rows, pg_csv_result *result, pg_workspace ws, void *stream) {
+    return pg::csv_parse(text, bytes, lines, nfields, kinds, pos_field, flags_field, domain_lo, domain_hi, table,
+                         max_rows, result, ws, S(stream));
 }
 
 int pg_stream_sync(void *stream) {

@@ -121,9 +121,25 @@ __global__ void k_scan_apply(const int32_t *in, int n, const int32_t *block_sums
     const int ex = block_exclusive_scan(v, s, total) + block_sums[blockIdx.x];
     if(i < n) {
         out[i] = ex;
-        cursor[i] = 0;
+        if(cursor != nullptr) { cursor[i] = 0; }
         if(i == n - 1) { out[n] = ex + v; }
     }
+}
+
+// Exclusive scan of n int32 values into out[0 .. n] (out[n] = the total) with the three
+// kernels above; block_sums holds scan_block_sums_len(n) values.
+int64_t scan_block_sums_len(int n) { return n < 0 ? 0 : ((int64_t) n + kScanBlock - 1) / kScanBlock + 1; }
+
+int scan_exclusive_i32(const int32_t *in, int n, int32_t *out, int32_t *block_sums, cudaStream_t st) {
+    if(n <= 0) {
+        if(n == 0) { cudaMemsetAsync(out, 0, sizeof(int32_t), st); }
+        return n == 0 ? launch_status() : PG_ERR_ARGUMENT;
+    }
+    const int nb = (n + kScanBlock - 1) / kScanBlock;
+    k_scan_block_sums<<<nb, kScanBlock, 0, st>>>(in, n, block_sums); note_launch();
+    k_scan_sums<<<1, kScanBlock, 0, st>>>(block_sums, nb); note_launch();
+    k_scan_apply<<<nb, kScanBlock, 0, st>>>(in, n, block_sums, out, nullptr); note_launch();
+    return launch_status();
 }
 
 __global__ void k_scatter(int n, const int32_t *particle_cell, const int32_t *start,

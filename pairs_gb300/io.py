@@ -1,11 +1,14 @@
 """Particle input and output formats of the reference.
 
-read_particle_data  runtime/read_from_file.hpp:121-203: CSV, one particle per line,
+read_particle_data  runtime/read_from_file.hpp:33-116: CSV, one particle per line,
                     fields in the declared property order; a vector property takes
                     3 fields, a matrix 9, a quaternion 4; a particle is kept when its
                     position is inside the domain (x >= min, x < max - 1e-5 per
                     dimension, regular_6d_stencil.cpp:96-100) or its flags mark it
-                    infinite, fixed or global; its shape is set to `shape_id`.
+                    infinite, fixed or global; its shape is set to `shape_id`.  With a
+                    GPU the file's bytes go to the device and are indexed, parsed,
+                    filtered and compacted there (pg_csv_parse, csrc/csv.cu);
+                    parse_particle_csv is the host restatement it is tested against.
 write_vtk           runtime/vtk.hpp:11-86: legacy VTK ASCII unstructured grid of the
                     positions (vertices) with the mass as point data, 8 decimals,
                     infinite particles left out, file <name>_<timestep>.vtk.  The rows
@@ -45,14 +48,66 @@ def parse_particle_csv(lines, prop_types):
     return cols
 
 
-def read_particle_data(sim, filename, prop_names, shape_id):
-    """State dict (pos, vel, mass, type, uid, flags, shape, and any other declared
-    per-particle property by name) from a reference-format CSV file."""
-    with open(filename) as f:
-        lines = f.readlines()
-    props = [sim.property(p) for p in prop_names]
+def _field_plan(props):
+    """Per property its first field and width; the field kinds (PG_CSV_INT for the
+    integer types, PG_CSV_REAL otherwise)."""
+    from . import _capi as A
+    plan, kinds, off = [], [], 0
+    for p in props:
+        w = _WIDTH.get(p.type, 1)
+        plan.append((p, off, w))
+        kinds += [A.PG_CSV_INT if p.type in (Types.Int32, Types.Int64, Types.UInt64) else A.PG_CSV_REAL] * w
+        off += w
+    return plan, kinds
+
+
+def csv_table_device(data, kinds, pos_field=-1, flags_field=-1, lo=None, hi=None, device=None):
+    """Parse CSV bytes on the GPU (pg_count_lines + pg_csv_parse): the kept rows as a
+    float64 tensor [nfields, rows] on the device (integer fields as exact doubles).
+    Raises PairsError for a malformed line (naming it) or a number outside the exact
+    conversion range."""
+    import torch
+    from . import _capi as A
+    lib = A.load()
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    raw = np.frombuffer(bytes(data), dtype=np.uint8)
+    nbytes, nf = int(raw.size), len(kinds)
+    text = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
+    if nbytes:
+        text[:nbytes].copy_(torch.from_numpy(raw.copy()).pin_memory())
+    sh = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    cb = int(lib.pg_csv_count_bytes(nbytes))
+    ws = torch.empty(max(cb, 16), dtype=torch.uint8, device=dev)
+    lines = C.c_int64(0)
+    A.call("pg_csv_count_lines", C.c_void_p(text.data_ptr()), nbytes, C.byref(lines),
+           A.PgWorkspace(ws.data_ptr(), ws.numel()), sh)
+    nl = int(lines.value)
+    wb = int(lib.pg_csv_workspace_bytes(nbytes, nl, nf))
+    if wb < 0:
+        raise A.PairsError(f"CSV input: {nf} fields per line is more than the reader takes")
+    ws = torch.empty(max(wb, 16), dtype=torch.uint8, device=dev)
+    table = torch.empty((nf, max(nl, 1)), dtype=torch.float64, device=dev)
+    kind_arr = (C.c_int32 * nf)(*kinds)
+    dlo = (C.c_double * 3)(*lo) if lo is not None else None
+    dhi = (C.c_double * 3)(*hi) if hi is not None else None
+    res = A.PgCsvResult()
+    rc = lib.pg_csv_parse(C.c_void_p(text.data_ptr()), nbytes, nl, nf, kind_arr, int(pos_field), int(flags_field),
+                          dlo, dhi, C.c_void_p(table.data_ptr()), max(nl, 1), C.byref(res),
+                          A.PgWorkspace(ws.data_ptr(), ws.numel()), sh)
+    if res.bad_line >= 0:
+        raise A.PairsError(f"CSV input: line {res.bad_line + 1} has a missing or malformed field")
+    if res.inexact > 0:
+        raise A.PairsError(f"CSV input: {res.inexact} numbers have more than 19 significant digits or a decimal "
+                           "exponent beyond +-27 (outside the reader's exact conversion)")
+    if rc != A.PG_OK:
+        raise A.PairsError(f"pg_csv_parse failed: {rc}")
+    return table[:, : res.rows]
+
+
+def _kept_host(sim, props, lines):
+    """The host restatement: per property the kept rows as numpy arrays."""
     cols = parse_particle_csv(lines, [p.type for p in props])
-    n = len(lines) if not cols else len(cols[0])
+    n = 0 if not cols else len(cols[0])
     data = {p.name: np.array(cols[k]) for k, p in enumerate(props)}
     pos_name = sim.position_prop.name
     lo, hi = sim.grid if sim.grid is not None else ([-np.inf] * 3, [np.inf] * 3)
@@ -62,10 +117,43 @@ def read_particle_data(sim, filename, prop_names, shape_id):
         inside &= (pos[:, d] >= lo[d]) & (pos[:, d] < hi[d] - _SMALL)
     flags = data.get("flags", np.zeros(n, dtype=np.int64)).astype(np.int64)
     keep = inside | ((flags & (Flags.Infinite | Flags.Fixed | Flags.Global)) != 0)
+    return {name: arr[keep] for name, arr in data.items()}
+
+
+def _kept_device(sim, props, raw):
+    """The device reader: per property the kept rows, parsed on the GPU."""
+    plan, kinds = _field_plan(props)
+    pos_name = sim.position_prop.name
+    pos_field = next((off for p, off, w in plan if p.name == pos_name), -1)
+    flags_field = next((off for p, off, w in plan if p.name == "flags"), -1)
+    lo, hi = (sim.grid if sim.grid is not None else (None, None))
+    table = csv_table_device(raw, kinds, pos_field, flags_field, lo, hi).cpu().numpy()
     out = {}
-    for name, arr in data.items():
-        out[name] = arr[keep]
-    m = int(keep.sum())
+    for p, off, w in plan:
+        col = table[off:off + w].T if w > 1 else table[off]
+        out[p.name] = col.astype(np.int64) if kinds[off] == 1 else col
+    return out
+
+
+def read_particle_data(sim, filename, prop_names, shape_id, device=None):
+    """State dict (pos, vel, mass, type, uid, flags, shape, and any other declared
+    per-particle property by name) from a reference-format CSV file.  device: parse on
+    the GPU (the default when one is present) or with the host restatement (False)."""
+    props = [sim.property(p) for p in prop_names]
+    if device is None:
+        try:
+            import torch
+            device = torch.cuda.is_available()
+        except ImportError:
+            device = False
+    if device:
+        with open(filename, "rb") as f:
+            out = _kept_device(sim, props, f.read())
+    else:
+        with open(filename) as f:
+            out = _kept_host(sim, props, f.readlines())
+    pos_name = sim.position_prop.name
+    m = len(out[pos_name])
 
     def get(name, default):
         if name in out:
@@ -79,7 +167,7 @@ def read_particle_data(sim, filename, prop_names, shape_id):
         return np.full((m,) if width == 1 else (m, width), val, dtype=np.float64)
 
     vel_name = "linear_velocity"
-    state = dict(pos=out[pos_name].reshape(m, 3).astype(np.float64),
+    state = dict(pos=np.asarray(out[pos_name], dtype=np.float64).reshape(m, 3),
                  vel=np.asarray(get(vel_name, 0.0), dtype=np.float64).reshape(m, 3) if vel_name in sim.properties
                  else np.zeros((m, 3)),
                  mass=np.asarray(get("mass", 1.0), dtype=np.float64).reshape(m),
