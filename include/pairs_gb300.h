@@ -636,6 +636,25 @@ int pg_csv_parse(const char *text, int64_t bytes, int64_t lines, int32_t nfields
                  int32_t pos_field, int32_t flags_field, const double *domain_lo, const double *domain_hi,
                  double *table, int32_t max_rows, pg_csv_result *result, pg_workspace ws, void *stream);
 
+/* ---- DEM simple-cubic initialiser on the device -----------------------------
+ * Replaces dem_sc_grid (runtime/dem_sc_grid.hpp:62-172) on one rank: spheres on the grid
+ * points spacing/2 + k*spacing inside [0, xmax) x [0, ymax) x [diameter, zmax), x
+ * fastest; a point inside the domain [lo, hi - 1e-5) is kept with uid = its visit
+ * number + 1, a diameter drawn uniformly in [min_diameter, max_diameter) from a
+ * default-seeded std::mt19937 (one draw per visited point, libstdc++'s
+ * generate_canonical: two 32-bit words per draw), velocity (0.1 U(-v0, v0), 0.1
+ * U(-v0, v0), -v0) from two more draws, mass 4/3 pi r^3 density and type rand() %
+ * ntypes (glibc rand(), default seed); bit-identical to the reference on one rank.
+ * pg_dem_sc_grid_size gives the visited and kept counts and the workspace bytes (host
+ * arithmetic only).  Outputs are double4 pos and vel, and per sphere mass, radius,
+ * type, uid; capacity is their length.  The call synchronises the stream. */
+int pg_dem_sc_grid_size(double xmax, double ymax, double zmax, double spacing, double diameter, const double *lo,
+                        const double *hi, int64_t *npoints, int64_t *nkept, int64_t *ws_bytes);
+int pg_dem_sc_grid(double xmax, double ymax, double zmax, double spacing, double diameter, double min_diameter,
+                   double max_diameter, double initial_velocity, double density, int32_t ntypes, const double *lo,
+                   const double *hi, double *pos, double *vel, double *mass, double *radius, int32_t *type,
+                   int32_t *uid, int64_t capacity, pg_workspace ws, void *stream);
+
 /* cudaStreamSynchronize, returning PG_OK or PG_ERR_CUDA. */
 int pg_stream_sync(void *stream);
 

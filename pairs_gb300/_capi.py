@@ -156,6 +156,10 @@ SIGNATURES = {
     "pg_csv_parse": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32, P(C.c_int32), C.c_int32, C.c_int32,
                                P(C.c_double), P(C.c_double), C.c_void_p, C.c_int32, P(PgCsvResult), PgWorkspace,
                                C.c_void_p]),
+    "pg_dem_sc_grid_size": (C.c_int, [C.c_double] * 5 + [P(C.c_double), P(C.c_double), P(C.c_int64),
+                                                           P(C.c_int64), P(C.c_int64)]),
+    "pg_dem_sc_grid": (C.c_int, [C.c_double] * 9 + [C.c_int32, P(C.c_double), P(C.c_double)] + [C.c_void_p] * 6
+                       + [C.c_int64, PgWorkspace, C.c_void_p]),
     "pg_vtk_workspace_bytes": (C.c_int64, [C.c_int32]),
     "pg_vtk_format_rows": (C.c_int, [C.c_int, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      PgWorkspace, C.c_void_p]),

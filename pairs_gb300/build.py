@@ -23,7 +23,10 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I", INCLUDE, "-I", CSRC]
 # per-file flags: the FP64 DEM kernels follow the reference's operation order with
 # every multiply and add separately rounded
-FILE_FLAGS = {"dem.cu": ["-fmad=false"]}
+FILE_FLAGS = {"dem.cu": ["-fmad=false"],
+              # the DEM grid's host-side axis coordinates (ref + k * spacing) must not be
+              # contracted into a fused multiply-add (the host compiler on aarch64 would)
+              "demgrid.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc():

@@ -52,6 +52,12 @@ int vtk_format_rows(int what, int32_t rows, const int32_t *order, const double *
                     const int32_t *index, pg_workspace ws, cudaStream_t st);
 int vtk_pack_rows(int32_t rows, pg_workspace ws, const int64_t *offset, char *out, cudaStream_t st);
 int64_t csv_count_bytes(int64_t bytes);
+int dem_sc_grid_size(double xmax, double ymax, double zmax, double spacing, double diameter, const double *lo,
+                     const double *hi, int64_t *npoints, int64_t *nkept, int64_t *ws_bytes);
+int dem_sc_grid(double xmax, double ymax, double zmax, double spacing, double diameter, double min_diameter,
+                double max_diameter, double initial_velocity, double density, int ntypes, const double *lo,
+                const double *hi, double *pos, double *vel, double *mass, double *radius, int32_t *type,
+                int32_t *uid, int64_t capacity, pg_workspace ws, cudaStream_t st);
 int csv_count_lines(const char *text, int64_t bytes, int64_t *lines, pg_workspace ws, cudaStream_t st);
 int64_t csv_workspace_bytes(int64_t bytes, int64_t lines, int32_t nfields);
 int csv_parse(const char *text, int64_t bytes, int64_t lines, int32_t nfields, const int32_t *kinds, int32_t pos_field,
@@ -275,6 +281,19 @@ int pg_csv_parse(const char *text, int64_t bytes, int64_t lines, int32_t nfields
                  double *table, int32_t max_rows, pg_csv_result *result, pg_workspace ws, void *stream) {
     return pg::csv_parse(text, bytes, lines, nfields, kinds, pos_field, flags_field, domain_lo, domain_hi, table,
                          max_rows, result, ws, S(stream));
+}
+
+int pg_dem_sc_grid_size(double xmax, double ymax, double zmax, double spacing, double diameter, const double *lo,
+                        const double *hi, int64_t *npoints, int64_t *nkept, int64_t *ws_bytes) {
+    return pg::dem_sc_grid_size(xmax, ymax, zmax, spacing, diameter, lo, hi, npoints, nkept, ws_bytes);
+}
+
+int pg_dem_sc_grid(double xmax, double ymax, double zmax, double spacing, double diameter, double min_diameter,
+                   double max_diameter, double initial_velocity, double density, int32_t ntypes, const double *lo,
+                   const double *hi, double *pos, double *vel, double *mass, double *radius, int32_t *type,
+                   int32_t *uid, int64_t capacity, pg_workspace ws, void *stream) {
+    return pg::dem_sc_grid(xmax, ymax, zmax, spacing, diameter, min_diameter, max_diameter, initial_velocity, density,
+                           ntypes, lo, hi, pos, vel, mass, radius, type, uid, capacity, ws, S(stream));
 }
 
 int pg_stream_sync(void *stream) {

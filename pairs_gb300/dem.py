@@ -566,8 +566,12 @@ def build_dem_engine(sim, **over):
     for kind, args in sim.setups:
         if kind == "dem_sc_grid":
             xmax, ymax, zmax, spacing, diam, dmin, dmax, v0, dens, ntypes = args
-            parts.append(lattice.dem_sc_grid(xmax, ymax, zmax, spacing, diam, dmin, dmax, v0, dens, ntypes,
-                                             lo=lo, hi=hi))
+            # generated on the device (bit-identical to the host restatement lattice.dem_sc_grid)
+            g = lattice.dem_sc_grid_device(xmax, ymax, zmax, spacing, diam, dmin, dmax, v0, dens, ntypes,
+                                           lo=lo, hi=hi)
+            g = {k: v.cpu().numpy() for k, v in g.items()}
+            g["pos"], g["vel"] = g["pos"][:, :3], g["vel"][:, :3]
+            parts.append(g)
         elif kind == "read":
             st = read_particle_data(sim, *args)
             m = len(st["pos"])

@@ -228,6 +228,37 @@ def dem_sc_grid(xmax, ymax, zmax, spacing, diameter, min_diameter, max_diameter,
                 uid=(keep + 1).astype(np.int32), flags=np.zeros(n, np.int32), shape=np.zeros(n, np.int32))
 
 
+def dem_sc_grid_device(xmax, ymax, zmax, spacing, diameter, min_diameter, max_diameter, initial_velocity, density,
+                       ntypes, lo=(0.0, 0.0, 0.0), hi=None, device=None):
+    """dem_sc_grid generated on the GPU (pg_dem_sc_grid, csrc/demgrid.cu): the same
+    spheres, bit-identical, as torch tensors on the device (pos and vel n x 4, the
+    fourth component zero)."""
+    import ctypes as C
+    import torch
+    from . import _capi as A
+    lib = A.load()
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    hi = (xmax, ymax, zmax) if hi is None else hi
+    dlo, dhi = (C.c_double * 3)(*[float(v) for v in lo]), (C.c_double * 3)(*[float(v) for v in hi])
+    npts, kept, wsb = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+    A.call("pg_dem_sc_grid_size", float(xmax), float(ymax), float(zmax), float(spacing), float(diameter), dlo, dhi,
+           C.byref(npts), C.byref(kept), C.byref(wsb))
+    n = int(kept.value)
+    f64 = dict(dtype=torch.float64, device=dev)
+    out = dict(pos=torch.zeros((n, 4), **f64), vel=torch.zeros((n, 4), **f64), mass=torch.zeros(n, **f64),
+               radius=torch.zeros(n, **f64), type=torch.zeros(n, dtype=torch.int32, device=dev),
+               uid=torch.zeros(n, dtype=torch.int32, device=dev))
+    ws = torch.empty(max(int(wsb.value), 16), dtype=torch.uint8, device=dev)
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    A.call("pg_dem_sc_grid", float(xmax), float(ymax), float(zmax), float(spacing), float(diameter),
+           float(min_diameter), float(max_diameter), float(initial_velocity), float(density), int(ntypes), dlo, dhi,
+           ptr(out["pos"]), ptr(out["vel"]), ptr(out["mass"]), ptr(out["radius"]), ptr(out["type"]), ptr(out["uid"]),
+           n, A.PgWorkspace(ws.data_ptr(), ws.numel()), C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    out["flags"] = torch.zeros(n, dtype=torch.int32, device=dev)
+    out["shape"] = torch.zeros(n, dtype=torch.int32, device=dev)
+    return out
+
+
 # ---------------------------------------------------------------------------- ensembles
 
 def trimmed_fcc(natoms, rho, temperature, uid0=0):
