@@ -203,6 +203,7 @@ typedef struct {
     double  lo[3];
     double  len[3];
     double  cell_len[3];
+    double  inv_cell_len[3];     /* 1 / cell_len (the binning multiplies by it) */
     double  quantum;             /* grid step of this replica's pos_hi */
     float   len_hi[3];
     float   len_lo[3];

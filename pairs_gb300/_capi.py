@@ -103,7 +103,8 @@ class PgDemParams(C.Structure):
 class PgReplica(C.Structure):
     _fields_ = [("first", C.c_int32), ("n", C.c_int32), ("cell0", C.c_int32), ("ncells", C.c_int32),
                 ("dims", C.c_int32 * 3), ("reach", C.c_int32), ("lo", C.c_double * 3), ("len", C.c_double * 3),
-                ("cell_len", C.c_double * 3), ("quantum", C.c_double), ("len_hi", C.c_float * 3),
+                ("cell_len", C.c_double * 3), ("inv_cell_len", C.c_double * 3), ("quantum", C.c_double),
+                ("len_hi", C.c_float * 3),
                 ("len_lo", C.c_float * 3), ("fx_scale", C.c_double * 3), ("fx_unit", C.c_float * 3),
                 ("fx_pad_", C.c_int32)]
 

@@ -73,9 +73,11 @@ __global__ void __launch_bounds__(kBlock) k_ens_count(EnsArgs a, int32_t *count)
         atomicExch(&a.status->nonfinite, 1);
         cell = a.e.ncells;
     } else {
+        // multiplied by the inverse, floor and conversion in one round-down conversion
+        // (a division per axis made this pass FP64-bound: 301 us at 3.7M atoms)
         int idx = 0;
         for(int d = 0; d < 3; d++) {
-            int c = (int) floor((c3[d] - R.lo[d]) / R.cell_len[d]);
+            int c = __double2int_rd(__dmul_rn(__dsub_rn(c3[d], R.lo[d]), R.inv_cell_len[d]));
             c = c < 0 ? 0 : (c >= R.dims[d] ? R.dims[d] - 1 : c);
             idx = idx * R.dims[d] + c;
         }

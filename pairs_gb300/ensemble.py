@@ -160,6 +160,7 @@ class Ensemble:
                 R.lo[d] = 0.0
                 R.len[d] = L[d]
                 R.cell_len[d] = L[d] / dims
+                R.inv_cell_len[d] = 1.0 / R.cell_len[d]
                 nc *= dims
             R.ncells = nc
             R.reach = self.reach
