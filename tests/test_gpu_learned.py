@@ -157,6 +157,40 @@ def test_learned_schedule_time_per_step_at_32cube():
     assert ms["learned"] < 1.25 * ms["ema"], ms
 
 
+def test_learned_schedule_follows_a_cooling_at_once():
+    """What the learned schedule buys on a non-stationary system.  After calibration on
+    a liquid at T ~ 0.7, the velocities are halved (the cycle until the first trip about
+    doubles).  The network reads the new speeds in the features of the next build and
+    predicts the longer cycles at once; the EMA of past lengths only grows by a fraction
+    of its margin per cycle that ends before a trip, so it keeps rebuilding at the old
+    rate for many cycles.  Over the next 300 steps the learned schedule makes close to
+    the guard's (exact, on-trip) number of rebuilds and clearly fewer than the EMA."""
+    from pairs_gb300.engine import LJEngine
+    st = lattice.copper_fcc_lattice(24, 24, 24)
+    builds = {}
+    for policy in ("guard", "ema", "learned"):
+        eng = LJEngine(st, precision="mixed", half=True, sync="exact", policy=policy)
+        k = 0
+        while eng.schedule is not None and not eng.schedule.trained and k < 2000:
+            eng.step()
+            k += 1
+        eng.run(max(0, 200 - k))
+        pos, vel, _ = eng.state()
+        order = np.argsort(np.asarray(st["uid"]), kind="stable")
+        uid = np.asarray(st["uid"], dtype=np.int32)[order]
+        mass = np.asarray(st["mass"], dtype=np.float64)[order]
+        eng.upload(torch.from_numpy(pos).pin_memory(), torch.from_numpy(0.5 * vel).pin_memory(),
+                   mass=torch.from_numpy(mass).pin_memory(), uid=torch.from_numpy(uid).pin_memory())
+        b0 = eng.nbuilds
+        eng.run(300)
+        eng.settle()
+        builds[policy] = eng.nbuilds - b0
+        del eng
+    g, e, l = builds["guard"], builds["ema"], builds["learned"]
+    assert l <= 1.35 * g, builds
+    assert l < 0.8 * e, builds
+
+
 @pytest.mark.parametrize("half", [True, False])
 def test_cell_features_match_a_host_computation(half):
     """pg_cell_features against numpy on the engine's own cells: per cell max|v| dt /
