@@ -157,14 +157,15 @@ def test_learned_schedule_time_per_step_at_32cube():
     assert ms["learned"] < 1.25 * ms["ema"], ms
 
 
-def test_learned_schedule_follows_a_cooling_at_once():
-    """What the learned schedule buys on a non-stationary system.  After calibration on
-    a liquid at T ~ 0.7, the velocities are halved (the cycle until the first trip about
-    doubles).  The network reads the new speeds in the features of the next build and
-    predicts the longer cycles at once; the EMA of past lengths only grows by a fraction
-    of its margin per cycle that ends before a trip, so it keeps rebuilding at the old
-    rate for many cycles.  Over the next 300 steps the learned schedule makes close to
-    the guard's (exact, on-trip) number of rebuilds and clearly fewer than the EMA."""
+def test_learned_schedule_follows_a_cooling():
+    """A non-stationary case.  After calibration on a liquid at T ~ 0.7, the velocities
+    are halved; the cycle until the first trip grows and then shortens again as the
+    liquid re-heats from its potential energy.  The network reads the new speeds in the
+    features of each build, so its cycles follow the exact on-trip schedule (the guard's
+    rebuild count) with no retraining.  Measured over the next 300 steps of fcc 24^3:
+    guard 32, EMA 33, learned 33 rebuilds; the EMA of past lengths, which overshoots into
+    cheap rewinds and lengthens a cycle that ended before a trip, follows as closely, so
+    the bound below is against both and claims no gain over the EMA."""
     from pairs_gb300.engine import LJEngine
     st = lattice.copper_fcc_lattice(24, 24, 24)
     builds = {}
@@ -187,8 +188,8 @@ def test_learned_schedule_follows_a_cooling_at_once():
         builds[policy] = eng.nbuilds - b0
         del eng
     g, e, l = builds["guard"], builds["ema"], builds["learned"]
-    assert l <= 1.35 * g, builds
-    assert l < 0.8 * e, builds
+    assert l <= 1.2 * g, builds
+    assert l <= 1.2 * e, builds
 
 
 @pytest.mark.parametrize("half", [True, False])
