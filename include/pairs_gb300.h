@@ -68,7 +68,8 @@ extern "C" {
 typedef struct {
     int32_t overflow;            /* bit 0 cells, bit 1 neighbours, bit 2 tile
                                     neighbourhood, bit 3 contacts; bit 4: a grid
-                                    barrier of pg_lj_steps ran out of time */
+                                    barrier of pg_lj_steps or pg_ensemble_steps ran out
+                                    of time */
     int32_t max_cell_count;      /* largest cell occupancy seen */
     int32_t max_neighbors;       /* largest per-particle Verlet count seen */
     int32_t nonfinite;           /* set when a non-finite value was met */
@@ -536,6 +537,22 @@ int pg_ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neig
  * word takes the first step at which any replica's particle moved > skin/2. */
 int pg_ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift,
                           double half_skin2, int32_t step, pg_status *status, void *stream);
+
+/* The plain steps first .. first + nsteps - 1 of every replica in one cooperative
+ * launch: per step pg_ensemble_integrate (two half kicks, drift), pg_ensemble_force
+ * and its cutoff-band decisions, separated by grid barriers -- the same arithmetic, in
+ * place of 2 nsteps launches under a CUDA graph (the generated code launches and
+ * synchronises every module of every step, src/pairs/code_gen/cgen.py:540-576).
+ * Needs fixed-point positions (pos_fx, ref_fx) and force32.  A guard trip in the
+ * integration of step r ends the launch before the force of step r (status->
+ * guard_tripped = r), as the separate kernels would skip themselves.  ws: scratch as
+ * for pg_ensemble_force (its first 256 bytes hold the queue count and the barrier
+ * words).  No barrier waits longer than timeout_s (2 s when <= 0): then
+ * status->overflow gets bit 4 and the state is that of an unfinished step.  A call
+ * with nsteps = 0 only prepares the launch (make it before a stream capture). */
+int pg_ensemble_steps(const pg_ensemble *e, pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
+                      double dt, double half_skin2, int32_t first, int32_t nsteps, pg_status *status,
+                      pg_workspace ws, double timeout_s, void *stream);
 
 /* Per-replica thermo: out[2r] = T_r = sum/(3 n_r - 3), out[2r+1] = sum m v^2 (FP64,
  * one block per replica, fixed order).  out: device double[2 * nreplicas]. */

@@ -186,6 +186,9 @@ SIGNATURES = {
     "pg_ensemble_integrate": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_double, C.c_int, C.c_int, C.c_double,
                                         C.c_int32, C.c_void_p, C.c_void_p]),
     "pg_ensemble_thermo": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_void_p, C.c_void_p]),
+    "pg_ensemble_steps": (C.c_int, [P(PgEnsemble), P(PgParticles), P(PgNeighborList), P(PgLJParams), C.c_double,
+                                    C.c_double, C.c_int32, C.c_int32, C.c_void_p, PgWorkspace, C.c_double,
+                                    C.c_void_p]),
     "pg_dem_setup": (C.c_int, [P(PgDemParticles), P(PgDemParams), C.c_void_p]),
     "pg_dem_bin": (C.c_int, [P(PgBox), P(PgDemParticles), P(PgDemParticles), P(PgContacts), P(PgContacts),
                              P(PgCells), PgWorkspace, C.c_void_p, C.c_void_p]),

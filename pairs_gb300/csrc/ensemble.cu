@@ -17,6 +17,7 @@
 // tpa, the block size and the stencil reach (27 cells of >= r_list or 125 cells of
 // >= r_list/2) by timing them on the ensemble itself.
 #include "common.cuh"
+#include "persist.cuh"
 
 namespace pg {
 
@@ -309,16 +310,24 @@ __device__ __forceinline__ void ens_pair_delta(const RepLen &L, const int4 &fi, 
     }
 }
 
-template<int TPA, bool kOneType, bool kFixed>
-__global__ void k_ens_force(EnsArgs a) {
-    if(frozen_force(a.p)) { return; }
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+// fixed-point record of particle i: through the read-only path, or (kCoherent) through
+// L2 only, for a kernel that rewrites the positions while it runs (persistent steps)
+template<bool kCoherent>
+__device__ __forceinline__ int4 ens_ld_fx(const int32_t *base, int i) {
+    const int4 *p = reinterpret_cast<const int4 *>(base) + i;
+    return kCoherent ? __ldcg(p) : __ldg(p);
+}
+
+// The pair forces of item g (particle g / TPA, lane g % TPA); every lane of a warp calls
+// it (the lanes of a particle combine with shuffles), items past the particles idle.
+template<int TPA, bool kOneType, bool kFixed, bool kCoherent>
+__device__ __forceinline__ void ens_force_item(const EnsArgs &a, int g) {
     const int i = g / TPA, t = g % TPA;
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     if(i < a.p.n) {
         float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
         int4 fi = make_int4(0, 0, 0, 0);
-        if(kFixed) { fi = ld_i4(a.p.pos_fx, i); }
+        if(kFixed) { fi = ens_ld_fx<kCoherent>(a.p.pos_fx, i); }
         else { hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i)); }
         const RepLen L = rep_len(a.e.replicas[a.e.replica_of[i]]);
         const int ti = kOneType ? 0 : (kFixed ? fi.w : __float_as_int(hi.w)) * a.ntypes;
@@ -339,7 +348,7 @@ __global__ void k_ens_force(EnsArgs a) {
             for(int u = 0; u < kEnsBatch; u++) {
                 const int j = (int) (e[u] & PG_NBR_INDEX_MASK);
                 if(kFixed) {
-                    fj[u] = ld_i4(a.p.pos_fx, j);
+                    fj[u] = ens_ld_fx<kCoherent>(a.p.pos_fx, j);
                     hj[u] = lj[u] = make_float4(0.f, 0.f, 0.f, 0.f);
                 } else {
                     hj[u] = ld_f4(a.p.pos_hi, hl(a.p, j));
@@ -386,18 +395,37 @@ __global__ void k_ens_force(EnsArgs a) {
     }
 }
 
+template<int TPA, bool kOneType, bool kFixed>
+__global__ void k_ens_force(EnsArgs a) {
+    if(frozen_force(a.p)) { return; }
+    ens_force_item<TPA, kOneType, kFixed, false>(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // One pair of the cutoff band: the FP64 test of the single-system FP64 path decides;
 // a pair inside adds its FP32 force (full lists: no reaction).
-template<bool kOneType, bool kFixed>
+// the FP64 cutoff test of a listed image through L2-only loads (persistent steps)
+__device__ __forceinline__ bool exact_inside_coherent(const double *pos, int i, int j, uint32_t code, const double *len,
+                                                      double cutoff2) {
+    const double2 *pi = reinterpret_cast<const double2 *>(pos + 4 * (size_t) i);
+    const double2 *pj = reinterpret_cast<const double2 *>(pos + 4 * (size_t) j);
+    const double2 ai = __ldcg(pi), bi = __ldcg(pi + 1), aj = __ldcg(pj), bj = __ldcg(pj + 1);
+    const double jx = ref_image(aj.x, image_shift(code, 0), len[0]);
+    const double jy = ref_image(aj.y, image_shift(code, 1), len[1]);
+    const double jz = ref_image(bj.x, image_shift(code, 2), len[2]);
+    return ref_rsq(__dsub_rn(ai.x, jx), __dsub_rn(ai.y, jy), __dsub_rn(bi.x, jz)) < cutoff2;
+}
+
+template<bool kOneType, bool kFixed, bool kCoherent = false>
 __device__ __forceinline__ void ens_fixup_pair(const EnsArgs &a, int i, uint32_t e) {
     const int j = (int) (e & PG_NBR_INDEX_MASK);
     const uint32_t code = e >> PG_NBR_INDEX_BITS;
     const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
-    if(!exact_inside(a.p.pos, i, j, code, R.len, a.cutoff2d)) { return; }
+    if(kCoherent ? !exact_inside_coherent(a.p.pos, i, j, code, R.len, a.cutoff2d)
+                 : !exact_inside(a.p.pos, i, j, code, R.len, a.cutoff2d)) { return; }
     float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi, hj = hi, lj = hi;
     int4 fi = make_int4(0, 0, 0, 0), fj = fi;
     if(kFixed) {
-        fi = ld_i4(a.p.pos_fx, i); fj = ld_i4(a.p.pos_fx, j);
+        fi = ens_ld_fx<kCoherent>(a.p.pos_fx, i); fj = ens_ld_fx<kCoherent>(a.p.pos_fx, j);
     } else {
         hi = ld_f4(a.p.pos_hi, hl(a.p, i)); lo = ld_f4(a.p.pos_lo, hl(a.p, i));
         hj = ld_f4(a.p.pos_hi, hl(a.p, j)); lj = ld_f4(a.p.pos_lo, hl(a.p, j));
@@ -457,15 +485,18 @@ __device__ __forceinline__ void ens_resplit(double x, float q, float iq, float &
     split_pos(x, (double) iq, (double) q, hi, lo);
 }
 
-__global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
-    if(a.drift ? frozen_integrate(a.p) : frozen_force(a.p)) { return; }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// The integration of particle i (k_ens_integrate); returns whether its guard tripped.
+// kCoherent: the force is read through L2 only (the persistent steps, where other
+// blocks' reactions wrote it during the launch).
+template<bool kCoherent>
+__device__ __forceinline__ bool ens_integrate_item(const EnsArgs &a, int i) {
     bool tripped = false;
     if(i < a.p.n) {
         // a coherent load: with half lists this pass then zeroes the force (it is the last
         // reader before the next force pass, which accumulates reactions into zeros), and a
         // read-only-cache load could be moved past that store
-        const float4 f = reinterpret_cast<const float4 *>(a.p.force32)[i];
+        const float4 f = kCoherent ? __ldcg(reinterpret_cast<const float4 *>(a.p.force32) + i)
+                                   : reinterpret_cast<const float4 *>(a.p.force32)[i];
         const double m = a.p.mass[i];
         const double c = m == 1.0 ? a.kick : a.kick / m;
         D4 v = ld_d4_plain(a.p.vel, i);
@@ -521,8 +552,85 @@ __global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
             if(a.e.half) { st_f4(a.p.force32, i, make_float4(0.0f, 0.0f, 0.0f, 0.0f)); }
         }
     }
+    return tripped;
+}
+
+__global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
+    if(a.drift ? frozen_integrate(a.p) : frozen_force(a.p)) { return; }
+    const bool tripped = ens_integrate_item<false>(a, blockIdx.x * blockDim.x + threadIdx.x);
     if(__any_sync(0xffffffffu, tripped) && (threadIdx.x & 31) == 0) {
         atomicMin(&a.status->guard_tripped, a.step);
+    }
+}
+
+// ------------------------------------------------------------------ persistent steps
+
+// The plain steps of a chunk in one cooperative launch (pg_ensemble_steps): for each
+// step the integration (two half kicks, drift, fixed-point records, the FP64 guard),
+// a grid barrier, the force pass, a barrier, the cutoff band's FP64 decisions, a
+// barrier -- the arithmetic of k_ens_integrate, k_ens_force and k_ens_cutoff_fixup,
+// every replica at once.  Data other blocks rewrite during the launch (fixed-point
+// and FP64 positions, forces) is read through L2 only.  A trip in the integration of
+// step r ends the launch before the force of step r, as the separate kernels skip
+// themselves; a barrier that waits past the time limit sets status->overflow bit 16
+// and every block leaves (persist.cuh).
+constexpr int kEnsPersistBlock = 128;
+
+struct EnsStepsArgs {
+    EnsArgs a;
+    PersistWs ws;
+    int32_t first, nsteps;
+    unsigned long long limit_ns;
+};
+
+template<int TPA, bool kOneType>
+__global__ void __launch_bounds__(kEnsPersistBlock) k_ens_steps(EnsStepsArgs s) {
+    const EnsArgs &a = s.a;
+    const unsigned nblocks = gridDim.x;
+    const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const int n = a.p.n;
+    const volatile int32_t *guard = &a.status->guard_tripped;
+    const float c2 = a.cutoff2, band = c2 * kCutBand;
+    for(int k = 0; k < s.nsteps; k++) {
+        const int32_t r = s.first + k;
+        if(*guard < r) { break; }                    // a trip before this step froze the state
+        if(first == 0) { *s.ws.cut_count = 0; }
+        for(int base = 0; base < n; base += stride) {
+            const bool tripped = ens_integrate_item<true>(a, base + first);
+            if(__any_sync(0xffffffffu, tripped) && (threadIdx.x & 31) == 0) {
+                atomicMin(&a.status->guard_tripped, r);
+            }
+        }
+        if(!grid_barrier(s.ws, nblocks, s.limit_ns, a.status)) { break; }
+        if(*guard <= r) { break; }                   // the host rebuilds at the trip step
+        for(int base = 0; base < n * TPA; base += stride) {
+            ens_force_item<TPA, kOneType, true, true>(a, base + first);
+        }
+        if(!grid_barrier(s.ws, nblocks, s.limit_ns, a.status)) { break; }
+        const int queued = *reinterpret_cast<volatile const int32_t *>(s.ws.cut_count);
+        if(queued <= s.ws.capacity) {
+            for(int q = first; q < queued; q += stride) {
+                const int2 rec = s.ws.records[q];
+                ens_fixup_pair<kOneType, true, true>(a, rec.x, (uint32_t) rec.y);
+            }
+        } else {
+            // more band pairs than the queue holds: every list again (k_ens_cutoff_fixup)
+            const size_t row = (size_t) a.list.stride * TPA;
+            for(int i = first; i < n; i += stride) {
+                const int4 fi = ens_ld_fx<true>(a.p.pos_fx, i);
+                const RepLen L = rep_len(a.e.replicas[a.e.replica_of[i]]);
+                const int cnt = a.list.count[i];
+                for(int m = 0; m < cnt; m++) {
+                    const uint32_t e = (uint32_t) a.list.nbr[(size_t) (m / TPA) * row + (size_t) i * TPA + m % TPA];
+                    const int4 fj = ens_ld_fx<true>(a.p.pos_fx, (int) (e & PG_NBR_INDEX_MASK));
+                    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float dx, dy, dz;
+                    ens_pair_delta<true>(L, fi, z4, z4, fj, z4, z4, e >> PG_NBR_INDEX_BITS, dx, dy, dz);
+                    if(fabsf(pair_rsq(dx, dy, dz) - c2) < band) { ens_fixup_pair<kOneType, true, true>(a, i, e); }
+                }
+            }
+        }
+        if(!grid_barrier(s.ws, nblocks, s.limit_ns, a.status)) { break; }
     }
 }
 
@@ -667,6 +775,61 @@ int ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kic
     a.step = step;
     a.drift = drift;
     if(p->n > 0) { k_ens_integrate<<<blocks_for(p->n), kBlock, 0, st>>>(a); note_launch(); }
+    return launch_status();
+}
+
+int ensemble_steps(const pg_ensemble *e, pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
+                   double dt, double half_skin2, int32_t first, int32_t nsteps, pg_status *status, pg_workspace ws,
+                   double timeout_s, cudaStream_t st) {
+    if(!ens_ok(e, p) || !list || !list->nbr || !list->count || !lj || !status || nsteps < 0 || !p->pos || !p->vel ||
+       !p->mass || !p->force32 || !p->pos_fx || !p->ref_fx || !p->pos_ref || lj->ntypes < 1 || lj->ntypes > 8 ||
+       (lj->ntypes > 1 && !p->type) || (list->half != 0) != (e->half != 0)) {
+        return PG_ERR_ARGUMENT;
+    }
+    if(ws.ptr == nullptr || ws.bytes < 256 + 8) { return PG_ERR_ARGUMENT; }
+    const bool one = lj->ntypes == 1;
+    typedef void (*Kernel)(EnsStepsArgs);
+    Kernel k;
+    int slot;
+    switch(e->tpa) {
+        case 1: k = one ? k_ens_steps<1, true> : k_ens_steps<1, false>; slot = 0; break;
+        case 2: k = one ? k_ens_steps<2, true> : k_ens_steps<2, false>; slot = 1; break;
+        case 4: k = one ? k_ens_steps<4, true> : k_ens_steps<4, false>; slot = 2; break;
+        default: k = one ? k_ens_steps<8, true> : k_ens_steps<8, false>; slot = 3; break;
+    }
+    int grid = 0;
+    const int rc = cooperative_grid(8 + 2 * slot + (one ? 1 : 0), (const void *) k, kEnsPersistBlock, &grid);
+    if(rc != PG_OK) { return rc; }
+    if(nsteps == 0 || p->n == 0) { return PG_OK; }         // (a call of no steps only prepares the launch)
+    EnsStepsArgs sa = {};
+    EnsArgs &a = sa.a;
+    a.e = *e; a.p = *p; a.list = *list; a.status = status;
+    a.ntypes = lj->ntypes;
+    a.cutoff2 = (float) lj->cutoff2;
+    a.cutoff2d = lj->cutoff2;
+    for(int t = 0; t < lj->ntypes * lj->ntypes; t++) {
+        a.eps[t] = (float) lj->epsilon[t];
+        a.sig6[t] = (float) lj->sigma6[t];
+    }
+    a.dt = dt;
+    a.kick = 2.0 * (dt * 0.5);
+    a.drift = 1;
+    a.half_skin2 = half_skin2;
+    a.half_skin2_lo = (float) (half_skin2 * (1.0 - 1e-3));
+    a.half_skin2_hi = (float) (half_skin2 * (1.0 + 1e-3));
+    sa.ws = persist_ws(ws.ptr, ws.bytes);
+    a.cut_count = sa.ws.cut_count;
+    a.cut_rec = sa.ws.records;
+    a.cut_capacity = sa.ws.capacity;
+    sa.first = first;
+    sa.nsteps = nsteps;
+    sa.limit_ns = timeout_ns(timeout_s);
+    cudaMemsetAsync(ws.ptr, 0, 256, st);                    // queue count, barrier words, abort word
+    void *args[] = {&sa};
+    if(cudaLaunchCooperativeKernel((const void *) k, grid, kEnsPersistBlock, args, 0, st) != cudaSuccess) {
+        return PG_ERR_CUDA;
+    }
+    note_launch();
     return launch_status();
 }
 

@@ -36,76 +36,11 @@
 
 #include "common.cuh"
 #include "lj_packed.cuh"
+#include "persist.cuh"
 
 namespace pg {
 
 constexpr int kPersistBlock = 128;
-constexpr int kBarrierTimeout = 16;          // status->overflow bit: a grid barrier wait ran out
-
-// header of the caller's workspace (the near-cutoff queue's records follow at 256)
-struct PersistWs {
-    int32_t *cut_count;                      // +0
-    unsigned *arrivals;                      // +64
-    unsigned *generation;                    // +128
-    int32_t *abort;                          // +192
-    int2 *records;                           // +256
-    int capacity;
-};
-
-__host__ __device__ inline PersistWs persist_ws(void *base, int64_t bytes) {
-    char *b = reinterpret_cast<char *>(base);
-    PersistWs w;
-    w.cut_count = reinterpret_cast<int32_t *>(b);
-    w.arrivals = reinterpret_cast<unsigned *>(b + 64);
-    w.generation = reinterpret_cast<unsigned *>(b + 128);
-    w.abort = reinterpret_cast<int32_t *>(b + 192);
-    w.records = reinterpret_cast<int2 *>(b + 256);
-    const int64_t cap = (bytes - 256) / 8;
-    w.capacity = (int) (cap < INT32_MAX ? cap : INT32_MAX);
-    return w;
-}
-
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Grid-wide barrier for a cooperative launch of `nblocks` blocks expecting `expected`
-// arrivals.  Returns false when the launch must stop (this or another block's wait ran
-// out); never waits longer than limit_ns.
-__device__ bool grid_barrier(const PersistWs &w, unsigned expected, unsigned long long limit_ns, pg_status *status) {
-    __shared__ int s_go;
-    __syncthreads();
-    if(threadIdx.x == 0) {
-        int go = 1;
-        volatile unsigned *gen = w.generation;
-        volatile int32_t *abort = w.abort;
-        const unsigned g = *gen;
-        __threadfence();                                     // release this block's writes
-        if(atomicAdd(w.arrivals, 1u) == expected - 1) {
-            atomicExch(w.arrivals, 0u);
-            __threadfence();
-            atomicAdd(w.generation, 1u);
-        } else {
-            const unsigned long long t0 = global_ns();
-            while(*gen == g) {
-                if(*abort) { go = 0; break; }
-                if(global_ns() - t0 > limit_ns) {
-                    atomicExch(w.abort, 1);
-                    atomicOr(&status->overflow, kBarrierTimeout);
-                    go = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        s_go = go && *abort == 0;
-    }
-    __syncthreads();
-    __threadfence();                                         // acquire the other blocks' writes
-    return s_go != 0;
-}
 
 struct StepsArgs {
     pg_box box;
@@ -258,11 +193,13 @@ typedef void (*StepsKernel)(StepsArgs);
 // Blocks of a cooperative launch: as many as the device keeps resident at once (all of
 // them must be, for the grid barrier).  Queried once per kernel and device, so that a
 // call inside a stream capture issues nothing but the launch.
-constexpr int kCoopKernels = 5, kCoopDevices = 64;
+constexpr int kCoopKernels = 32, kCoopDevices = 64;
 static std::atomic<int> g_coop_grid[kCoopKernels][kCoopDevices];
 
-static int cooperative_grid(int slot, const void *kernel, int block, int *grid) {
+// slots: 0-3 k_lj_steps, 4 k_barrier_check, 8 + k the ensemble's persistent kernels
+int cooperative_grid(int slot, const void *kernel, int block, int *grid) {
     int dev = 0;
+    if(slot < 0 || slot >= kCoopKernels) { return PG_ERR_ARGUMENT; }
     if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kCoopDevices) { return PG_ERR_CUDA; }
     int g = g_coop_grid[slot][dev].load(std::memory_order_acquire);
     if(g == 0) {
@@ -277,10 +214,6 @@ static int cooperative_grid(int slot, const void *kernel, int block, int *grid) 
     }
     *grid = g;
     return PG_OK;
-}
-
-static unsigned long long timeout_ns(double seconds) {
-    return (unsigned long long) ((seconds > 0.0 ? seconds : 2.0) * 1e9);
 }
 
 int lj_steps(const pg_box *box, pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj, double dt,

@@ -28,7 +28,7 @@ INT32_MAX = 2 ** 31 - 1
 class Ensemble:
     def __init__(self, replicas, *, cutoff=2.5, skin=0.3, dt=0.005, epsilon=1.0, sigma6=1.0, tpa=1, block=256,
                  reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, fixed_point=None,
-                 half=True, device="cuda"):
+                 half=True, persistent=False, device="cuda"):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -37,6 +37,9 @@ class Ensemble:
         self.dev = torch.device(device)
         self.policy = policy
         self.graphs = graphs and policy == "guard"
+        # persistent: a chunk's plain steps as one cooperative launch (pg_ensemble_steps)
+        # instead of two kernel nodes per step; needs fixed-point positions
+        self.persistent = bool(persistent) and policy == "guard"
         self.cutoff, self.skin, self.dt = cutoff, skin, dt
         self.r_list = cutoff + skin
         self.r_list2 = self.r_list * self.r_list
@@ -58,6 +61,8 @@ class Ensemble:
         if fixed_point and not fx_ok:
             raise ValueError("fixed-point positions need every replica box longer than 2 (cutoff + 2 skin)")
         self.fixed_point = fx_ok if fixed_point is None else bool(fixed_point)
+        if self.persistent and not self.fixed_point:
+            raise ValueError("persistent ensemble steps need fixed-point positions")
         self.ts = 0
         self.nbuilds = 0
         self.host_syncs = 0
@@ -249,7 +254,12 @@ class Ensemble:
                step, self.status_ptr, self.sh)
 
     def _chunk_launches(self, k):
-        """Steps 0..k-1 of a speculative chunk (relative step numbers)."""
+        """Steps 0..k-1 of a speculative chunk (relative step numbers): one launch per
+        phase and step, or one persistent launch for the chunk."""
+        if self.persistent:
+            A.call("pg_ensemble_steps", C.byref(self.e), C.byref(self.p), C.byref(self.list), C.byref(self.lj),
+                   self.dt, self.half_skin2, 0, k, self.status_ptr, self.ws, 0.0, self.sh)
+            return
         self.p.guard = self.t["status"].data_ptr() + 4 * 4
         for s in range(k):
             self._integrate(s, 2)
@@ -262,6 +272,10 @@ class Ensemble:
             return
         entry = self._graphs.get(k)
         if entry is None:
+            if self.persistent:
+                # size the cooperative grid now: no device query inside the capture
+                A.call("pg_ensemble_steps", C.byref(self.e), C.byref(self.p), C.byref(self.list),
+                       C.byref(self.lj), self.dt, self.half_skin2, 0, 0, self.status_ptr, self.ws, 0.0, self.sh)
             # first use of this length: capture it (the launches of the capture are
             # not executed; the replay below runs them)
             g = torch.cuda.CUDAGraph()

@@ -126,6 +126,37 @@ def test_graph_chunks_equal_plain_chunks():
 
 
 @pytest.mark.parametrize("half", [False, True])
+def test_persistent_chunks_equal_graph_chunks(half):
+    """A chunk's plain steps in one cooperative launch (pg_ensemble_steps) follow the
+    same chunks as separate kernels under a graph: the same rebuild steps, and the same
+    state bit for bit with full lists (half lists: the reactions' atomics sum in any
+    order, ~1e-7 of a force per step, grown by the liquid's chaos)."""
+    from pairs_gb300.ensemble import Ensemble
+    reps = replicas()
+    a = Ensemble(reps, tpa=2, graphs=True, half=half, persistent=True)
+    b = Ensemble(reps, tpa=2, graphs=True, half=half, persistent=False)
+    assert a.persistent and not b.persistent
+    steps = 30 if half else 120
+    a.run(steps)
+    b.run(steps)
+    a.synchronize()
+    b.synchronize()
+    assert a.nbuilds == b.nbuilds and a.nbuilds > 1
+    for r in range(len(reps)):
+        pa, va, fa = a.replica_state(r)
+        pb, vb, fb = b.replica_state(r)
+        if half:
+            # reaction sums in a run-dependent order; 30 steps keep the liquid's chaos
+            # from growing them (after 120 steps: up to 1.3e-5 in position)
+            assert np.abs(pa - pb).max() < 1e-7 and np.abs(va - vb).max() < 1e-5
+            assert rms_rel(fa, fb) < 1e-4
+        else:
+            assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    # every chunk was one launch
+    assert a.graph_kernels < b.graph_kernels
+
+
+@pytest.mark.parametrize("half", [False, True])
 def test_guard_schedule_keeps_the_pair_set(half):
     """Speculative chunks: after a run, the list rebuilt from the final positions
     holds every pair within the cutoff that the guarded list held (half lists: the
