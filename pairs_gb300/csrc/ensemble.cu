@@ -158,44 +158,19 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
         const int4 fi = fxs ? ld_i4(a.p.pos_fx, i) : make_int4(0, 0, 0, 0);
         int32_t *wp = a.list.nbr + (size_t) i * tpa;       // entry 0 of the interleaved layout
         const size_t row_step = (size_t) stride * tpa - (size_t) (tpa - 1);
-        // the particle's offset inside its cell in x and y; a partner in stencil column
-        // (ox, oy) lies at least g away laterally, so within sqrt(r_list^2 - g^2) in z
-        // (windows widened by 1e-3 sigma and r_list^2 (1 + 1e-3) over the rounding).
-        // Each run of z cells is entered and left by binary search on the particles' z
-        // (cells are sorted by z, so a column's run is).  Measured at 512 replicas (3.7M
-        // atoms, 125-cell stencil): 4.34 ms per rebuild with the binning against 4.76
-        // ms scanning whole cells; FP64 keys in the searches made it 5.98 ms.
-        const float xr = (float) (xi.x - (R.lo[0] + cx * R.cell_len[0]));
-        const float yr = (float) (xi.y - (R.lo[1] + cy * R.cell_len[1]));
-        const float clx = (float) R.cell_len[0], cly = (float) R.cell_len[1];
-        const float r2w = (float) (a.r_list2 * (1.0 + 1.0e-3));
-        constexpr float kMargin = 1.0e-3f;
-        // z keys: the FP32 grid value pos_hi.z (monotone in z, within q/2 << kMargin of it)
-        const float zf = hi.z + lo.z;
         for(int ox = -rr; ox <= rr; ox++) {
             if(ox < -dx_ || ox > dx_) { continue; }
             int nx, sx;
             wrap_cell(cx + ox, dx_, nx, sx);
-            const float gx = ox == 0 ? 0.0f : fmaxf((ox > 0 ? ox * clx - xr : (-ox - 1) * clx + xr) - kMargin, 0.0f);
             for(int oy = -rr; oy <= rr; oy++) {
                 if(oy < -dy_ || oy > dy_) { continue; }
                 int ny, sy;
                 wrap_cell(cy + oy, dy_, ny, sy);
-                const float gy = oy == 0 ? 0.0f : fmaxf((oy > 0 ? oy * cly - yr : (-oy - 1) * cly + yr) - kMargin, 0.0f);
-                const float q = r2w - gx * gx - gy * gy;
-                if(q < 0.0f) { continue; }
-                const float wz = sqrtf(q) + kMargin;
-                const float z_lo = zf - wz, z_hi = zf + wz;
-                const int col = R.cell0 + (nx * dy_ + ny) * dz_;
-                // the stencil's z cells in offset order as runs of one image shift: cells
-                // wrapped below, the unwrapped ones, cells wrapped above
-                const int oz0 = -rr < -dz_ ? -dz_ : -rr, oz1 = rr > dz_ ? dz_ : rr;
-                for(int seg = 0; seg < 3; seg++) {
-                    int a0, a1, sz;                  // offsets [a0, a1] of this run
-                    if(seg == 0) { a0 = oz0; a1 = min(oz1, -cz - 1); sz = -1; }
-                    else if(seg == 1) { a0 = max(oz0, -cz); a1 = min(oz1, dz_ - 1 - cz); sz = 0; }
-                    else { a0 = max(oz0, dz_ - cz); a1 = oz1; sz = 1; }
-                    if(a0 > a1) { continue; }
+                for(int oz = -rr; oz <= rr; oz++) {
+                    if(oz < -dz_ || oz > dz_) { continue; }
+                    int nz, sz;
+                    wrap_cell(cz + oz, dz_, nz, sz);
+                    const int c = R.cell0 + (nx * dy_ + ny) * dz_ + nz;
                     const uint32_t code = image_code(sx, sy, sz) << PG_NBR_INDEX_BITS;
                     // half lists as the single-system build (nlist.cu): an interior pair
                     // once, stored by the particle whose partner lies above it in x (cells
@@ -203,22 +178,8 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
                     // through an image from both sides
                     if(a.list.half && code == 0u && ox < 0) { continue; }
                     const bool slab = a.list.half && code == 0u && ox == 0;
-                    const int c0 = col + cz + a0 - sz * dz_, c1 = col + cz + a1 - sz * dz_;
-                    const int b = a.cells.cell_start[c0], e = a.cells.cell_start[c1] + a.cells.cell_count[c1];
-                    const float shift = sz == 0 ? 0.0f : (sz > 0 ? (float) R.len[2] : -(float) R.len[2]);
-                    int lo_j = b, hi_j = e;
-                    while(lo_j < hi_j) {
-                        const int mid = (lo_j + hi_j) >> 1;
-                        if(__ldg(a.p.pos_hi + 4 * (size_t) hl(a.p, mid) + 2) + shift < z_lo) { lo_j = mid + 1; }
-                        else { hi_j = mid; }
-                    }
-                    int end = e;
-                    for(int l = lo_j; l < end;) {
-                        const int mid = (l + end) >> 1;
-                        if(__ldg(a.p.pos_hi + 4 * (size_t) hl(a.p, mid) + 2) + shift <= z_hi) { l = mid + 1; }
-                        else { end = mid; }
-                    }
-                    for(int j = lo_j; j < end; j++) {
+                    const int b = a.cells.cell_start[c], e = b + a.cells.cell_count[c];
+                    for(int j = b; j < e; j++) {
                         if(j == i && code == 0u) { continue; }
                         float fx, fy, fz;
                         if(fxs) {
