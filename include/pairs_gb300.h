@@ -210,7 +210,8 @@ typedef struct {
     float   len_lo[3];
     double  fx_scale[3];         /* 2^32 / len: fixed-point units of this replica's box (pos_fx) */
     float   fx_unit[3];          /* len / 2^32 rounded to FP32 */
-    int32_t fx_pad_;
+    int32_t reach_x;             /* stencil reach along x (0: `reach`); 2 with reach 1: x cells
+                                    of >= r_list / 2, a 5 x 3 x 3 stencil */
 } pg_replica;
 
 /* A batched ensemble (config: hundreds of independent periodic LJ replicas run by

@@ -106,7 +106,7 @@ class PgReplica(C.Structure):
                 ("cell_len", C.c_double * 3), ("inv_cell_len", C.c_double * 3), ("quantum", C.c_double),
                 ("len_hi", C.c_float * 3),
                 ("len_lo", C.c_float * 3), ("fx_scale", C.c_double * 3), ("fx_unit", C.c_float * 3),
-                ("fx_pad_", C.c_int32)]
+                ("reach_x", C.c_int32)]
 
 
 class PgEnsemble(C.Structure):

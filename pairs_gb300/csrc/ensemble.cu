@@ -148,17 +148,17 @@ __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
     const int ci = a.cells.particle_cell[i] - R.cell0;
     if(ci >= 0 && ci < R.ncells) {
         const int dz_ = R.dims[2], dy_ = R.dims[1], dx_ = R.dims[0], rr = R.reach;
+        const int rx = R.reach_x > 0 ? R.reach_x : rr;
         const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
         const int stride = a.list.stride, cap = a.list.max_neighbors;
         // fixed-point screen where the replica's grid keeps every candidate's stencil
-        // image within half a box (at least 4 cells per axis, 6 with reach 2; see
+        // image within half a box (at least 2 reach + 2 cells per axis; see
         // nlist.cu), the compensated one elsewhere
-        const int need = rr == 1 ? 4 : 6;
-        const bool fxs = a.p.pos_fx != nullptr && dx_ >= need && dy_ >= need && dz_ >= need;
+        const bool fxs = a.p.pos_fx != nullptr && dx_ >= 2 * rx + 2 && dy_ >= 2 * rr + 2 && dz_ >= 2 * rr + 2;
         const int4 fi = fxs ? ld_i4(a.p.pos_fx, i) : make_int4(0, 0, 0, 0);
         int32_t *wp = a.list.nbr + (size_t) i * tpa;       // entry 0 of the interleaved layout
         const size_t row_step = (size_t) stride * tpa - (size_t) (tpa - 1);
-        for(int ox = -rr; ox <= rr; ox++) {
+        for(int ox = -rx; ox <= rx; ox++) {
             if(ox < -dx_ || ox > dx_) { continue; }
             int nx, sx;
             wrap_cell(cx + ox, dx_, nx, sx);

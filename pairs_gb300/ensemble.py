@@ -142,9 +142,10 @@ class Ensemble:
     # ------------------------------------------------------------------ layout
 
     def configure(self, tpa, block, reach, half=None):
-        """Set the force kernel's threads per atom / block size, the cell size (cells
-        of >= r_list / reach) and, if given, the list layout (half or full); takes
-        effect at the next rebuild."""
+        """Set the force kernel's threads per atom / block size, the cell size and, if
+        given, the list layout (half or full); takes effect at the next rebuild.  reach 1:
+        cells of >= r_list (27-cell stencil); 2: cells of >= r_list / 2 (125 cells); 3:
+        cells of >= r_list / 2 along x and >= r_list along y and z (5 x 3 x 3 cells)."""
         if half is not None:
             self.half = bool(half)
             self.list.half = int(self.half)
@@ -159,8 +160,9 @@ class Ensemble:
             R.first, R.n = int(self.first[r]), int(self.sizes[r])
             R.cell0 = cell0
             nc = 1
+            per_axis = (2, 1, 1) if self.reach == 3 else (self.reach,) * 3
             for d in range(3):
-                dims = max(1, int(math.floor(L[d] * self.reach / self.r_list)))
+                dims = max(1, int(math.floor(L[d] * per_axis[d] / self.r_list)))
                 R.dims[d] = dims
                 R.lo[d] = 0.0
                 R.len[d] = L[d]
@@ -168,7 +170,8 @@ class Ensemble:
                 R.inv_cell_len[d] = 1.0 / R.cell_len[d]
                 nc *= dims
             R.ncells = nc
-            R.reach = self.reach
+            R.reach = 1 if self.reach == 3 else self.reach
+            R.reach_x = 2 if self.reach == 3 else 0
             q = _box_quantum(np.zeros(3), L)
             R.quantum = q
             for d in range(3):
@@ -385,7 +388,7 @@ def autotune(replicas, candidates=None, steps=6, cycle=5.0, **kw):
     between rebuilds (any replica's trip rebuilds all: about every 5 steps at 512
     replicas).  Returns (best, table)."""
     if candidates is None:
-        candidates = [(t, b, r, h) for h in (True, False) for r in (1, 2) for t in (1, 2, 4, 8) for b in (128, 256)]
+        candidates = [(t, b, r, h) for h in (True, False) for r in (1, 2, 3) for t in (1, 2, 4, 8) for b in (128, 256)]
     ens = Ensemble(replicas, graphs=False, **kw)
     table = []
     for tpa, block, reach, half in candidates:

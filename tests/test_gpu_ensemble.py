@@ -46,7 +46,7 @@ def unordered(p):
 
 
 @pytest.mark.parametrize("tpa,reach,half", [(1, 1, False), (4, 1, False), (2, 2, False), (8, 2, False),
-                                            (1, 1, True), (2, 2, True), (4, 2, True)])
+                                            (1, 1, True), (2, 2, True), (4, 2, True), (2, 3, True), (1, 3, False)])
 def test_lists_and_forces_match_oracle(tpa, reach, half):
     from pairs_gb300.ensemble import Ensemble
     reps = replicas()
