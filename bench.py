@@ -449,12 +449,15 @@ def run_ensemble(args, rank, world, dist):
     natoms = sum(len(r["mass"]) for r in reps)
     steps = args.steps
     if args.ensemble_layout:
-        # a fixed layout "tpa,block,reach,half" instead of the autotuner's choice
+        # a fixed layout "tpa,block,reach,half" instead of the autotuner's choice (half:
+        # 0 full lists, 1 half lists, 2 pair-cluster half lists)
         tpa, block, reach, half = (int(v) for v in args.ensemble_layout.split(","))
-        half, table = bool(half), []
+        half, table = ("pairs" if half == 2 else bool(half)), []
     else:
         (tpa, block, reach, half), table = autotune(reps)
-    ens = Ensemble(reps, tpa=tpa, block=block, reach=reach, half=half, persistent=args.ensemble_persistent)
+    pairs = half == "pairs"
+    ens = Ensemble(reps, tpa=tpa, block=block, reach=reach, half=True if pairs else half, pair_lists=pairs,
+                   persistent=args.ensemble_persistent)
     ens.run(args.warmup)
     ens.synchronize()
     clocks = ClockSampler(dev.index or 0)
@@ -493,9 +496,11 @@ def run_ensemble(args, rank, world, dist):
         "data": "synthetic (trimmed fcc lattices, reference velocity rule, seed 2024)",
         "config": {"workload": f"{len(reps)} LJ replicas, {natoms} atoms total, sizes log-uniform 500..32000, "
                                "rho U[0.6,0.9], T U[0.7,1.5], rc 2.5, skin 0.3, dt 0.005, mixed, "
-                               f"{'half' if ens.half else 'full'} lists, guard rebuilds, CUDA-graph chunks",
+                               f"{'pair-cluster half' if pairs else ('half' if ens.half else 'full')} lists, "
+                               "guard rebuilds, CUDA-graph chunks",
                    "replicas": len(reps), "atoms": natoms,
-                   "autotuned": {"tpa": tpa, "block": block, "reach": reach, "half_lists": half}},
+                   "autotuned": {"tpa": tpa, "block": block, "reach": reach, "half_lists": bool(half),
+                                 "pair_lists": pairs}},
         "autotune_table": table,
         "one_by_one": {"value": one_value, "steps": one_steps, "seconds": one_s,
                        "definition": f"each replica alone through LJEngine (mixed, {'half' if ens.half else 'full'} "
@@ -695,7 +700,8 @@ def main():
     ap.add_argument("--dem-spheres", type=int, default=1000000, help="dem workload: number of spheres")
     ap.add_argument("--replicas", type=int, default=512, help="ensemble workload: number of replicas")
     ap.add_argument("--ensemble-layout", default="",
-                    help="ensemble workload: fixed layout 'tpa,block,reach,half' instead of the autotuner's")
+                    help="ensemble workload: fixed layout 'tpa,block,reach,half' (half 0 full, 1 half, "
+                         "2 pair-cluster half lists) instead of the autotuner's")
     ap.add_argument("--ensemble-persistent", action="store_true",
                     help="ensemble workload: each chunk's plain steps in one persistent launch")
     ap.add_argument("--one-by-one-steps", type=int, default=100,

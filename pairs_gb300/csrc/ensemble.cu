@@ -645,8 +645,19 @@ int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_work
     return launch_status();
 }
 
+int ens_pc_build(const pg_ensemble *e, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
+                 double r_list2, pg_status *status, cudaStream_t st);
+int ens_pc_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
+                 int32_t *cut_count, int2 *cut_rec, int cut_capacity, cudaStream_t st);
+
 int ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                          double r_list2, pg_status *status, cudaStream_t st) {
+    if(list != nullptr && list->pair_table != nullptr) {
+        // pair-cluster half lists (pairlist.cu), each slot on its replica's box and grid
+        if(!ens_ok(e, p) || !cells || (e->half == 0) || cells->ncells != e->ncells) { return PG_ERR_ARGUMENT; }
+        list->steps_since_build = 0;
+        return ens_pc_build(e, p, cells, list, r_list2, status, st);
+    }
     if(!ens_ok(e, p) || !cells || !list || !list->nbr || !list->count || !status || !p->pos_ref || !p->pos_hi ||
        !p->pos_lo || (p->ref_fx != nullptr ? !p->pos_fx : (!p->ref_hi || !p->ref_lo)) || list->stride < p->n ||
        p->n >= (1 << PG_NBR_INDEX_BITS) || (list->half != 0) != (e->half != 0)) {
@@ -700,6 +711,9 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
     a.cut_rec = (int2 *) ((char *) ws.ptr + 256);
     a.cut_capacity = (int) ((ws.bytes - 256) / 8 < INT32_MAX ? (ws.bytes - 256) / 8 : INT32_MAX);
     cudaMemsetAsync(a.cut_count, 0, sizeof(int32_t), st);
+    if(list->pair_table != nullptr) {            // pair-cluster half lists (pairlist.cu)
+        return ens_pc_force(e, p, list, lj, a.cut_count, a.cut_rec, a.cut_capacity, st);
+    }
     const bool one = lj->ntypes == 1;
     switch(e->tpa) {
         case 1: launch_force<1>(a, p->n, e->block, one, fixed, st); break;
@@ -747,7 +761,7 @@ int ensemble_steps(const pg_ensemble *e, pg_particles *p, const pg_neighbor_list
        (lj->ntypes > 1 && !p->type) || (list->half != 0) != (e->half != 0)) {
         return PG_ERR_ARGUMENT;
     }
-    if(ws.ptr == nullptr || ws.bytes < 256 + 8) { return PG_ERR_ARGUMENT; }
+    if(ws.ptr == nullptr || ws.bytes < 256 + 8 || list->pair_table != nullptr) { return PG_ERR_ARGUMENT; }
     const bool one = lj->ntypes == 1;
     typedef void (*Kernel)(EnsStepsArgs);
     Kernel k;

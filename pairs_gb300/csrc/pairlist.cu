@@ -70,15 +70,17 @@ struct PcBuildArgs {
     pg_neighbor_list list;
     double r_list2;
     float r2_lo, r2_hi;          // screening band, box units squared when kCubic
+    const pg_replica *replicas;  // batched ensembles: each slot's box and grid from its replica
+    const int32_t *replica_of;
 };
 
 // The FP64 decision of a candidate in the screening band: the reference's separately
 // rounded rsq to the stencil's image of the partner (as nlist.cu).
-__device__ __noinline__ bool pc_exact(const PcBuildArgs &a, int i, int j, int sx, int sy, int sz) {
+__device__ __noinline__ bool pc_exact(const PcBuildArgs &a, const double *len, int i, int j, int sx, int sy, int sz) {
     const D4 xi = ld_d4_rare(a.p.pos, i), xj = ld_d4_rare(a.p.pos, j);
-    const double dx = __dsub_rn(xi.x, ref_image(xj.x, sx, a.box.len[0]));
-    const double dy = __dsub_rn(xi.y, ref_image(xj.y, sy, a.box.len[1]));
-    const double dz = __dsub_rn(xi.z, ref_image(xj.z, sz, a.box.len[2]));
+    const double dx = __dsub_rn(xi.x, ref_image(xj.x, sx, len[0]));
+    const double dy = __dsub_rn(xi.y, ref_image(xj.y, sy, len[1]));
+    const double dz = __dsub_rn(xi.z, ref_image(xj.z, sz, len[2]));
     return ref_rsq(dx, dy, dz) < a.r_list2;
 }
 
@@ -124,7 +126,13 @@ struct PcWindow {
 
 constexpr int kPcBuildBlock = 128;
 
-template<bool kCubic>
+// Batched ensembles (kEns): a slot's box, units and grid come from its replica (the
+// cells of replica r are [cell0, cell0 + ncells) of the shared arrays, z fastest), and a
+// replica whose grid would visit a stencil cell twice (fewer than 2 reach + 1 cells on an
+// axis) sets overflow bit 5 instead of listing.
+constexpr int kPcGridTooSmall = 32;
+
+template<bool kCubic, bool kEns>
 __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, PcWindow w, pg_status *status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if(t >= a.list.stride) { return; }
@@ -144,17 +152,39 @@ __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, Pc
         }
         const bool use_a = !(a.p.flags != nullptr && (a.p.flags[ia] & kFlagFixed));
         const bool use_b = has_b && !(a.p.flags != nullptr && (a.p.flags[ib] & kFlagFixed));
-        const int ci = a.cells.particle_cell[ia];
-        if((use_a || use_b) && ci < a.cells.ncells) {
-            const int dz_ = a.cells.dims[2], dy_ = a.cells.dims[1], dx_ = a.cells.dims[0];
+        // the grid and box of the slot (the system's, or its replica's)
+        int ci = a.cells.particle_cell[ia], cell0 = 0, ncells = a.cells.ncells;
+        int dz_ = a.cells.dims[2], dy_ = a.cells.dims[1], dx_ = a.cells.dims[0];
+        int rr = a.cells.reach > 1 ? a.cells.reach : 1;
+        int rx = a.cells.reach_x > 0 ? a.cells.reach_x : rr;
+        float fu[3] = {a.box.fx_unit[0], a.box.fx_unit[1], a.box.fx_unit[2]};
+        const double *len = a.box.len;
+        double clx_u = w.clx_u, cly_u = w.cly_u;
+        float clx = w.clx, cly = w.cly, scale_z = w.scale_z;
+        bool grid_ok = true;
+        if(kEns) {
+            const pg_replica &R = a.replicas[a.replica_of[ia]];
+            cell0 = R.cell0; ncells = R.ncells; ci -= cell0;
+            dx_ = R.dims[0]; dy_ = R.dims[1]; dz_ = R.dims[2];
+            rr = R.reach > 1 ? R.reach : 1;
+            rx = R.reach_x > 0 ? R.reach_x : rr;
+            fu[0] = R.fx_unit[0]; fu[1] = R.fx_unit[1]; fu[2] = R.fx_unit[2];
+            len = R.len;
+            clx_u = R.cell_len[0] * R.fx_scale[0]; cly_u = R.cell_len[1] * R.fx_scale[1];
+            clx = (float) R.cell_len[0]; cly = (float) R.cell_len[1]; scale_z = (float) R.fx_scale[2];
+            // each stencil cell visited once (the half stencil's ox 0 .. rx, oy and oz
+            // -rr .. rr): then a pair within r_list (< half a box) is met once, through the
+            // image its fixed-point difference gives
+            grid_ok = dx_ >= 2 * rx + 1 && dy_ >= 2 * rr + 1 && dz_ >= 2 * rr + 1;
+            if(!grid_ok) { atomicOr(&status->overflow, kPcGridTooSmall); }
+        }
+        if((use_a || use_b) && ci >= 0 && ci < ncells && grid_ok) {
             const int cz = ci % dz_, cy = (ci / dz_) % dy_, cx = ci / (dz_ * dy_);
-            const int rr = a.cells.reach > 1 ? a.cells.reach : 1;
-            const int rx = a.cells.reach_x > 0 ? a.cells.reach_x : rr;
-            const float unit2 = kCubic ? a.box.fx_unit[0] * a.box.fx_unit[0] : 1.0f;
+            const float unit2 = kCubic ? fu[0] * fu[0] : 1.0f;
             const float r2_lo = a.r2_lo / unit2, r2_hi = a.r2_hi / unit2;
-            const float2 ux = make_float2(a.box.fx_unit[0], a.box.fx_unit[0]);
-            const float2 uy = make_float2(a.box.fx_unit[1], a.box.fx_unit[1]);
-            const float2 uz = make_float2(a.box.fx_unit[2], a.box.fx_unit[2]);
+            const float2 ux = make_float2(fu[0], fu[0]);
+            const float2 uy = make_float2(fu[1], fu[1]);
+            const float2 uz = make_float2(fu[2], fu[2]);
             const int stride = a.list.stride;
             int32_t *wp = a.list.nbr + t;
             // the members' z keys in their own cell (b follows a in z order)
@@ -162,12 +192,12 @@ __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, Pc
             const int64_t za = z_key((uint32_t) fa.z, own_top), zb = z_key((uint32_t) fb.z, own_top);
             // the members' offsets inside their cell in x and y (a member rounded onto the
             // box's upper face wraps to 0 units; the wrapped difference keeps it at the top)
-            const uint32_t ex = (uint32_t) (unsigned long long) llrint(cx * w.clx_u);
-            const uint32_t ey = (uint32_t) (unsigned long long) llrint(cy * w.cly_u);
-            const float xa = (float) (int) ((uint32_t) fa.x - ex) * a.box.fx_unit[0];
-            const float xb = (float) (int) ((uint32_t) fb.x - ex) * a.box.fx_unit[0];
-            const float ya = (float) (int) ((uint32_t) fa.y - ey) * a.box.fx_unit[1];
-            const float yb = (float) (int) ((uint32_t) fb.y - ey) * a.box.fx_unit[1];
+            const uint32_t ex = (uint32_t) (unsigned long long) llrint(cx * clx_u);
+            const uint32_t ey = (uint32_t) (unsigned long long) llrint(cy * cly_u);
+            const float xa = (float) (int) ((uint32_t) fa.x - ex) * fu[0];
+            const float xb = (float) (int) ((uint32_t) fb.x - ex) * fu[0];
+            const float ya = (float) (int) ((uint32_t) fa.y - ey) * fu[1];
+            const float yb = (float) (int) ((uint32_t) fb.y - ey) * fu[1];
             constexpr float kMargin = 1.0e-3f;
             // column ranges: the unwrapped cells, then the cells wrapped below / above
             const int z_lo = cz - rr < 0 ? 0 : cz - rr, z_hi = cz + rr > dz_ - 1 ? dz_ - 1 : cz + rr;
@@ -187,8 +217,8 @@ __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, Pc
                 const bool above_b = ox > 0 || (dxb != 0 ? dxb < 0 : (dyb != 0 ? dyb < 0 : (dzb != 0 ? dzb < 0 : j > ib)));
                 bool ka = use_a && j != ia && above_a && R.x <= r2_hi;
                 bool kb = use_b && j != ib && above_b && R.y <= r2_hi;
-                if(ka && !(R.x < r2_lo)) { ka = pc_exact(a, ia, j, sx, sy, sz); }
-                if(kb && !(R.y < r2_lo)) { kb = pc_exact(a, ib, j, sx, sy, sz); }
+                if(ka && !(R.x < r2_lo)) { ka = pc_exact(a, len, ia, j, sx, sy, sz); }
+                if(kb && !(R.y < r2_lo)) { kb = pc_exact(a, len, ib, j, sx, sy, sz); }
                 if(ka || kb) {
                     if(cnt < cap) {
                         __stcs(wp, (int32_t) ((uint32_t) j | (ka ? kPcMaskA : 0u) | (kb ? kPcMaskB : 0u)));
@@ -200,28 +230,28 @@ __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, Pc
             for(int ox = 0; ox <= rx; ox++) {
                 int nx = cx + ox, sx = 0;
                 if(nx >= dx_) { nx -= dx_; sx = 1; }
-                const float gxa = ox == 0 ? 0.0f : fmaxf(ox * w.clx - xa - kMargin, 0.0f);
-                const float gxb = ox == 0 ? 0.0f : fmaxf(ox * w.clx - xb - kMargin, 0.0f);
+                const float gxa = ox == 0 ? 0.0f : fmaxf(ox * clx - xa - kMargin, 0.0f);
+                const float gxb = ox == 0 ? 0.0f : fmaxf(ox * clx - xb - kMargin, 0.0f);
                 for(int oy = -rr; oy <= rr; oy++) {
                     int ny = cy + oy, sy = 0;
                     if(ny < 0) { ny += dy_; sy = -1; } else if(ny >= dy_) { ny -= dy_; sy = 1; }
                     const float gya = oy == 0 ? 0.0f
-                                              : fmaxf((oy < 0 ? ya + (-oy - 1) * w.cly : oy * w.cly - ya) - kMargin, 0.0f);
+                                              : fmaxf((oy < 0 ? ya + (-oy - 1) * cly : oy * cly - ya) - kMargin, 0.0f);
                     const float gyb = oy == 0 ? 0.0f
-                                              : fmaxf((oy < 0 ? yb + (-oy - 1) * w.cly : oy * w.cly - yb) - kMargin, 0.0f);
+                                              : fmaxf((oy < 0 ? yb + (-oy - 1) * cly : oy * cly - yb) - kMargin, 0.0f);
                     const float qa = use_a ? w.r2w - gxa * gxa - gya * gya : -1.0f;
                     const float qb = use_b ? w.r2w - gxb * gxb - gyb * gyb : -1.0f;
                     if(qa < 0.0f && qb < 0.0f) { continue; }
                     int64_t w_lo = INT64_MAX, w_hi = INT64_MIN;
                     if(qa >= 0.0f) {
-                        const int64_t h = (int64_t) (sqrtf(qa) * w.scale_z) + 16;
+                        const int64_t h = (int64_t) (sqrtf(qa) * scale_z) + 16;
                         w_lo = za - h; w_hi = za + h;
                     }
                     if(qb >= 0.0f) {
-                        const int64_t h = (int64_t) (sqrtf(qb) * w.scale_z) + 16;
+                        const int64_t h = (int64_t) (sqrtf(qb) * scale_z) + 16;
                         w_lo = min(w_lo, zb - h); w_hi = max(w_hi, zb + h);
                     }
-                    const int col = (nx * dy_ + ny) * dz_;
+                    const int col = cell0 + (nx * dy_ + ny) * dz_;
                     for(int seg = 0; seg < 3; seg++) {
                         int c0, c1, sz;
                         if(seg == 0) { c0 = z_lo; c1 = z_hi; sz = 0; }
@@ -274,7 +304,22 @@ struct PcForceArgs {
     int32_t *cut_count;          // pairs within the cutoff band, queued (particle, partner)
     int2 *cut_rec;
     int cut_capacity;
+    const pg_replica *replicas;  // batched ensembles: each slot's units from its replica
+    const int32_t *replica_of;
 };
+
+// the fixed-point units and box lengths of particle i (the system's, or its replica's)
+template<bool kEns>
+__device__ __forceinline__ void pc_units(const PcForceArgs &a, int i, float u[3], const double **len) {
+    if(kEns) {
+        const pg_replica &R = a.replicas[a.replica_of[i]];
+        u[0] = R.fx_unit[0]; u[1] = R.fx_unit[1]; u[2] = R.fx_unit[2];
+        *len = R.len;
+    } else {
+        u[0] = a.box.fx_unit[0]; u[1] = a.box.fx_unit[1]; u[2] = a.box.fx_unit[2];
+        *len = a.box.len;
+    }
+}
 
 __device__ __forceinline__ void pc_block_energy(double pe, double vir, double *energy) {
     __shared__ double s[2][kPcBlock / 32];
@@ -296,7 +341,7 @@ __device__ __forceinline__ void pc_block_energy(double pe, double vir, double *e
 // in the per-particle kernels (the squared distance in the order of pair_rsq, the
 // factor 48 sr6 (sr6 - 1/2) sr2 eps in FP32, examples/md.py:5-8); a pair within
 // kCutBand of rc^2 is queued for the FP64 decision of k_pc_fixup.
-template<bool kOneType, bool kEnergy>
+template<bool kOneType, bool kEnergy, bool kEns>
 __global__ void __launch_bounds__(kPcBlock, 5) k_pc_lj(PcForceArgs a) {
     if(frozen_force(a.p)) { return; }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -312,9 +357,12 @@ __global__ void __launch_bounds__(kPcBlock, 5) k_pc_lj(PcForceArgs a) {
         const int32_t *nb = a.list.nbr + t;
         const size_t stride = (size_t) a.list.stride;
         const float c2 = a.lj.cutoff2f, band = c2 * kCutBand;
-        const float2 ux = make_float2(a.box.fx_unit[0], a.box.fx_unit[0]);
-        const float2 uy = make_float2(a.box.fx_unit[1], a.box.fx_unit[1]);
-        const float2 uz = make_float2(a.box.fx_unit[2], a.box.fx_unit[2]);
+        float fu[3];
+        const double *len;
+        pc_units<kEns>(a, ia, fu, &len);
+        const float2 ux = make_float2(fu[0], fu[0]);
+        const float2 uy = make_float2(fu[1], fu[1]);
+        const float2 uz = make_float2(fu[2], fu[2]);
         const float2 half2 = make_float2(-0.5f, -0.5f);
         float2 FX = make_float2(0.0f, 0.0f), FY = FX, FZ = FX;
         uint32_t cur[kPcBatch];
@@ -400,23 +448,26 @@ __global__ void __launch_bounds__(kPcBlock, 5) k_pc_lj(PcForceArgs a) {
 // partner nearest the particle (the image the reference's ghost carries; the pair is
 // far closer than half a box), then applied as the main pass would have: the FP32 force
 // on the particle and its reaction on the partner.
-template<bool kOneType, bool kEnergy>
+template<bool kOneType, bool kEnergy, bool kEns>
 __device__ void pc_fixup_pair(const PcForceArgs &a, int i, int j) {
+    float fu[3];
+    const double *len;
+    pc_units<kEns>(a, i, fu, &len);
     const D4 xi = ld_d4_rare(a.p.pos, i), xj = ld_d4_rare(a.p.pos, j);
     const double di[3] = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
     int s[3];
     for(int d = 0; d < 3; d++) {
-        const double h = 0.5 * a.box.len[d];
+        const double h = 0.5 * len[d];
         s[d] = di[d] > h ? 1 : (di[d] < -h ? -1 : 0);
     }
-    const double dx = __dsub_rn(xi.x, ref_image(xj.x, s[0], a.box.len[0]));
-    const double dy = __dsub_rn(xi.y, ref_image(xj.y, s[1], a.box.len[1]));
-    const double dz = __dsub_rn(xi.z, ref_image(xj.z, s[2], a.box.len[2]));
+    const double dx = __dsub_rn(xi.x, ref_image(xj.x, s[0], len[0]));
+    const double dy = __dsub_rn(xi.y, ref_image(xj.y, s[1], len[1]));
+    const double dz = __dsub_rn(xi.z, ref_image(xj.z, s[2], len[2]));
     if(!(ref_rsq(dx, dy, dz) < a.lj.cutoff2)) { return; }
     const int4 fi = ld_i4(a.p.pos_fx, i), fj = ld_i4(a.p.pos_fx, j);
-    const float ex = __fmul_rn((float) fx_diff(fi.x, fj.x), a.box.fx_unit[0]);
-    const float ey = __fmul_rn((float) fx_diff(fi.y, fj.y), a.box.fx_unit[1]);
-    const float ez = __fmul_rn((float) fx_diff(fi.z, fj.z), a.box.fx_unit[2]);
+    const float ex = __fmul_rn((float) fx_diff(fi.x, fj.x), fu[0]);
+    const float ey = __fmul_rn((float) fx_diff(fi.y, fj.y), fu[1]);
+    const float ez = __fmul_rn((float) fx_diff(fi.z, fj.z), fu[2]);
     const float rsq = pair_rsq(ex, ey, ez);
     const int tij = kOneType ? 0 : fi.w * a.lj.ntypes + fj.w;
     const float s2 = rcp_approx(rsq);
@@ -433,7 +484,7 @@ __device__ void pc_fixup_pair(const PcForceArgs &a, int i, int j) {
 // The band pairs the main pass left out: the queued records, or, when more pairs fell
 // in the band than the queue holds, every cluster list walked again with the main
 // pass's screen arithmetic (which finds exactly the pairs it left out).
-template<bool kOneType, bool kEnergy>
+template<bool kOneType, bool kEnergy, bool kEns>
 __global__ void __launch_bounds__(kBlock) k_pc_fixup(PcForceArgs a) {
     if(frozen_force(a.p)) { return; }
     const int queued = *a.cut_count;
@@ -441,7 +492,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_fixup(PcForceArgs a) {
     if(queued <= a.cut_capacity) {
         for(int r = first; r < queued; r += step) {
             const int2 q = a.cut_rec[r];
-            pc_fixup_pair<kOneType, kEnergy>(a, q.x, q.y);
+            pc_fixup_pair<kOneType, kEnergy, kEns>(a, q.x, q.y);
         }
         return;
     }
@@ -452,6 +503,9 @@ __global__ void __launch_bounds__(kBlock) k_pc_fixup(PcForceArgs a) {
         const int ia = rec & (int) kPcIndexMask;
         const int ib = (rec & kPcHasB) != 0 ? ia + 1 : ia;
         const int4 fa = ld_i4(a.p.pos_fx, ia), fb = ld_i4(a.p.pos_fx, ib);
+        float fu[3];
+        const double *len;
+        pc_units<kEns>(a, ia, fu, &len);
         const int cnt = a.list.count[t];
         for(int k = 0; k < cnt; k++) {
             const uint32_t e = (uint32_t) a.list.nbr[(size_t) k * a.list.stride + t];
@@ -460,10 +514,12 @@ __global__ void __launch_bounds__(kBlock) k_pc_fixup(PcForceArgs a) {
             for(int m = 0; m < 2; m++) {
                 if(!(e & (m == 0 ? kPcMaskA : kPcMaskB))) { continue; }
                 const int4 fm = m == 0 ? fa : fb;
-                const float ex = __fmul_rn((float) fx_diff(fm.x, fj.x), a.box.fx_unit[0]);
-                const float ey = __fmul_rn((float) fx_diff(fm.y, fj.y), a.box.fx_unit[1]);
-                const float ez = __fmul_rn((float) fx_diff(fm.z, fj.z), a.box.fx_unit[2]);
-                if(fabsf(pair_rsq(ex, ey, ez) - c2) < band) { pc_fixup_pair<kOneType, kEnergy>(a, m == 0 ? ia : ib, j); }
+                const float ex = __fmul_rn((float) fx_diff(fm.x, fj.x), fu[0]);
+                const float ey = __fmul_rn((float) fx_diff(fm.y, fj.y), fu[1]);
+                const float ez = __fmul_rn((float) fx_diff(fm.z, fj.z), fu[2]);
+                if(fabsf(pair_rsq(ex, ey, ez) - c2) < band) {
+                    pc_fixup_pair<kOneType, kEnergy, kEns>(a, m == 0 ? ia : ib, j);
+                }
             }
         }
     }
@@ -481,6 +537,7 @@ int pc_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg
     a.box = *box; a.p = *p; a.cells = *cells; a.list = *list; a.r_list2 = r_list2;
     a.r2_lo = (float) r_list2 * (1.0f - kPcScreenBand);
     a.r2_hi = (float) r_list2 * (1.0f + kPcScreenBand);
+    a.replicas = nullptr; a.replica_of = nullptr;
     cudaMemsetAsync(list->pair_table, 0xff, (size_t) list->stride * sizeof(int32_t), st);
     if(cells->ncells > 0) {
         k_pc_table<<<blocks_for(cells->ncells), kBlock, 0, st>>>(*cells, list->pair_table); note_launch();
@@ -494,13 +551,26 @@ int pc_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg
     w.scale_z = (float) box->fx_scale[2];
     const bool cubic = box->fx_unit[0] == box->fx_unit[1] && box->fx_unit[1] == box->fx_unit[2];
     const int grid = blocks_for(list->stride, kPcBuildBlock);
-    if(cubic) { k_pc_build<true><<<grid, kPcBuildBlock, 0, st>>>(a, w, status); }
-    else { k_pc_build<false><<<grid, kPcBuildBlock, 0, st>>>(a, w, status); }
+    if(cubic) { k_pc_build<true, false><<<grid, kPcBuildBlock, 0, st>>>(a, w, status); }
+    else { k_pc_build<false, false><<<grid, kPcBuildBlock, 0, st>>>(a, w, status); }
     note_launch();
     return launch_status();
 }
 
 constexpr int kPcFixupBlocks = 2 * kSMs;
+
+template<bool kEns>
+static void pc_force_launch(const PcForceArgs &a, bool one, bool en, cudaStream_t st) {
+    const int grid = blocks_for(a.list.stride, kPcBlock);
+    if(one) {
+        if(en) { k_pc_lj<true, true, kEns><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<true, true, kEns><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+        else { k_pc_lj<true, false, kEns><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<true, false, kEns><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+    } else {
+        if(en) { k_pc_lj<false, true, kEns><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<false, true, kEns><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+        else { k_pc_lj<false, false, kEns><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<false, false, kEns><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+    }
+    note_launch(2);
+}
 
 int pc_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list *list, const LJTable &lj,
                 double *energy, int32_t *cut_count, int2 *cut_rec, int cut_capacity, cudaStream_t st) {
@@ -508,16 +578,59 @@ int pc_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list
     PcForceArgs a;
     a.box = *box; a.p = *p; a.list = *list; a.lj = lj;
     a.energy = energy; a.cut_count = cut_count; a.cut_rec = cut_rec; a.cut_capacity = cut_capacity;
-    const bool one = lj.ntypes == 1, en = energy != nullptr;
-    const int grid = blocks_for(list->stride, kPcBlock);
-    if(one) {
-        if(en) { k_pc_lj<true, true><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<true, true><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
-        else { k_pc_lj<true, false><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<true, false><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
-    } else {
-        if(en) { k_pc_lj<false, true><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<false, true><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
-        else { k_pc_lj<false, false><<<grid, kPcBlock, 0, st>>>(a); k_pc_fixup<false, false><<<kPcFixupBlocks, kBlock, 0, st>>>(a); }
+    a.replicas = nullptr; a.replica_of = nullptr;
+    pc_force_launch<false>(a, lj.ntypes == 1, energy != nullptr, st);
+    return launch_status();
+}
+
+// ------------------------------------------------------------------ batched ensembles
+
+// Pair-cluster half lists over every replica of a batched ensemble: the table of slots
+// over the shared cell arrays (a cell's slots depend only on its start and index), then
+// the build with each slot's box, units and grid from its replica.  Every replica needs
+// at least 2 reach + 1 cells per axis (else overflow bit 5).
+int ens_pc_build(const pg_ensemble *e, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
+                 double r_list2, pg_status *status, cudaStream_t st) {
+    if(!e || !p || !cells || !list || !status || !list->half || !list->pair_table || !list->nbr || !list->count ||
+       !p->pos || !p->pos_fx || !p->ref_fx || !p->pos_ref) {
+        return PG_ERR_ARGUMENT;
     }
-    note_launch(2);
+    if((int64_t) list->stride < pair_slots(p->n, cells->ncells) || p->n >= (1 << 30)) { return PG_ERR_ARGUMENT; }
+    PcBuildArgs a;
+    a.box = pg_box{}; a.p = *p; a.cells = *cells; a.list = *list; a.r_list2 = r_list2;
+    a.r2_lo = (float) r_list2 * (1.0f - kPcScreenBand);
+    a.r2_hi = (float) r_list2 * (1.0f + kPcScreenBand);
+    a.replicas = e->replicas; a.replica_of = e->replica_of;
+    cudaMemsetAsync(list->pair_table, 0xff, (size_t) list->stride * sizeof(int32_t), st);
+    if(cells->ncells > 0) {
+        k_pc_table<<<blocks_for(cells->ncells), kBlock, 0, st>>>(*cells, list->pair_table); note_launch();
+    }
+    PcWindow w = {};
+    w.r2w = (float) (r_list2 * (1.0 + 1.0e-3));
+    // replicas may differ in shape: distances in length units (the general form)
+    k_pc_build<false, true><<<blocks_for(list->stride, kPcBuildBlock), kPcBuildBlock, 0, st>>>(a, w, status);
+    note_launch();
+    return launch_status();
+}
+
+int ens_pc_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
+                 int32_t *cut_count, int2 *cut_rec, int cut_capacity, cudaStream_t st) {
+    if(!e || !lj || !list->half || !p->pos_fx || !list->nbr || !list->count || !list->pair_table || !cut_count ||
+       lj->ntypes < 1 || lj->ntypes > kMaxTypes) {
+        return PG_ERR_ARGUMENT;
+    }
+    PcForceArgs a;
+    a.box = pg_box{}; a.p = *p; a.list = *list;
+    a.lj.ntypes = lj->ntypes;
+    a.lj.cutoff2 = lj->cutoff2;
+    a.lj.cutoff2f = (float) lj->cutoff2;
+    for(int k = 0; k < lj->ntypes * lj->ntypes; k++) {
+        a.lj.eps[k] = lj->epsilon[k]; a.lj.sig6[k] = lj->sigma6[k];
+        a.lj.epsf[k] = (float) lj->epsilon[k]; a.lj.sig6f[k] = (float) lj->sigma6[k];
+    }
+    a.energy = nullptr; a.cut_count = cut_count; a.cut_rec = cut_rec; a.cut_capacity = cut_capacity;
+    a.replicas = e->replicas; a.replica_of = e->replica_of;
+    pc_force_launch<true>(a, lj->ntypes == 1, false, st);
     return launch_status();
 }
 

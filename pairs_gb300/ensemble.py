@@ -9,9 +9,10 @@ force), replayed without host work; the FP64 displacement guard freezes every la
 pass on the device once any replica's atom moved more than skin/2, the host then
 rebuilds all replicas and continues from the step after the trip.
 
-`autotune()` picks the threads per atom of the force kernel, its block size and the
-cell size (27 cells of >= r_list, or 125 cells of >= r_list/2) by timing the
-candidates on the ensemble itself.
+`autotune()` picks the threads per atom of the force kernel, its block size, the
+cell size (27 cells of >= r_list, or 125 cells of >= r_list/2) and the list layout
+(per-particle full or half lists, or pair-cluster half lists) by timing the candidates
+on the ensemble itself.
 """
 import ctypes as C
 import math
@@ -28,7 +29,7 @@ INT32_MAX = 2 ** 31 - 1
 class Ensemble:
     def __init__(self, replicas, *, cutoff=2.5, skin=0.3, dt=0.005, epsilon=1.0, sigma6=1.0, tpa=1, block=256,
                  reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, fixed_point=None,
-                 half=True, persistent=False, device="cuda"):
+                 half=True, pair_lists=False, persistent=False, device="cuda"):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -63,6 +64,7 @@ class Ensemble:
         self.fixed_point = fx_ok if fixed_point is None else bool(fixed_point)
         if self.persistent and not self.fixed_point:
             raise ValueError("persistent ensemble steps need fixed-point positions")
+        self.pair_lists = False
         self.ts = 0
         self.nbuilds = 0
         self.host_syncs = 0
@@ -132,7 +134,7 @@ class Ensemble:
         self.e.half = int(self.half)
         # a liquid at rho <= 0.9 has about 4/3 pi 2.8^3 rho ~ 83 partners within r_list
         self._max_nb = int(neighbor_capacity or 112)
-        self.configure(tpa, block, reach)
+        self.configure(tpa, block, reach, pair_lists=pair_lists)
         with torch.cuda.stream(self.stream):
             self.rebuild()
             self._force(0)                     # step 0: forces only (the reference's skip_first)
@@ -141,15 +143,29 @@ class Ensemble:
 
     # ------------------------------------------------------------------ layout
 
-    def configure(self, tpa, block, reach, half=None):
+    def configure(self, tpa, block, reach, half=None, pair_lists=None):
         """Set the force kernel's threads per atom / block size, the cell size and, if
-        given, the list layout (half or full); takes effect at the next rebuild.  reach 1:
-        cells of >= r_list (27-cell stencil); 2: cells of >= r_list / 2 (125 cells); 3:
-        cells of >= r_list / 2 along x and >= r_list along y and z (5 x 3 x 3 cells)."""
+        given, the list layout (half or full; per-particle or pair-cluster rows); takes
+        effect at the next rebuild.  reach 1: cells of >= r_list (27-cell stencil); 2:
+        cells of >= r_list / 2 (125 cells); 3: cells of >= r_list / 2 along x and >= r_list
+        along y and z (5 x 3 x 3 cells); 0: per replica the first of 1, 3, 2 whose grid
+        has 2 reach + 1 cells per axis (else 2).
+
+        Pair-cluster lists (pair_lists=True): one row per two consecutive particles of a
+        cell, each entry a partner and which of the two members it pairs with; half lists
+        on fixed-point positions, one thread per row in the force pass (tpa and block do
+        not apply).  Every replica grid needs 2 reach + 1 cells per axis."""
         if half is not None:
             self.half = bool(half)
             self.list.half = int(self.half)
             self.e.half = int(self.half)
+        if pair_lists is not None:
+            self.pair_lists = bool(pair_lists)
+        if self.pair_lists:
+            if not (self.half and self.fixed_point):
+                raise ValueError("pair-cluster lists are half lists on fixed-point positions")
+            if self.persistent:
+                raise ValueError("persistent ensemble steps run per-particle lists")
         self.tpa, self.block, self.reach = int(tpa), int(block), int(reach)
         self.e.tpa, self.e.block = self.tpa, self.block
         reps = (A.PgReplica * self.nrep)()
@@ -159,19 +175,29 @@ class Ensemble:
             L = self.boxes[r]
             R.first, R.n = int(self.first[r]), int(self.sizes[r])
             R.cell0 = cell0
+            # (cells per r_list along x, along y and z) of the layout: reach 0 takes per
+            # replica the largest cells whose grid visits every stencil cell once
+            modes = {1: [(1, 1)], 2: [(2, 2)], 3: [(2, 1)], 0: [(1, 1), (2, 1), (2, 2)]}[self.reach]
+            for rx, rr in modes:
+                dims = [max(1, int(math.floor(L[d] * (rx if d == 0 else rr) / self.r_list))) for d in range(3)]
+                if all(dims[d] >= 2 * (rx if d == 0 else rr) + 1 for d in range(3)):
+                    break
+            else:
+                if self.pair_lists:
+                    need = tuple(2 * (rx if d == 0 else rr) + 1 for d in range(3))
+                    raise ValueError(f"replica {r}: pair-cluster lists need {need} cells per axis at reach "
+                                     f"{self.reach}, the box gives {tuple(dims)}")
             nc = 1
-            per_axis = (2, 1, 1) if self.reach == 3 else (self.reach,) * 3
             for d in range(3):
-                dims = max(1, int(math.floor(L[d] * per_axis[d] / self.r_list)))
-                R.dims[d] = dims
+                R.dims[d] = dims[d]
                 R.lo[d] = 0.0
                 R.len[d] = L[d]
-                R.cell_len[d] = L[d] / dims
+                R.cell_len[d] = L[d] / dims[d]
                 R.inv_cell_len[d] = 1.0 / R.cell_len[d]
-                nc *= dims
+                nc *= dims[d]
             R.ncells = nc
-            R.reach = 1 if self.reach == 3 else self.reach
-            R.reach_x = 2 if self.reach == 3 else 0
+            R.reach = rr
+            R.reach_x = rx if rx != rr else 0
             q = _box_quantum(np.zeros(3), L)
             R.quantum = q
             for d in range(3):
@@ -205,11 +231,24 @@ class Ensemble:
     def _alloc_list(self, max_nb):
         self._max_nb = max_nb
         self.list.max_neighbors = max_nb
-        rows = -(-max_nb // self.tpa) * self.tpa
-        self.t["nbr"] = torch.zeros((rows * self.n,), dtype=torch.int32, device=self.dev)
-        self.t["count"] = torch.zeros((self.n,), dtype=torch.int32, device=self.dev)
-        self.list.nbr = self.t["nbr"].data_ptr()
-        self.list.count = self.t["count"].data_ptr()
+        t = self.t
+        if self.pair_lists:
+            # nbr[k * stride + slot] over the slots of every cell of every replica
+            stride = int(A.load().pg_pair_slots(self.n, self.ncells))
+            t["pair_table"] = torch.zeros((stride,), dtype=torch.int32, device=self.dev)
+            t["nbr"] = torch.zeros((max_nb * stride,), dtype=torch.int32, device=self.dev)
+            t["count"] = torch.zeros((stride,), dtype=torch.int32, device=self.dev)
+            self.list.stride = stride
+            self.list.pair_table = t["pair_table"].data_ptr()
+        else:
+            rows = -(-max_nb // self.tpa) * self.tpa
+            t.pop("pair_table", None)
+            t["nbr"] = torch.zeros((rows * self.n,), dtype=torch.int32, device=self.dev)
+            t["count"] = torch.zeros((self.n,), dtype=torch.int32, device=self.dev)
+            self.list.stride = self.n
+            self.list.pair_table = None
+        self.list.nbr = t["nbr"].data_ptr()
+        self.list.count = t["count"].data_ptr()
         self._graphs = {}
 
     # ------------------------------------------------------------------ modules
@@ -238,6 +277,8 @@ class Ensemble:
             st = self.read_status()
             if st.nonfinite:
                 raise A.PairsError("non-finite particle position met while binning")
+            if st.overflow & 32:
+                raise A.PairsError("a replica's cell grid is too small for pair-cluster lists")
             if st.overflow & 2:
                 self._alloc_list(int(st.max_neighbors * 1.15) + 8)
                 continue
@@ -362,6 +403,8 @@ class Ensemble:
         replica's first particle."""
         self.stream.synchronize()
         a, b = int(self.first[r]), int(self.first[r] + self.sizes[r])
+        if self.pair_lists:
+            return self._cluster_pairs(r, a, b)
         cnt = self.t["count"].cpu().numpy()[a:b]
         nbr = self.t["nbr"].cpu().numpy().astype(np.int64) & 0xFFFFFFFF
         uid = self.t["uid"].cpu().numpy()
@@ -379,20 +422,68 @@ class Ensemble:
         return np.stack([uid[ii] - a, uid[j] - a, dec(code & 3), dec((code >> 2) & 3), dec((code >> 4) & 3)],
                         axis=1).astype(np.int32)
 
+    def _cluster_pairs(self, r, a, b):
+        """Pair-cluster entries of replica r: the member that stores the pair first; the
+        image is the partner's nearest to that member at the last rebuild."""
+        stride = self.list.stride
+        table = self.t["pair_table"].cpu().numpy().astype(np.int64)
+        cnt = self.t["count"].cpu().numpy()
+        first = table & ((1 << 30) - 1)
+        slots = np.nonzero((table >= 0) & (first >= a) & (first < b))[0]
+        nbr = self.t["nbr"].cpu().numpy().view(np.uint32).reshape(-1, stride)
+        uid = self.t["uid"].cpu().numpy()
+        ref = self.t["pos_ref"][:, :3].cpu().numpy()
+        kmax = int(cnt[slots].max()) if len(slots) else 0
+        k = np.arange(kmax)[:, None]
+        mask = k < cnt[slots][None, :]
+        e = nbr[:kmax, slots][mask]
+        slot_first = np.broadcast_to(first[slots][None, :], mask.shape)[mask]
+        j = (e & ((1 << 30) - 1)).astype(np.int64)
+        half = 0.5 * self.boxes[r]
+        rows = []
+        for member, bit in ((0, 1 << 30), (1, 1 << 31)):
+            m = (e & np.uint32(bit)) != 0
+            i = slot_first[m] + member
+            d = ref[i] - ref[j[m]]
+            img = np.where(d > half, 1, np.where(d < -half, -1, 0))
+            rows.append(np.concatenate([(uid[i] - a)[:, None], (uid[j[m]] - a)[:, None], img], axis=1))
+        return np.concatenate(rows).astype(np.int32)
+
+    def list_size(self):
+        """(pairs, entries) of the current Verlet list over all replicas: a per-particle
+        entry holds one pair, a pair-cluster entry one or two (its member bits)."""
+        cnt = self.t["count"][: self.list.stride]
+        entries = int(cnt.sum().item())
+        if not self.pair_lists:
+            return entries, entries
+        nbr = self.t["nbr"].view(-1, self.list.stride)
+        k = torch.arange(nbr.shape[0], device=self.dev)[:, None]
+        e = nbr.to(torch.int64) & 0xFFFFFFFF
+        bits = ((e >> 30) & 1) + ((e >> 31) & 1)
+        return int(bits[k < cnt[None, :]].sum().item()), entries
+
 
 def autotune(replicas, candidates=None, steps=6, cycle=5.0, **kw):
     """Time layout candidates (tpa, block, reach, half) on this ensemble: threads per
     atom, block size, cell size (cells of >= r_list / reach) and list layout (half
-    lists with reactions, or full lists).  Per candidate one list build and `steps`
+    lists with reactions, full lists, or half = "pairs": pair-cluster half lists, for
+    the replica grids that have 2 reach + 1 cells per axis).  Per candidate one list build and `steps`
     force passes (CUDA events); score = force time + build time / `cycle`, the steps
     between rebuilds (any replica's trip rebuilds all: about every 5 steps at 512
     replicas).  Returns (best, table)."""
     if candidates is None:
         candidates = [(t, b, r, h) for h in (True, False) for r in (1, 2, 3) for t in (1, 2, 4, 8) for b in (128, 256)]
+        candidates += [(1, 192, r, "pairs") for r in (0, 1, 2, 3)]
     ens = Ensemble(replicas, graphs=False, **kw)
     table = []
     for tpa, block, reach, half in candidates:
-        ens.configure(tpa, block, reach, half=half)
+        pairs = half == "pairs"
+        if pairs and not ens.fixed_point:
+            continue
+        try:
+            ens.configure(tpa, block, reach, half=True if pairs else half, pair_lists=pairs)
+        except ValueError:                     # a replica grid too small for this layout
+            continue
         with torch.cuda.stream(ens.stream):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(ens.stream)
