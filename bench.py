@@ -457,14 +457,15 @@ def run_ensemble(args, rank, world, dist):
         (tpa, block, reach, half), table = autotune(reps)
     pairs = half == "pairs"
     ens = Ensemble(reps, tpa=tpa, block=block, reach=reach, half=True if pairs else half, pair_lists=pairs,
-                   persistent=args.ensemble_persistent)
+                   persistent=args.ensemble_persistent, partial=not args.ensemble_full_rebuilds,
+                   select=args.ensemble_select)
     ens.run(args.warmup)
     ens.synchronize()
     clocks = ClockSampler(dev.index or 0)
     clocks.start()
     lib = A.load()
     l0 = lib.pg_kernel_launches() + ens.graph_kernels - ens.graph_captured
-    b0, s0 = ens.nbuilds, ens.host_syncs
+    b0, s0, a0 = ens.nbuilds, ens.host_syncs, ens.rebuilt_atoms
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("timed")            # ncu --nvtx-include "timed/" selects these launches
     e0.record(ens.stream)
@@ -497,7 +498,7 @@ def run_ensemble(args, rank, world, dist):
         "config": {"workload": f"{len(reps)} LJ replicas, {natoms} atoms total, sizes log-uniform 500..32000, "
                                "rho U[0.6,0.9], T U[0.7,1.5], rc 2.5, skin 0.3, dt 0.005, mixed, "
                                f"{'pair-cluster half' if pairs else ('half' if ens.half else 'full')} lists, "
-                               "guard rebuilds, CUDA-graph chunks",
+                               f"guard rebuilds ({'selected replicas' if ens.partial else 'every replica'}), CUDA-graph chunks",
                    "replicas": len(reps), "atoms": natoms,
                    "autotuned": {"tpa": tpa, "block": block, "reach": reach, "half_lists": bool(half),
                                  "pair_lists": pairs}},
@@ -507,7 +508,9 @@ def run_ensemble(args, rank, world, dist):
                                      "list, guard), "
                                      "wall time including its setup"},
         "speedup_vs_one_by_one": value / one_value if one_value else None,
-        "schedule": {"rebuilds": ens.nbuilds - b0, "host_syncs": ens.host_syncs - s0},
+        "schedule": {"rebuilds": ens.nbuilds - b0, "host_syncs": ens.host_syncs - s0,
+                     "partial": ens.partial, "select": args.ensemble_select,
+                     "rebuilt_atoms_per_step": (ens.rebuilt_atoms - a0) / steps},
         "gpu_launches": launches, "clocks": clk,
     }
     print(json.dumps(line))
@@ -702,6 +705,10 @@ def main():
     ap.add_argument("--ensemble-layout", default="",
                     help="ensemble workload: fixed layout 'tpa,block,reach,half' (half 0 full, 1 half, "
                          "2 pair-cluster half lists) instead of the autotuner's")
+    ap.add_argument("--ensemble-full-rebuilds", action="store_true",
+                    help="ensemble workload: rebuild every replica at each trip (default: the selected ones)")
+    ap.add_argument("--ensemble-select", type=float, default=0.8,
+                    help="ensemble workload: partial rebuilds take the replicas displaced by this x skin/2")
     ap.add_argument("--ensemble-persistent", action="store_true",
                     help="ensemble workload: each chunk's plain steps in one persistent launch")
     ap.add_argument("--one-by-one-steps", type=int, default=100,

@@ -229,6 +229,11 @@ typedef struct {
                                     pass of pg_ensemble_integrate then zeroes force32 after its
                                     kick, and the force pass adds reactions into it */
     int32_t pad_;
+    const int32_t *rebuild;      /* device [nreplicas] or NULL: a partial rebuild.  Binning and
+                                    list build then touch only the replicas with a nonzero flag
+                                    (pg_ensemble_select); the others keep their particle order,
+                                    cells and list rows.  The cell arrays must hold the last
+                                    binning of every replica.  NULL: every replica. */
 } pg_ensemble;
 
 /* DEM particle state, sorted order (the properties of examples/dem.py:144-162).
@@ -558,6 +563,14 @@ int pg_ensemble_steps(const pg_ensemble *e, pg_particles *p, const pg_neighbor_l
 /* Per-replica thermo: out[2r] = T_r = sum/(3 n_r - 3), out[2r+1] = sum m v^2 (FP64,
  * one block per replica, fixed order).  out: device double[2 * nreplicas]. */
 int pg_ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, void *stream);
+
+/* The replicas of a partial rebuild: rebuild[r] = 1 when a particle of replica r moved
+ * more than sqrt(thresh2) since its last list build (the guard's FP32 displacement:
+ * fixed point, or the hi/lo pair), or holds a non-finite position; else 0.  thresh2 < 0
+ * selects every replica.  With thresh2 below skin^2 / 4 every replica the guard tripped
+ * on is selected.  rebuild: device int32[nreplicas].  Replaces nothing in the reference
+ * (one system per run); the batched ensemble's per-replica rebuilds. */
+int pg_ensemble_select(const pg_ensemble *e, const pg_particles *p, double thresh2, int32_t *rebuild, void *stream);
 
 /* ---- DEM (examples/dem.py) ------------------------------------------------ */
 

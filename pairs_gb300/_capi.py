@@ -112,7 +112,7 @@ class PgReplica(C.Structure):
 class PgEnsemble(C.Structure):
     _fields_ = [("nreplicas", C.c_int32), ("ncells", C.c_int32), ("replicas", C.c_void_p),
                 ("replica_of", C.c_void_p), ("tpa", C.c_int32), ("block", C.c_int32), ("half", C.c_int32),
-                ("pad_", C.c_int32)]
+                ("pad_", C.c_int32), ("rebuild", C.c_void_p)]
 
 
 class PgCsvResult(C.Structure):
@@ -186,6 +186,7 @@ SIGNATURES = {
     "pg_ensemble_integrate": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_double, C.c_int, C.c_int, C.c_double,
                                         C.c_int32, C.c_void_p, C.c_void_p]),
     "pg_ensemble_thermo": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_void_p, C.c_void_p]),
+    "pg_ensemble_select": (C.c_int, [P(PgEnsemble), P(PgParticles), C.c_double, C.c_void_p, C.c_void_p]),
     "pg_ensemble_steps": (C.c_int, [P(PgEnsemble), P(PgParticles), P(PgNeighborList), P(PgLJParams), C.c_double,
                                     C.c_double, C.c_int32, C.c_int32, C.c_void_p, PgWorkspace, C.c_double,
                                     C.c_void_p]),

@@ -42,6 +42,7 @@ int ensemble_force(const pg_ensemble *e, const pg_particles *p, const pg_neighbo
 int ensemble_integrate(const pg_ensemble *e, pg_particles *p, double dt, int kicks, int drift, double half_skin2,
                        int32_t step, pg_status *status, cudaStream_t st);
 int ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, cudaStream_t st);
+int ensemble_select(const pg_ensemble *e, const pg_particles *p, double thresh2, int32_t *rebuild, cudaStream_t st);
 int ensemble_steps(const pg_ensemble *e, pg_particles *p, const pg_neighbor_list *list, const pg_lj_params *lj,
                    double dt, double half_skin2, int32_t first, int32_t nsteps, pg_status *status, pg_workspace ws,
                    double timeout_s, cudaStream_t st);
@@ -202,6 +203,10 @@ int pg_ensemble_steps(const pg_ensemble *e, pg_particles *p, const pg_neighbor_l
                       double dt, double half_skin2, int32_t first, int32_t nsteps, pg_status *status,
                       pg_workspace ws, double timeout_s, void *stream) {
     return pg::ensemble_steps(e, p, list, lj, dt, half_skin2, first, nsteps, status, ws, timeout_s, S(stream));
+}
+
+int pg_ensemble_select(const pg_ensemble *e, const pg_particles *p, double thresh2, int32_t *rebuild, void *stream) {
+    return pg::ensemble_select(e, p, thresh2, rebuild, S(stream));
 }
 
 int pg_ensemble_thermo(const pg_ensemble *e, const pg_particles *p, double *out, void *stream) {

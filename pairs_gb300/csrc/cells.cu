@@ -165,9 +165,9 @@ int scan_exclusive_i32(const int32_t *in, int n, int32_t *out, int32_t *block_su
 }
 
 __global__ void k_scatter(int n, const int32_t *particle_cell, const int32_t *start,
-                          int32_t *cursor, int32_t *perm) {
+                          int32_t *cursor, int32_t *perm, RepMask mask) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= n) { return; }
+    if(i >= n || mask.skip(i)) { return; }
     const int c = particle_cell[i];
     perm[start[c] + atomicAdd(&cursor[c], 1)] = i;
 }
@@ -190,9 +190,11 @@ __device__ __forceinline__ long long z_order_key(double z) {
 }
 
 __global__ void k_rank_cells(int n, const int32_t *unordered, const int32_t *particle_cell, const int32_t *start,
-                             const int32_t *uid, const double *pos, int32_t *perm, pg_status *status) {
+                             const int32_t *uid, const double *pos, int32_t *perm, pg_status *status,
+                             RepMask mask) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if(s >= n) { return; }
+    if(mask.skip(s)) { perm[s] = s; return; }     // a replica left alone keeps its order
     const int v = unordered[s];
     const int c = particle_cell[v];
     const int b = start[c], e = start[c + 1];
@@ -290,9 +292,10 @@ __host__ __device__ inline StageView stage_view(char *stage, int n) {
     return v;
 }
 
-__global__ void k_gather_all(int n, const int32_t *perm, pg_particles p, const int32_t *cell, StageView v) {
+__global__ void k_gather_all(int n, const int32_t *perm, pg_particles p, const int32_t *cell, StageView v,
+                             RepMask mask) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if(k >= n) { return; }
+    if(k >= n || mask.skip(k)) { return; }
     const int s = perm[k];
     v.pos[k] = ld_d4_plain(p.pos, s);
     if(p.vel != nullptr) { v.vel[k] = ld_d4_plain(p.vel, s); }
@@ -303,9 +306,10 @@ __global__ void k_gather_all(int n, const int32_t *perm, pg_particles p, const i
     v.cell[k] = cell[s];
 }
 
-__global__ void k_copy_back_all(int n, pg_particles p, int32_t *cell, StageView v, pg_box box, int split) {
+__global__ void k_copy_back_all(int n, pg_particles p, int32_t *cell, StageView v, pg_box box, int split,
+                                RepMask mask) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if(k >= n) { return; }
+    if(k >= n || mask.skip(k)) { return; }
     const D4 x = v.pos[k];
     st_d4(p.pos, k, x);
     if(p.vel != nullptr) { st_d4(p.vel, k, v.vel[k]); }
@@ -382,8 +386,10 @@ int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cud
 // the trailing bucket), scatter, per-cell order by z then uid, the permutation of every
 // per-particle array of p and of cells->particle_cell, and the cell bookkeeping.
 // With a box, the FP32 position layouts of p are refreshed from the new positions.
+// With a replica mask, the particles of the replicas left alone keep their places (their
+// cells' counts must be in the count array already, so their starts come out unchanged).
 int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_cells *cells, pg_status *status,
-               cudaStream_t st, int32_t **perm_out, const pg_box *split_box) {
+               cudaStream_t st, int32_t **perm_out, const pg_box *split_box, RepMask mask) {
     BinWs w;
     bin_ws_layout(n, ncells, (char *) ws.ptr, &w);
     if(perm_out) { *perm_out = w.perm; }
@@ -396,14 +402,16 @@ int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_c
     // the scatter's unordered cell ranges go to the staging area's cell column (the
     // gather fills it later), the ranked order to perm
     const StageView v = stage_view(w.stage, n);
-    k_scatter<<<blocks_for(n), kBlock, 0, st>>>(n, cells->particle_cell, w.start, w.cursor, v.cell); note_launch();
-    k_rank_cells<<<blocks_for(n), kBlock, 0, st>>>(n, v.cell, cells->particle_cell, w.start, p->uid, p->pos, w.perm,
-                                                   status);
+    k_scatter<<<blocks_for(n), kBlock, 0, st>>>(n, cells->particle_cell, w.start, w.cursor, v.cell, mask);
     note_launch();
-    k_gather_all<<<blocks_for(n), kBlock, 0, st>>>(n, w.perm, *p, cells->particle_cell, v); note_launch();
+    k_rank_cells<<<blocks_for(n), kBlock, 0, st>>>(n, v.cell, cells->particle_cell, w.start, p->uid, p->pos, w.perm,
+                                                   status, mask);
+    note_launch();
+    k_gather_all<<<blocks_for(n), kBlock, 0, st>>>(n, w.perm, *p, cells->particle_cell, v, mask); note_launch();
     pg_box box = {};
     if(split_box != nullptr) { box = *split_box; }
-    k_copy_back_all<<<blocks_for(n), kBlock, 0, st>>>(n, *p, cells->particle_cell, v, box, split_box != nullptr ? 1 : 0);
+    k_copy_back_all<<<blocks_for(n), kBlock, 0, st>>>(n, *p, cells->particle_cell, v, box, split_box != nullptr ? 1 : 0,
+                                                      mask);
     note_launch();
     // cell bookkeeping for the sorted order
     cudaMemcpyAsync(cells->cell_start, w.start, (size_t) (ntot + 1) * 4, cudaMemcpyDeviceToDevice, st);
@@ -444,7 +452,7 @@ int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_worksp
         k_bin_count<<<blocks_for(n), kBlock, 0, st>>>(*box, *p, *cells, inv, count, status); note_launch();
     }
     const bool split = (p->pos_hi != nullptr && p->pos_lo != nullptr) || p->pos_fx != nullptr;
-    return bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out, split ? box : nullptr);
+    return bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out, split ? box : nullptr, RepMask{});
 }
 
 int split_positions(const pg_box *box, pg_particles *p, cudaStream_t st) {

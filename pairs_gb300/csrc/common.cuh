@@ -10,6 +10,16 @@ namespace pg {
 
 // 32-byte particle record (x, y, z, unused) of the double4 layout
 struct alignas(32) D4 { double x, y, z, w; };
+
+// The replicas of a batched ensemble that take part in a partial rebuild: particle i
+// is left alone when rebuild[replica_of[i]] == 0 (rebuild NULL: every particle takes
+// part).  Each replica's particles keep their index range, so the mask applies to a
+// particle before and after the binning's permutation alike.
+struct RepMask {
+    const int32_t *rebuild = nullptr;
+    const int32_t *replica_of = nullptr;
+    __device__ __forceinline__ bool skip(int i) const { return rebuild != nullptr && rebuild[replica_of[i]] == 0; }
+};
 __host__ __device__ __forceinline__ D4 make_d4(double x, double y, double z, double w) {
     D4 r; r.x = x; r.y = y; r.z = z; r.w = w; return r;
 }

@@ -23,7 +23,15 @@ namespace pg {
 
 int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cudaStream_t st);
 int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_cells *cells, pg_status *status,
-               cudaStream_t st, int32_t **perm_out, const pg_box *split_box);
+               cudaStream_t st, int32_t **perm_out, const pg_box *split_box, RepMask mask);
+
+// the replicas of a partial rebuild (e.rebuild), as a mask over particles
+__host__ __device__ __forceinline__ RepMask ens_mask(const pg_ensemble &e) {
+    RepMask m;
+    m.rebuild = e.rebuild;
+    m.replica_of = e.replica_of;
+    return m;
+}
 
 constexpr float kEnsBand = 1.0e-4f;
 
@@ -54,7 +62,7 @@ struct EnsArgs {
 
 __global__ void __launch_bounds__(kBlock) k_ens_count(EnsArgs a, int32_t *count) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= a.p.n) { return; }
+    if(i >= a.p.n || ens_mask(a.e).skip(i)) { return; }
     const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
     D4 x = ld_d4_plain(a.p.pos, i);
     double c3[3] = {x.x, x.y, x.z};
@@ -88,6 +96,14 @@ __global__ void __launch_bounds__(kBlock) k_ens_count(EnsArgs a, int32_t *count)
     atomicAdd(&count[cell], 1);
 }
 
+// A partial rebuild: the cells of a replica left alone keep their counts (one block per
+// replica), so the scan gives every cell its old start; its particles stay where they are.
+__global__ void __launch_bounds__(kBlock) k_ens_count_keep(EnsArgs a, int32_t *count) {
+    if(a.e.rebuild[blockIdx.x] != 0) { return; }
+    const pg_replica &R = a.e.replicas[blockIdx.x];
+    for(int c = threadIdx.x; c < R.ncells; c += blockDim.x) { count[R.cell0 + c] = a.cells.cell_count[R.cell0 + c]; }
+}
+
 // fixed-point position on a replica's own box (2^32 units per box length)
 __device__ __forceinline__ int4 ens_fx(const pg_replica &R, const D4 &x, int type) {
     return make_int4(to_fx(x.x, R.lo[0], R.fx_scale[0]), to_fx(x.y, R.lo[1], R.fx_scale[1]),
@@ -97,7 +113,7 @@ __device__ __forceinline__ int4 ens_fx(const pg_replica &R, const D4 &x, int typ
 // hi/lo split on each replica's own grid (and its fixed-point position)
 __global__ void __launch_bounds__(kBlock) k_ens_split(EnsArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= a.p.n) { return; }
+    if(i >= a.p.n || ens_mask(a.e).skip(i)) { return; }
     const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
     const double q = R.quantum, iq = 1.0 / q;
     const D4 x = ld_d4_plain(a.p.pos, i);
@@ -132,7 +148,7 @@ __device__ __forceinline__ void wrap_cell(int c, int dims, int &nc, int &s) {
 
 __global__ void __launch_bounds__(kBlock) k_ens_list(EnsArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= a.p.n) { return; }
+    if(i >= a.p.n || ens_mask(a.e).skip(i)) { return; }      // a replica left alone keeps its list
     const D4 xi = ld_d4(a.p.pos, i);
     st_d4(a.p.pos_ref, i, xi);
     const float4 hi = ld_f4(a.p.pos_hi, hl(a.p, i)), lo = ld_f4(a.p.pos_lo, hl(a.p, i));
@@ -524,6 +540,34 @@ __global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
     }
 }
 
+// The replicas of the next partial rebuild: those with a particle whose displacement
+// since the replica's last list build (the guard's FP32 measure: fixed point, or the
+// hi/lo pair) exceeds sqrt(thresh2), or is not a number.  One block per replica.
+// thresh2 below the guard's skin^2 / 4 selects every replica the guard tripped on.
+__global__ void __launch_bounds__(kBlock) k_ens_select(EnsArgs a, float thresh2, int32_t *rebuild) {
+    const pg_replica &R = a.e.replicas[blockIdx.x];
+    bool far = false;
+    for(int i = R.first + threadIdx.x; i < R.first + R.n; i += blockDim.x) {
+        float dx, dy, dz;
+        if(a.p.pos_fx != nullptr) {
+            const int4 xf = ld_i4(a.p.pos_fx, i), rf = ld_i4(a.p.ref_fx, i);
+            dx = (float) fx_diff(xf.x, rf.x) * R.fx_unit[0];
+            dy = (float) fx_diff(xf.y, rf.y) * R.fx_unit[1];
+            dz = (float) fx_diff(xf.z, rf.z) * R.fx_unit[2];
+        } else {
+            const float4 h = ld_f4(a.p.pos_hi, hl(a.p, i)), l = ld_f4(a.p.pos_lo, hl(a.p, i));
+            const float4 rh = ld_f4(a.p.ref_hi, i), rl = ld_f4(a.p.ref_lo, i);
+            dx = (h.x - rh.x) + (l.x - rl.x);
+            dy = (h.y - rh.y) + (l.y - rl.y);
+            dz = (h.z - rh.z) + (l.z - rl.z);
+        }
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        far = far || !(d2 <= thresh2);
+    }
+    far = __syncthreads_or(far) != 0;
+    if(threadIdx.x == 0) { rebuild[blockIdx.x] = far || thresh2 < 0.0f ? 1 : 0; }
+}
+
 // ------------------------------------------------------------------ persistent steps
 
 // The plain steps of a chunk in one cooperative launch (pg_ensemble_steps): for each
@@ -637,8 +681,13 @@ int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_work
     if(rc) { return rc; }
     EnsArgs a = {};
     a.e = *e; a.p = *p; a.cells = *cells; a.status = status;
+    if(e->rebuild != nullptr) {
+        // a partial rebuild: the cell arrays must hold the last binning of every replica
+        if(!cells->cell_count || !cells->cell_start) { return PG_ERR_ARGUMENT; }
+        k_ens_count_keep<<<e->nreplicas, kBlock, 0, st>>>(a, count); note_launch();
+    }
     if(n > 0) { k_ens_count<<<blocks_for(n), kBlock, 0, st>>>(a, count); note_launch(); }
-    rc = bin_finish(n, e->ncells, ws, p, cells, status, st, nullptr, nullptr);
+    rc = bin_finish(n, e->ncells, ws, p, cells, status, st, nullptr, nullptr, ens_mask(*e));
     if(rc || n == 0) { return rc; }
     a.p = *p;
     k_ens_split<<<blocks_for(n), kBlock, 0, st>>>(a); note_launch();
@@ -805,6 +854,17 @@ int ensemble_steps(const pg_ensemble *e, pg_particles *p, const pg_neighbor_list
         return PG_ERR_CUDA;
     }
     note_launch();
+    return launch_status();
+}
+
+int ensemble_select(const pg_ensemble *e, const pg_particles *p, double thresh2, int32_t *rebuild, cudaStream_t st) {
+    const bool fixed = p != nullptr && p->pos_fx != nullptr;
+    if(!ens_ok(e, p) || !rebuild || (fixed ? !p->ref_fx : (!p->pos_hi || !p->pos_lo || !p->ref_hi || !p->ref_lo))) {
+        return PG_ERR_ARGUMENT;
+    }
+    EnsArgs a = {};
+    a.e = *e; a.p = *p;
+    k_ens_select<<<e->nreplicas, kBlock, 0, st>>>(a, (float) thresh2, rebuild); note_launch();
     return launch_status();
 }
 

@@ -72,6 +72,7 @@ struct PcBuildArgs {
     float r2_lo, r2_hi;          // screening band, box units squared when kCubic
     const pg_replica *replicas;  // batched ensembles: each slot's box and grid from its replica
     const int32_t *replica_of;
+    const int32_t *rebuild;      // batched ensembles: the replicas of a partial rebuild (or NULL)
 };
 
 // The FP64 decision of a candidate in the screening band: the reference's separately
@@ -141,6 +142,9 @@ __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, Pc
     int cnt = 0;
     if(rec >= 0) {
         const int ia = rec & (int) kPcIndexMask;
+        // a replica left alone by a partial rebuild keeps its rows (its cells, and so its
+        // slots, are unchanged)
+        if(kEns && a.rebuild != nullptr && a.rebuild[a.replica_of[ia]] == 0) { return; }
         const bool has_b = (rec & kPcHasB) != 0;
         const int ib = has_b ? ia + 1 : ia;
         const int4 fa = ld_i4(a.p.pos_fx, ia), fb = ld_i4(a.p.pos_fx, ib);
@@ -537,7 +541,7 @@ int pc_build(const pg_box *box, const pg_particles *p, const pg_cells *cells, pg
     a.box = *box; a.p = *p; a.cells = *cells; a.list = *list; a.r_list2 = r_list2;
     a.r2_lo = (float) r_list2 * (1.0f - kPcScreenBand);
     a.r2_hi = (float) r_list2 * (1.0f + kPcScreenBand);
-    a.replicas = nullptr; a.replica_of = nullptr;
+    a.replicas = nullptr; a.replica_of = nullptr; a.rebuild = nullptr;
     cudaMemsetAsync(list->pair_table, 0xff, (size_t) list->stride * sizeof(int32_t), st);
     if(cells->ncells > 0) {
         k_pc_table<<<blocks_for(cells->ncells), kBlock, 0, st>>>(*cells, list->pair_table); note_launch();
@@ -600,7 +604,7 @@ int ens_pc_build(const pg_ensemble *e, const pg_particles *p, const pg_cells *ce
     a.box = pg_box{}; a.p = *p; a.cells = *cells; a.list = *list; a.r_list2 = r_list2;
     a.r2_lo = (float) r_list2 * (1.0f - kPcScreenBand);
     a.r2_hi = (float) r_list2 * (1.0f + kPcScreenBand);
-    a.replicas = e->replicas; a.replica_of = e->replica_of;
+    a.replicas = e->replicas; a.replica_of = e->replica_of; a.rebuild = e->rebuild;
     cudaMemsetAsync(list->pair_table, 0xff, (size_t) list->stride * sizeof(int32_t), st);
     if(cells->ncells > 0) {
         k_pc_table<<<blocks_for(cells->ncells), kBlock, 0, st>>>(*cells, list->pair_table); note_launch();

@@ -7,7 +7,14 @@ phase (pg_ensemble_*).  Between list rebuilds the steps run speculatively in chu
 captured once as a CUDA graph: a chunk of K steps is 2K kernel nodes (integrate,
 force), replayed without host work; the FP64 displacement guard freezes every later
 pass on the device once any replica's atom moved more than skin/2, the host then
-rebuilds all replicas and continues from the step after the trip.
+rebuilds the replicas that need it and continues from the step after the trip.
+
+Partial rebuilds (`partial=True`, the default with the guard policy): at a trip only the
+replicas with an atom displaced by more than `select` x skin/2 since their own last build
+are binned and listed again (pg_ensemble_select, pg_ensemble.rebuild); the others keep
+their particle order, cells and lists.  A replica's guard reference is its own last
+build, so every replica rebuilds on its own cycle; `select` below 1 rebuilds replicas
+close to their trip along with the tripped ones, saving host round trips.
 
 `autotune()` picks the threads per atom of the force kernel, its block size, the
 cell size (27 cells of >= r_list, or 125 cells of >= r_list/2) and the list layout
@@ -29,7 +36,7 @@ INT32_MAX = 2 ** 31 - 1
 class Ensemble:
     def __init__(self, replicas, *, cutoff=2.5, skin=0.3, dt=0.005, epsilon=1.0, sigma6=1.0, tpa=1, block=256,
                  reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, fixed_point=None,
-                 half=True, pair_lists=False, persistent=False, device="cuda"):
+                 half=True, pair_lists=False, persistent=False, partial=True, select=0.8, device="cuda"):
         A.load()
         if not torch.cuda.is_available():
             raise A.PairsError("a CUDA device is required: the particle path runs only on the GPU")
@@ -41,6 +48,11 @@ class Ensemble:
         # persistent: a chunk's plain steps as one cooperative launch (pg_ensemble_steps)
         # instead of two kernel nodes per step; needs fixed-point positions
         self.persistent = bool(persistent) and policy == "guard"
+        # partial rebuilds: the replicas whose displacement reached select * skin/2
+        if not 0.0 < select < 0.95:
+            raise ValueError("select must lie in (0, 0.95): the tripped replicas must be selected")
+        self.partial = bool(partial) and policy == "guard"
+        self.select2 = (select * 0.5 * skin) ** 2
         self.cutoff, self.skin, self.dt = cutoff, skin, dt
         self.r_list = cutoff + skin
         self.r_list2 = self.r_list * self.r_list
@@ -67,6 +79,7 @@ class Ensemble:
         self.pair_lists = False
         self.ts = 0
         self.nbuilds = 0
+        self.rebuilt_atoms = 0                 # atoms binned and listed again, over all builds
         self.host_syncs = 0
         self.chunk = chunk
         self._cycle = 6
@@ -116,9 +129,12 @@ class Ensemble:
 
         init = A.PgStatus()
         init.guard_tripped = INT32_MAX
-        t["status_init"] = torch.tensor(np.frombuffer(bytes(init), dtype=np.int32).copy(), device=self.dev)
-        t["status"] = t["status_init"].clone()
+        # the status record, then the per-replica rebuild flags (one read gets both)
+        words = np.frombuffer(bytes(init), dtype=np.int32)
+        t["status"] = torch.tensor(np.concatenate([words, np.ones(self.nrep, np.int32)]), device=self.dev)
         self.status_ptr = C.c_void_p(t["status"].data_ptr())
+        self.nstatus = len(words)
+        self.flags_ptr = C.c_void_p(t["status"].data_ptr() + 4 * self.nstatus)
         t["thermo"] = z((2 * self.nrep,), f64)
         self.e = A.PgEnsemble()
         self.e.nreplicas = self.nrep
@@ -226,6 +242,7 @@ class Ensemble:
         self.ws = A.PgWorkspace(t["ws"].data_ptr(), int(wsb))
         self._alloc_list(self._max_nb)
         self._graphs = {}
+        self._full_next = True                 # new cell arrays: the next build bins every replica
         torch.cuda.synchronize(self.dev)       # the new buffers are used on self.stream
 
     def _alloc_list(self, max_nb):
@@ -257,32 +274,51 @@ class Ensemble:
         self.host_syncs += 1
         with torch.cuda.stream(self.stream):
             s = self.t["status"].cpu().numpy()
-        return A.PgStatus.from_buffer_copy(s.tobytes())
+        self._flags = s[self.nstatus:]
+        return A.PgStatus.from_buffer_copy(s[: self.nstatus].tobytes())
 
-    def rebuild(self):
+    def rebuild(self, partial=False):
+        """Bin and list every replica again, or with partial=True (and the ensemble's
+        `partial` option) only those selected by displacement."""
         # the status resets below are torch ops: they must run on the stream the
         # library's kernels run on, whichever stream the caller has current
         with torch.cuda.stream(self.stream):
-            self._rebuild()
+            self._rebuild(partial and self.partial and not self._full_next)
 
-    def _rebuild(self):
+    def _rebuild(self, partial):
         by = C.byref
         self.p.guard = None
-        A.call("pg_ensemble_bin", by(self.e), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
-        while True:
-            self.t["status"][0] = 0
-            self.t["status"][2] = 0
-            A.call("pg_ensemble_build_lists", by(self.e), by(self.p), by(self.cells), by(self.list), self.r_list2,
-                   self.status_ptr, self.sh)
-            st = self.read_status()
-            if st.nonfinite:
-                raise A.PairsError("non-finite particle position met while binning")
-            if st.overflow & 32:
-                raise A.PairsError("a replica's cell grid is too small for pair-cluster lists")
-            if st.overflow & 2:
-                self._alloc_list(int(st.max_neighbors * 1.15) + 8)
-                continue
-            break
+        if partial:
+            A.call("pg_ensemble_select", by(self.e), by(self.p), self.select2, self.flags_ptr, self.sh)
+            self.e.rebuild = self.flags_ptr.value
+        else:
+            self.t["status"][self.nstatus:] = 1
+        try:
+            A.call("pg_ensemble_bin", by(self.e), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
+            while True:
+                self.t["status"][0] = 0
+                self.t["status"][2] = 0
+                A.call("pg_ensemble_build_lists", by(self.e), by(self.p), by(self.cells), by(self.list),
+                       self.r_list2, self.status_ptr, self.sh)
+                st = self.read_status()
+                if st.nonfinite:
+                    raise A.PairsError("non-finite particle position met while binning")
+                if st.overflow & 32:
+                    raise A.PairsError("a replica's cell grid is too small for pair-cluster lists")
+                if st.overflow & 2:
+                    # new (empty) list arrays: every replica is binned and listed again
+                    self._alloc_list(int(st.max_neighbors * 1.15) + 8)
+                    if self.e.rebuild:
+                        self.e.rebuild = None
+                        self.t["status"][self.nstatus:] = 1
+                        A.call("pg_ensemble_bin", by(self.e), by(self.p), by(self.cells), self.ws, self.status_ptr,
+                               self.sh)
+                    continue
+                break
+        finally:
+            self.e.rebuild = None
+        self.rebuilt_atoms += int(np.dot(self._flags != 0, self.sizes))
+        self._full_next = False
         self.t["status"][4] = INT32_MAX
         self.nbuilds += 1
         self._build_ts = self.ts
@@ -343,7 +379,7 @@ class Ensemble:
                     # after step 0 otherwise, which owes no final half kick)
                     self._integrate(self.ts, 2 if self._pending else 1)
                     if self.policy == "every" or self.read_status().guard_tripped != INT32_MAX:
-                        self.rebuild()
+                        self.rebuild(partial=True)
                     self._force(self.ts)
                     self.ts += 1
                     self._pending = True
@@ -360,7 +396,7 @@ class Ensemble:
                     # positions are those of step start + g; rebuild, then its force
                     self.ts = start + g
                     self._cycle = max(1, self.ts - self._build_ts)
-                    self.rebuild()
+                    self.rebuild(partial=True)
                     self._force(self.ts)
                     self.ts += 1
                 else:

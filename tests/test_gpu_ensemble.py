@@ -13,7 +13,11 @@
 * per-replica thermo equals the oracle's temperature of the same velocities;
 * pair-cluster half lists over the ensemble (two particles of a cell per row) hold
   every pair of the oracle's list once, non-cubic replicas included, their forces
-  agree with the oracle, and their trajectory follows the per-particle half lists.
+  agree with the oracle, and their trajectory follows the per-particle half lists;
+* a partial rebuild bins and lists only the selected replicas: the others keep their
+  particle order and list rows entry for entry, the selected ones get the oracle's
+  list of their current positions, and a guarded run with partial rebuilds keeps every
+  pair (forces against the oracle's) while listing fewer atoms than full rebuilds.
 """
 import numpy as np
 import pytest
@@ -259,3 +263,92 @@ def test_pair_cluster_trajectory_follows_per_particle_half_lists():
         sim.step()
         _, _, f_ref = sim.state()
         assert rms_rel(f, f_ref) < 2e-5
+
+
+@pytest.mark.parametrize("layout", ["full", "pairs"])
+def test_partial_rebuild_touches_only_selected_replicas(layout):
+    import ctypes as C
+    from pairs_gb300 import _capi as A
+    from pairs_gb300.ensemble import Ensemble
+    reps = replicas()
+    kw = dict(tpa=2, reach=2, half=False) if layout == "full" else dict(reach=2, pair_lists=True)
+    ens = Ensemble(reps, partial=True, **kw)
+    ens.run(12)
+    ens.synchronize()
+    t = ens.t
+    uid0 = t["uid"].cpu().numpy().copy()
+    cnt0 = t["count"].cpu().numpy().copy()
+    nbr0 = t["nbr"].cpu().numpy().copy()
+    table0 = t["pair_table"].cpu().numpy().copy() if layout == "pairs" else None
+    flags = np.array([1, 0, 1, 0], dtype=np.int32)
+    with torch.cuda.stream(ens.stream):
+        t["status"][ens.nstatus:] = torch.from_numpy(flags).to(ens.dev)
+        ens.e.rebuild = ens.flags_ptr.value
+        by = C.byref
+        A.call("pg_ensemble_bin", by(ens.e), by(ens.p), by(ens.cells), ens.ws, ens.status_ptr, ens.sh)
+        A.call("pg_ensemble_build_lists", by(ens.e), by(ens.p), by(ens.cells), by(ens.list), ens.r_list2,
+               ens.status_ptr, ens.sh)
+        ens.e.rebuild = None
+        assert ens.read_status().overflow == 0
+        t["force32"].zero_()                   # half lists accumulate into zeros
+        ens._force(ens.ts)
+    ens.synchronize()
+    uid1 = t["uid"].cpu().numpy()
+    cnt1 = t["count"].cpu().numpy()
+    nbr1 = t["nbr"].cpu().numpy()
+    cell = t["particle_cell"].cpu().numpy()
+    for r, st in enumerate(reps):
+        a, b = int(ens.first[r]), int(ens.first[r] + ens.sizes[r])
+        assert np.all(np.diff(cell[a:b]) >= 0), r                 # cell order
+        if not flags[r]:
+            assert np.array_equal(uid1[a:b], uid0[a:b]), r
+            if layout == "full":
+                assert np.array_equal(cnt1[a:b], cnt0[a:b]), r
+                # entry k of particle i at ((k / tpa) * n + i) * tpa + k % tpa
+                rows0, rows1 = nbr0.reshape(-1, ens.n, ens.tpa), nbr1.reshape(-1, ens.n, ens.tpa)
+                assert np.array_equal(rows1[:, a:b], rows0[:, a:b]), r
+        else:
+            pos, vel, _ = ens.replica_state(r)
+            sim = olj.Sim(dict(st, pos=pos, vel=vel), every=1, exact_sync=True)
+            sim.step()
+            got, ref = ens.replica_pairs(r), sim.pairs()
+            if layout == "full":
+                assert np.array_equal(canonical_pairs(got), canonical_pairs(ref)), r
+            else:
+                assert np.array_equal(unordered(got), unordered(ref)), r
+    if layout == "pairs":
+        # the rows of the replicas left alone: same slots, same entries
+        table1 = t["pair_table"].cpu().numpy()
+        first = table1 & ((1 << 30) - 1)
+        keep = (table1 >= 0) & np.isin(t["replica_of"].cpu().numpy()[np.clip(first, 0, ens.n - 1)], [1, 3])
+        assert np.array_equal(table1[keep], table0[keep])
+        assert np.array_equal(cnt1[keep], cnt0[keep])
+        stride = ens.list.stride
+        for k in range(int(cnt1[keep].max())):
+            row0, row1 = nbr0[k * stride:(k + 1) * stride], nbr1[k * stride:(k + 1) * stride]
+            live = keep & (cnt1 > k)
+            assert np.array_equal(row1[live], row0[live])
+    # every replica's force (lists of both kinds) against the oracle's
+    for r, st in enumerate(reps):
+        pos, vel, f = ens.replica_state(r)
+        sim = olj.Sim(dict(st, pos=pos, vel=vel), every=1, exact_sync=True)
+        sim.step()
+        assert rms_rel(f, sim.state()[2]) < 2e-5, r
+
+
+@pytest.mark.parametrize("pairs", [False, True])
+def test_partial_rebuilds_keep_every_pair(pairs):
+    from pairs_gb300.ensemble import Ensemble
+    reps = replicas()
+    kw = dict(reach=2, pair_lists=True) if pairs else dict(tpa=4, half=True)
+    ens = Ensemble(reps, partial=True, **kw)
+    ens.run(80)
+    ens.synchronize()
+    assert ens.nbuilds >= 2
+    # some builds left replicas alone
+    assert ens.rebuilt_atoms < ens.nbuilds * ens.n
+    for r, st in enumerate(reps):
+        pos, vel, f = ens.replica_state(r)
+        sim = olj.Sim(dict(st, pos=pos, vel=vel), every=1, exact_sync=True)
+        sim.step()
+        assert rms_rel(f, sim.state()[2]) < 2e-5, r
