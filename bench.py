@@ -707,7 +707,7 @@ def main():
                          "2 pair-cluster half lists) instead of the autotuner's")
     ap.add_argument("--ensemble-full-rebuilds", action="store_true",
                     help="ensemble workload: rebuild every replica at each trip (default: the selected ones)")
-    ap.add_argument("--ensemble-select", type=float, default=0.8,
+    ap.add_argument("--ensemble-select", type=float, default=0.6,
                     help="ensemble workload: partial rebuilds take the replicas displaced by this x skin/2")
     ap.add_argument("--ensemble-persistent", action="store_true",
                     help="ensemble workload: each chunk's plain steps in one persistent launch")

@@ -306,8 +306,9 @@ __global__ void k_gather_all(int n, const int32_t *perm, pg_particles p, const i
     v.cell[k] = cell[s];
 }
 
+// With replicas (a batched ensemble), each particle's layouts are on its replica's grid.
 __global__ void k_copy_back_all(int n, pg_particles p, int32_t *cell, StageView v, pg_box box, int split,
-                                RepMask mask) {
+                                RepMask mask, const pg_replica *replicas) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if(k >= n || mask.skip(k)) { return; }
     const D4 x = v.pos[k];
@@ -320,8 +321,9 @@ __global__ void k_copy_back_all(int n, pg_particles p, int32_t *cell, StageView 
     if(p.flags != nullptr) { p.flags[k] = v.flags[k]; }
     cell[k] = v.cell[k];
     if(split) {
+        const pg_replica *R = replicas != nullptr ? &replicas[mask.replica_of[k]] : nullptr;
         if(p.pos_hi != nullptr) {
-            const double q = box.quantum, iq = 1.0 / q;
+            const double q = R != nullptr ? R->quantum : box.quantum, iq = 1.0 / q;
             float4 h, l;
             split_pos(x.x, iq, q, h.x, l.x);
             split_pos(x.y, iq, q, h.y, l.y);
@@ -331,7 +333,9 @@ __global__ void k_copy_back_all(int n, pg_particles p, int32_t *cell, StageView 
             st_f4(p.pos_hi, hl(p, k), h);
             st_f4(p.pos_lo, hl(p, k), l);
         }
-        if(p.pos_fx != nullptr) { st_i4(p.pos_fx, k, fx_position(box, x.x, x.y, x.z, type)); }
+        if(p.pos_fx != nullptr) {
+            st_i4(p.pos_fx, k, R != nullptr ? replica_fx(*R, x.x, x.y, x.z, type) : fx_position(box, x.x, x.y, x.z, type));
+        }
     }
 }
 
@@ -388,8 +392,11 @@ int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cud
 // With a box, the FP32 position layouts of p are refreshed from the new positions.
 // With a replica mask, the particles of the replicas left alone keep their places (their
 // cells' counts must be in the count array already, so their starts come out unchanged).
+// With split_replicas (a batched ensemble; mask.replica_of set), the layouts are refreshed
+// on each particle's replica grid.
 int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_cells *cells, pg_status *status,
-               cudaStream_t st, int32_t **perm_out, const pg_box *split_box, RepMask mask) {
+               cudaStream_t st, int32_t **perm_out, const pg_box *split_box, RepMask mask,
+               const pg_replica *split_replicas) {
     BinWs w;
     bin_ws_layout(n, ncells, (char *) ws.ptr, &w);
     if(perm_out) { *perm_out = w.perm; }
@@ -410,8 +417,8 @@ int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_c
     k_gather_all<<<blocks_for(n), kBlock, 0, st>>>(n, w.perm, *p, cells->particle_cell, v, mask); note_launch();
     pg_box box = {};
     if(split_box != nullptr) { box = *split_box; }
-    k_copy_back_all<<<blocks_for(n), kBlock, 0, st>>>(n, *p, cells->particle_cell, v, box, split_box != nullptr ? 1 : 0,
-                                                      mask);
+    const int split = split_box != nullptr || split_replicas != nullptr ? 1 : 0;
+    k_copy_back_all<<<blocks_for(n), kBlock, 0, st>>>(n, *p, cells->particle_cell, v, box, split, mask, split_replicas);
     note_launch();
     // cell bookkeeping for the sorted order
     cudaMemcpyAsync(cells->cell_start, w.start, (size_t) (ntot + 1) * 4, cudaMemcpyDeviceToDevice, st);
@@ -452,7 +459,7 @@ int bin_particles(const pg_box *box, pg_particles *p, pg_cells *cells, pg_worksp
         k_bin_count<<<blocks_for(n), kBlock, 0, st>>>(*box, *p, *cells, inv, count, status); note_launch();
     }
     const bool split = (p->pos_hi != nullptr && p->pos_lo != nullptr) || p->pos_fx != nullptr;
-    return bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out, split ? box : nullptr, RepMask{});
+    return bin_finish(n, cells->ncells, ws, p, cells, status, st, perm_out, split ? box : nullptr, RepMask{}, nullptr);
 }
 
 int split_positions(const pg_box *box, pg_particles *p, cudaStream_t st) {

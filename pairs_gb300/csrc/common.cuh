@@ -176,6 +176,12 @@ __device__ __forceinline__ int4 fx_position(const pg_box &box, double x, double 
                      to_fx(z, box.lo[2], box.fx_scale[2]), type);
 }
 
+// fixed-point position on a batched-ensemble replica's own box (2^32 units per length)
+__device__ __forceinline__ int4 replica_fx(const pg_replica &R, double x, double y, double z, int type) {
+    return make_int4(to_fx(x, R.lo[0], R.fx_scale[0]), to_fx(y, R.lo[1], R.fx_scale[1]),
+                     to_fx(z, R.lo[2], R.fx_scale[2]), type);
+}
+
 // wrapped difference a - b of two fixed-point coordinates
 __device__ __forceinline__ int fx_diff(int32_t a, int32_t b) { return (int) ((uint32_t) a - (uint32_t) b); }
 

@@ -23,7 +23,8 @@ namespace pg {
 
 int bin_prepare(int32_t n, int32_t ncells, pg_workspace ws, int32_t **count, cudaStream_t st);
 int bin_finish(int32_t n, int32_t ncells, pg_workspace ws, pg_particles *p, pg_cells *cells, pg_status *status,
-               cudaStream_t st, int32_t **perm_out, const pg_box *split_box, RepMask mask);
+               cudaStream_t st, int32_t **perm_out, const pg_box *split_box, RepMask mask,
+               const pg_replica *split_replicas);
 
 // the replicas of a partial rebuild (e.rebuild), as a mask over particles
 __host__ __device__ __forceinline__ RepMask ens_mask(const pg_ensemble &e) {
@@ -106,26 +107,7 @@ __global__ void __launch_bounds__(kBlock) k_ens_count_keep(EnsArgs a, int32_t *c
 
 // fixed-point position on a replica's own box (2^32 units per box length)
 __device__ __forceinline__ int4 ens_fx(const pg_replica &R, const D4 &x, int type) {
-    return make_int4(to_fx(x.x, R.lo[0], R.fx_scale[0]), to_fx(x.y, R.lo[1], R.fx_scale[1]),
-                     to_fx(x.z, R.lo[2], R.fx_scale[2]), type);
-}
-
-// hi/lo split on each replica's own grid (and its fixed-point position)
-__global__ void __launch_bounds__(kBlock) k_ens_split(EnsArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= a.p.n || ens_mask(a.e).skip(i)) { return; }
-    const pg_replica &R = a.e.replicas[a.e.replica_of[i]];
-    const double q = R.quantum, iq = 1.0 / q;
-    const D4 x = ld_d4_plain(a.p.pos, i);
-    float4 h, l;
-    split_pos(x.x, iq, q, h.x, l.x);
-    split_pos(x.y, iq, q, h.y, l.y);
-    split_pos(x.z, iq, q, h.z, l.z);
-    h.w = __int_as_float(a.p.type != nullptr ? a.p.type[i] : 0);
-    l.w = 0.0f;
-    st_f4(a.p.pos_hi, hl(a.p, i), h);
-    st_f4(a.p.pos_lo, hl(a.p, i), l);
-    if(a.p.pos_fx != nullptr) { st_i4(a.p.pos_fx, i, ens_fx(R, x, __float_as_int(h.w))); }
+    return replica_fx(R, x.x, x.y, x.z, type);
 }
 
 // ------------------------------------------------------------------ list build
@@ -542,30 +524,34 @@ __global__ void __launch_bounds__(kBlock) k_ens_integrate(EnsArgs a) {
 
 // The replicas of the next partial rebuild: those with a particle whose displacement
 // since the replica's last list build (the guard's FP32 measure: fixed point, or the
-// hi/lo pair) exceeds sqrt(thresh2), or is not a number.  One block per replica.
-// thresh2 below the guard's skin^2 / 4 selects every replica the guard tripped on.
+// hi/lo pair) exceeds sqrt(thresh2), or is not a number.  One thread per particle over
+// flags zeroed before; a flag already set is not stored again.  thresh2 below the
+// guard's skin^2 / 4 selects every replica the guard tripped on.
 __global__ void __launch_bounds__(kBlock) k_ens_select(EnsArgs a, float thresh2, int32_t *rebuild) {
-    const pg_replica &R = a.e.replicas[blockIdx.x];
-    bool far = false;
-    for(int i = R.first + threadIdx.x; i < R.first + R.n; i += blockDim.x) {
-        float dx, dy, dz;
-        if(a.p.pos_fx != nullptr) {
-            const int4 xf = ld_i4(a.p.pos_fx, i), rf = ld_i4(a.p.ref_fx, i);
-            dx = (float) fx_diff(xf.x, rf.x) * R.fx_unit[0];
-            dy = (float) fx_diff(xf.y, rf.y) * R.fx_unit[1];
-            dz = (float) fx_diff(xf.z, rf.z) * R.fx_unit[2];
-        } else {
-            const float4 h = ld_f4(a.p.pos_hi, hl(a.p, i)), l = ld_f4(a.p.pos_lo, hl(a.p, i));
-            const float4 rh = ld_f4(a.p.ref_hi, i), rl = ld_f4(a.p.ref_lo, i);
-            dx = (h.x - rh.x) + (l.x - rl.x);
-            dy = (h.y - rh.y) + (l.y - rl.y);
-            dz = (h.z - rh.z) + (l.z - rl.z);
-        }
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        far = far || !(d2 <= thresh2);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= a.p.n) { return; }
+    const int r = a.e.replica_of[i];
+    const pg_replica &R = a.e.replicas[r];
+    float dx, dy, dz;
+    if(a.p.pos_fx != nullptr) {
+        const int4 xf = ld_i4(a.p.pos_fx, i), rf = ld_i4(a.p.ref_fx, i);
+        dx = (float) fx_diff(xf.x, rf.x) * R.fx_unit[0];
+        dy = (float) fx_diff(xf.y, rf.y) * R.fx_unit[1];
+        dz = (float) fx_diff(xf.z, rf.z) * R.fx_unit[2];
+    } else {
+        const float4 h = ld_f4(a.p.pos_hi, hl(a.p, i)), l = ld_f4(a.p.pos_lo, hl(a.p, i));
+        const float4 rh = ld_f4(a.p.ref_hi, i), rl = ld_f4(a.p.ref_lo, i);
+        dx = (h.x - rh.x) + (l.x - rl.x);
+        dy = (h.y - rh.y) + (l.y - rl.y);
+        dz = (h.z - rh.z) + (l.z - rl.z);
     }
-    far = __syncthreads_or(far) != 0;
-    if(threadIdx.x == 0) { rebuild[blockIdx.x] = far || thresh2 < 0.0f ? 1 : 0; }
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if(!(d2 <= thresh2) && rebuild[r] == 0) { rebuild[r] = 1; }
+}
+
+__global__ void k_ens_select_all(int nreplicas, int32_t *rebuild) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if(r < nreplicas) { rebuild[r] = 1; }
 }
 
 // ------------------------------------------------------------------ persistent steps
@@ -672,7 +658,9 @@ static bool ens_ok(const pg_ensemble *e, const pg_particles *p) {
 
 int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_workspace ws, pg_status *status,
                  cudaStream_t st) {
-    if(!ens_ok(e, p) || !cells || !status || !p->pos || !p->pos_hi || !p->pos_lo || cells->ncells != e->ncells) {
+    // hi/lo layouts are optional with fixed-point positions (the pair-cluster path reads none)
+    if(!ens_ok(e, p) || !cells || !status || !p->pos || (!p->pos_fx && (!p->pos_hi || !p->pos_lo)) ||
+       (!p->pos_hi) != (!p->pos_lo) || cells->ncells != e->ncells) {
         return PG_ERR_ARGUMENT;
     }
     const int n = p->n;
@@ -687,11 +675,8 @@ int ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_work
         k_ens_count_keep<<<e->nreplicas, kBlock, 0, st>>>(a, count); note_launch();
     }
     if(n > 0) { k_ens_count<<<blocks_for(n), kBlock, 0, st>>>(a, count); note_launch(); }
-    rc = bin_finish(n, e->ncells, ws, p, cells, status, st, nullptr, nullptr, ens_mask(*e));
-    if(rc || n == 0) { return rc; }
-    a.p = *p;
-    k_ens_split<<<blocks_for(n), kBlock, 0, st>>>(a); note_launch();
-    return launch_status();
+    // the copy back refreshes hi/lo and the fixed-point records on each replica's grid
+    return bin_finish(n, e->ncells, ws, p, cells, status, st, nullptr, nullptr, ens_mask(*e), e->replicas);
 }
 
 int ens_pc_build(const pg_ensemble *e, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
@@ -864,7 +849,12 @@ int ensemble_select(const pg_ensemble *e, const pg_particles *p, double thresh2,
     }
     EnsArgs a = {};
     a.e = *e; a.p = *p;
-    k_ens_select<<<e->nreplicas, kBlock, 0, st>>>(a, (float) thresh2, rebuild); note_launch();
+    if(thresh2 < 0.0) {
+        k_ens_select_all<<<blocks_for(e->nreplicas), kBlock, 0, st>>>(e->nreplicas, rebuild); note_launch();
+    } else {
+        cudaMemsetAsync(rebuild, 0, (size_t) e->nreplicas * sizeof(int32_t), st);
+        if(p->n > 0) { k_ens_select<<<blocks_for(p->n), kBlock, 0, st>>>(a, (float) thresh2, rebuild); note_launch(); }
+    }
     return launch_status();
 }
 

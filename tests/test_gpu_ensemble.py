@@ -341,7 +341,9 @@ def test_partial_rebuilds_keep_every_pair(pairs):
     from pairs_gb300.ensemble import Ensemble
     reps = replicas()
     kw = dict(reach=2, pair_lists=True) if pairs else dict(tpa=4, half=True)
-    ens = Ensemble(reps, partial=True, **kw)
+    # select 0.9: only replicas close to their own trip join a rebuild (four replicas
+    # at the default 0.6 are often all selected)
+    ens = Ensemble(reps, partial=True, select=0.9, **kw)
     ens.run(80)
     ens.synchronize()
     assert ens.nbuilds >= 2
@@ -352,3 +354,19 @@ def test_partial_rebuilds_keep_every_pair(pairs):
         sim = olj.Sim(dict(st, pos=pos, vel=vel), every=1, exact_sync=True)
         sim.step()
         assert rms_rel(f, sim.state()[2]) < 2e-5, r
+
+
+def test_autotune_picks_the_fastest_finalist():
+    """Stage 1 scores every layout; stage 2 runs the best scores as real guarded steps
+    and returns the fastest of them."""
+    from pairs_gb300.ensemble import autotune
+    reps = replicas()
+    cands = [(2, 128, 2, True), (1, 256, 1, False), (1, 192, 2, "pairs"), (1, 192, 1, "pairs")]
+    best, table = autotune(reps, candidates=cands, finalists=2, trial_steps=12)
+    # reach-1 pair-cluster lists do not fit the 500-atom replica's grid: skipped
+    assert len(table) == 3 and not any(r["half"] == "pairs" and r["reach"] == 1 for r in table)
+    timed = [r for r in table if "step_ms" in r]
+    assert len(timed) == 2
+    assert sorted(table, key=lambda r: r["score"])[:2] == sorted(timed, key=lambda r: r["score"])
+    fastest = min(timed, key=lambda r: r["step_ms"])
+    assert best == (fastest["tpa"], fastest["block"], fastest["reach"], fastest["half"])
