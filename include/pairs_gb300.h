@@ -228,7 +228,8 @@ typedef struct {
     int32_t half;                /* 1: half lists (the list's own flag must agree); the drift
                                     pass of pg_ensemble_integrate then zeroes force32 after its
                                     kick, and the force pass adds reactions into it */
-    int32_t pad_;
+    int32_t cubic;               /* 1: every replica's box is cubic; the pair-cluster build then
+                                    screens distances in fixed-point units (0: in lengths) */
     const int32_t *rebuild;      /* device [nreplicas] or NULL: a partial rebuild.  Binning and
                                     list build then touch only the replicas with a nonzero flag
                                     (pg_ensemble_select); the others keep their particle order,

@@ -112,7 +112,7 @@ class PgReplica(C.Structure):
 class PgEnsemble(C.Structure):
     _fields_ = [("nreplicas", C.c_int32), ("ncells", C.c_int32), ("replicas", C.c_void_p),
                 ("replica_of", C.c_void_p), ("tpa", C.c_int32), ("block", C.c_int32), ("half", C.c_int32),
-                ("pad_", C.c_int32), ("rebuild", C.c_void_p)]
+                ("cubic", C.c_int32), ("rebuild", C.c_void_p)]
 
 
 class PgCsvResult(C.Structure):

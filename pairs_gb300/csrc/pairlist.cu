@@ -76,8 +76,11 @@ struct PcBuildArgs {
 };
 
 // The FP64 decision of a candidate in the screening band: the reference's separately
-// rounded rsq to the stencil's image of the partner (as nlist.cu).
-__device__ __noinline__ bool pc_exact(const PcBuildArgs &a, const double *len, int i, int j, int sx, int sy, int sz) {
+// rounded rsq to the stencil's image of the partner (as nlist.cu).  The box lengths are
+// the system's, or (batched ensembles) those of particle i's replica, looked up here so
+// that the build's loops keep no pointer to them.
+__device__ __noinline__ bool pc_exact(const PcBuildArgs &a, int i, int j, int sx, int sy, int sz) {
+    const double *len = a.replicas != nullptr ? a.replicas[a.replica_of[i]].len : a.box.len;
     const D4 xi = ld_d4_rare(a.p.pos, i), xj = ld_d4_rare(a.p.pos, j);
     const double dx = __dsub_rn(xi.x, ref_image(xj.x, sx, len[0]));
     const double dy = __dsub_rn(xi.y, ref_image(xj.y, sy, len[1]));
@@ -162,7 +165,6 @@ __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, Pc
         int rr = a.cells.reach > 1 ? a.cells.reach : 1;
         int rx = a.cells.reach_x > 0 ? a.cells.reach_x : rr;
         float fu[3] = {a.box.fx_unit[0], a.box.fx_unit[1], a.box.fx_unit[2]};
-        const double *len = a.box.len;
         double clx_u = w.clx_u, cly_u = w.cly_u;
         float clx = w.clx, cly = w.cly, scale_z = w.scale_z;
         bool grid_ok = true;
@@ -173,7 +175,6 @@ __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, Pc
             rr = R.reach > 1 ? R.reach : 1;
             rx = R.reach_x > 0 ? R.reach_x : rr;
             fu[0] = R.fx_unit[0]; fu[1] = R.fx_unit[1]; fu[2] = R.fx_unit[2];
-            len = R.len;
             clx_u = R.cell_len[0] * R.fx_scale[0]; cly_u = R.cell_len[1] * R.fx_scale[1];
             clx = (float) R.cell_len[0]; cly = (float) R.cell_len[1]; scale_z = (float) R.fx_scale[2];
             // each stencil cell visited once (the half stencil's ox 0 .. rx, oy and oz
@@ -221,8 +222,8 @@ __global__ void __launch_bounds__(kPcBuildBlock, 8) k_pc_build(PcBuildArgs a, Pc
                 const bool above_b = ox > 0 || (dxb != 0 ? dxb < 0 : (dyb != 0 ? dyb < 0 : (dzb != 0 ? dzb < 0 : j > ib)));
                 bool ka = use_a && j != ia && above_a && R.x <= r2_hi;
                 bool kb = use_b && j != ib && above_b && R.y <= r2_hi;
-                if(ka && !(R.x < r2_lo)) { ka = pc_exact(a, len, ia, j, sx, sy, sz); }
-                if(kb && !(R.y < r2_lo)) { kb = pc_exact(a, len, ib, j, sx, sy, sz); }
+                if(ka && !(R.x < r2_lo)) { ka = pc_exact(a, ia, j, sx, sy, sz); }
+                if(kb && !(R.y < r2_lo)) { kb = pc_exact(a, ib, j, sx, sy, sz); }
                 if(ka || kb) {
                     if(cnt < cap) {
                         __stcs(wp, (int32_t) ((uint32_t) j | (ka ? kPcMaskA : 0u) | (kb ? kPcMaskB : 0u)));
@@ -592,7 +593,7 @@ int pc_lj_force(const pg_box *box, const pg_particles *p, const pg_neighbor_list
 // Pair-cluster half lists over every replica of a batched ensemble: the table of slots
 // over the shared cell arrays (a cell's slots depend only on its start and index), then
 // the build with each slot's box, units and grid from its replica.  Every replica needs
-// at least 2 reach + 1 cells per axis (else overflow bit 5).
+// at least 2 reach + 1 cells per axis (else overflow bit 5); e->cubic promises cubic boxes.
 int ens_pc_build(const pg_ensemble *e, const pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                  double r_list2, pg_status *status, cudaStream_t st) {
     if(!e || !p || !cells || !list || !status || !list->half || !list->pair_table || !list->nbr || !list->count ||
@@ -611,8 +612,10 @@ int ens_pc_build(const pg_ensemble *e, const pg_particles *p, const pg_cells *ce
     }
     PcWindow w = {};
     w.r2w = (float) (r_list2 * (1.0 + 1.0e-3));
-    // replicas may differ in shape: distances in length units (the general form)
-    k_pc_build<false, true><<<blocks_for(list->stride, kPcBuildBlock), kPcBuildBlock, 0, st>>>(a, w, status);
+    // cubic replicas screen in their own fixed-point units; replicas of other shapes in lengths
+    const int grid = blocks_for(list->stride, kPcBuildBlock);
+    if(e->cubic) { k_pc_build<true, true><<<grid, kPcBuildBlock, 0, st>>>(a, w, status); }
+    else { k_pc_build<false, true><<<grid, kPcBuildBlock, 0, st>>>(a, w, status); }
     note_launch();
     return launch_status();
 }

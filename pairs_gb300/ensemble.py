@@ -139,6 +139,8 @@ class Ensemble:
         self.e = A.PgEnsemble()
         self.e.nreplicas = self.nrep
         self.e.replica_of = t["replica_of"].data_ptr()
+        # cubic boxes: the pair-cluster build screens in each replica's fixed-point units
+        self.e.cubic = int(all(L[0] == L[1] == L[2] for L in self.boxes))
         self.list = A.PgNeighborList()
         self.list.stride = n
         # half lists (each interior pair once, the reaction by a vector atomic): at 512
