@@ -33,6 +33,24 @@ from .engine import _box_quantum
 INT32_MAX = 2 ** 31 - 1
 
 
+def replica_grid(box, r_list, reach, pair_lists=False, index=0):
+    """Cell grid of one replica: (dims, reach_x, reach) with cells of >= r_list /
+    reach_x along x and >= r_list / reach along y and z.  reach 1, 2, 3 name the layouts
+    (1, 1), (2, 2) and (2, 1); reach 0 takes the first of (1, 1), (2, 1), (2, 2) whose grid
+    has 2 reach + 1 cells per axis (every stencil cell visited once), else (2, 2).
+    Pair-cluster lists need that grid: a replica without it raises ValueError."""
+    modes = {1: [(1, 1)], 2: [(2, 2)], 3: [(2, 1)], 0: [(1, 1), (2, 1), (2, 2)]}[reach]
+    for rx, rr in modes:
+        dims = [max(1, int(math.floor(box[d] * (rx if d == 0 else rr) / r_list))) for d in range(3)]
+        if all(dims[d] >= 2 * (rx if d == 0 else rr) + 1 for d in range(3)):
+            return dims, rx, rr
+    if pair_lists:
+        need = tuple(2 * (rx if d == 0 else rr) + 1 for d in range(3))
+        raise ValueError(f"replica {index}: pair-cluster lists need {need} cells per axis at reach "
+                         f"{reach}, the box gives {tuple(dims)}")
+    return dims, rx, rr
+
+
 class Ensemble:
     def __init__(self, replicas, *, cutoff=2.5, skin=0.3, dt=0.005, epsilon=1.0, sigma6=1.0, tpa=1, block=256,
                  reach=1, neighbor_capacity=None, policy="guard", chunk=None, graphs=True, fixed_point=None,
@@ -197,18 +215,7 @@ class Ensemble:
             L = self.boxes[r]
             R.first, R.n = int(self.first[r]), int(self.sizes[r])
             R.cell0 = cell0
-            # (cells per r_list along x, along y and z) of the layout: reach 0 takes per
-            # replica the largest cells whose grid visits every stencil cell once
-            modes = {1: [(1, 1)], 2: [(2, 2)], 3: [(2, 1)], 0: [(1, 1), (2, 1), (2, 2)]}[self.reach]
-            for rx, rr in modes:
-                dims = [max(1, int(math.floor(L[d] * (rx if d == 0 else rr) / self.r_list))) for d in range(3)]
-                if all(dims[d] >= 2 * (rx if d == 0 else rr) + 1 for d in range(3)):
-                    break
-            else:
-                if self.pair_lists:
-                    need = tuple(2 * (rx if d == 0 else rr) + 1 for d in range(3))
-                    raise ValueError(f"replica {r}: pair-cluster lists need {need} cells per axis at reach "
-                                     f"{self.reach}, the box gives {tuple(dims)}")
+            dims, rx, rr = replica_grid(L, self.r_list, self.reach, self.pair_lists, r)
             nc = 1
             for d in range(3):
                 R.dims[d] = dims[d]

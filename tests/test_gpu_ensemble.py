@@ -370,3 +370,32 @@ def test_autotune_picks_the_fastest_finalist():
     assert sorted(table, key=lambda r: r["score"])[:2] == sorted(timed, key=lambda r: r["score"])
     fastest = min(timed, key=lambda r: r["step_ms"])
     assert best == (fastest["tpa"], fastest["block"], fastest["reach"], fastest["half"])
+
+
+def test_select_flags_the_displaced_replicas():
+    """pg_ensemble_select: a replica is flagged when one of its atoms moved more than
+    sqrt(thresh2) from its position at the replica's last build (the guard's measure);
+    thresh2 < 0 flags every replica."""
+    import ctypes as C
+    from pairs_gb300 import _capi as A
+    from pairs_gb300.ensemble import Ensemble
+    reps = replicas()
+    ens = Ensemble(reps, tpa=2, policy="every")
+    ens.synchronize()
+    t = ens.t
+
+    def select(thresh2):
+        with torch.cuda.stream(ens.stream):
+            A.call("pg_ensemble_select", C.byref(ens.e), C.byref(ens.p), thresh2, ens.flags_ptr, ens.sh)
+        ens.synchronize()
+        return t["status"][ens.nstatus:].cpu().numpy().copy()
+
+    assert np.array_equal(select(0.0), [0, 0, 0, 0])          # right after the build
+    assert np.array_equal(select(-1.0), [1, 1, 1, 1])
+    # move one atom of replica 2 by 0.1 along y (0.1 / unit fixed-point steps)
+    i = int(ens.first[2]) + 17
+    unit = ens.boxes[2][1] / 2.0 ** 32
+    with torch.cuda.stream(ens.stream):
+        t["pos_fx"][i, 1] += int(round(0.1 / unit))
+    assert np.array_equal(select(0.09 ** 2), [0, 0, 1, 0])
+    assert np.array_equal(select(0.11 ** 2), [0, 0, 0, 0])
