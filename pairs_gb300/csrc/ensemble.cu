@@ -13,9 +13,15 @@
 // is two blocks); batched, every phase is one grid over all ~4M particles.  The
 // force kernel can give each particle tpa threads (1, 2, 4 or 8) that split its
 // list and combine with shuffles; the list layout interleaves tpa entries per
-// particle so those threads read consecutive words.  The host-side autotuner picks
-// tpa, the block size and the stencil reach (27 cells of >= r_list or 125 cells of
-// >= r_list/2) by timing them on the ensemble itself.
+// particle so those threads read consecutive words.  Pair-cluster half lists
+// (pairlist.cu) serve replicas too, each row on its replica's box and grid.  The
+// host-side autotuner picks tpa, the block size, the stencil reach (27 cells of
+// >= r_list, 125 cells of >= r_list/2, or per replica) and the list layout by timing
+// them on the ensemble itself.
+//
+// Partial rebuilds (pg_ensemble.rebuild): binning and list build touch only the
+// flagged replicas; the others keep their particle order, cells and list rows, so each
+// replica rebuilds on its own displacement cycle.
 #include "common.cuh"
 #include "persist.cuh"
 
