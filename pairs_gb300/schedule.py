@@ -13,7 +13,10 @@ when the host rebuilds and synchronises:
   forward / soft-minimum / backward / Adam kernels.
 * Inference: right after every rebuild the network predicts R for the new cycle;
   the host enqueues steps up to the predicted trip without reading anything back,
-  then rebuilds proactively.  If the guard tripped earlier, every force and
+  then rebuilds proactively.  At a build only the sample's features run on the
+  engine's stream, before the particles are re-sorted; the forward pass, soft minimum
+  and the copy of the prediction to the host run on a side stream while the build
+  proceeds (the learned policy's time at 1M atoms: 0.3114 -> 0.3083 ms per step).  If the guard tripped earlier, every force and
   integration pass after the trip did nothing (pg_particles.guard), so the host
   rewinds to the trip step, rebuilds there and continues: a misprediction costs
   skipped launches, never a wrong force.
@@ -82,6 +85,12 @@ class LearnedSchedule:
         self.loss = torch.zeros(1, dtype=torch.float32, device=dev)
         self.feat = torch.zeros((max_samples, self.ncells, 4), dtype=torch.float32, device=dev)
         self.feat_all = torch.zeros((self.ncells_all, 4), dtype=torch.float32, device=dev)
+        # the prediction at a build runs on a side stream (after the features event)
+        self.side = torch.cuda.Stream(device=dev)
+        self.side_h = C.c_void_p(self.side.cuda_stream)
+        self.ev_feat = torch.cuda.Event()
+        self.ev_pred = torch.cuda.Event()
+        self._side_busy = False
         self.labels = []                  # (slot, log R, censored)
         self.pending = []                 # (slot, step) samples of the open cycle
         self.cycles = 0
@@ -107,12 +116,24 @@ class LearnedSchedule:
             A.call("pg_cell_select", self._ptr(self.feat_all), self.ncells_all, self.ncells, self._ptr(self.feat[slot]),
                    e.sh)
 
-    def predict_log(self, slot):
-        """Soft-min prediction for the features in `slot` (device scalar in result[0])."""
+    def _side_done(self):
+        """Order the engine's stream after the side stream's last prediction (it
+        shares the output buffers) and wait for its copy to the host."""
+        if self._side_busy:
+            self.e.stream.wait_event(self.ev_pred)
+            self.ev_pred.synchronize()
+            self._side_busy = False
+
+    def predict_log(self, slot, stream=None):
+        """Soft-min prediction for the features in `slot` (device scalar in result[0]),
+        on the engine's stream or the given stream handle."""
         e = self.e
+        if stream is None:
+            self._side_done()
+        sh = e.sh if stream is None else stream
         A.call("pg_mlp_forward", self._ptr(self.params), self._ptr(self.feat[slot]), self.ncells,
-               self._ptr(self.out), e.sh)
-        A.call("pg_mlp_softmin", self._ptr(self.out), self.ncells, self.temperature, self._ptr(self.result), e.sh)
+               self._ptr(self.out), sh)
+        A.call("pg_mlp_softmin", self._ptr(self.out), self.ncells, self.temperature, self._ptr(self.result), sh)
 
     def _slot(self):
         used = {s for s, _, _ in self.labels} | {s for s, _ in self.pending}
@@ -137,10 +158,18 @@ class LearnedSchedule:
         `predict`, also queue the network's prediction; its value is copied to host
         memory with the rebuild's own status read.  Returns the sample's slot."""
         slot = self._slot()
+        self._side_done()
         self.features_into(slot, since=0)
         if predict:
-            self.predict_log(slot)
-            self.result_host.copy_(self.result, non_blocking=True)
+            # the network runs beside the binning and list build, which follow on the
+            # engine's stream; only the features precede them
+            self.ev_feat.record(self.e.stream)
+            self.side.wait_event(self.ev_feat)
+            self.predict_log(slot, stream=self.side_h)
+            with torch.cuda.stream(self.side):
+                self.result_host.copy_(self.result, non_blocking=True)
+            self.ev_pred.record(self.side)
+            self._side_busy = True
         self._next = slot
         return slot
 
@@ -158,12 +187,14 @@ class LearnedSchedule:
 
     def predicted(self):
         """Predicted steps of the new cycle (after the rebuild's status read)."""
+        self._side_done()
         return self._calibrated(float(self.result_host[0]))
 
     def raw_prediction(self):
         """The network's log prediction for the new cycle, as read with the rebuild's
         status, and the calibrated number of steps (the bias as of the last closed
         cycle).  note_prediction() later records it for the cycle's calibration."""
+        self._side_done()
         raw = float(self.result_host[0])
         return raw, math.exp(raw + self.bias)
 
