@@ -215,9 +215,12 @@ typedef struct {
 } pg_replica;
 
 /* A batched ensemble (config: hundreds of independent periodic LJ replicas run by
- * one launch per phase).  The list layout interleaves `tpa` entries per particle:
- * entry k of particle i is at ((k / tpa) * stride + i) * tpa + k % tpa, so the tpa
- * threads that share a particle read consecutive words. */
+ * one launch per phase).  The per-particle list layout interleaves `tpa` entries per
+ * particle: entry k of particle i is at ((k / tpa) * stride + i) * tpa + k % tpa, so the
+ * tpa threads that share a particle read consecutive words.  With list->pair_table set,
+ * the lists are pair-cluster half lists over every replica's cells (the layout of
+ * pg_build_neighbor_lists; stride >= pg_pair_slots(n, total cells)), tpa and block
+ * then unused. */
 typedef struct {
     int32_t nreplicas;
     int32_t ncells;              /* cells of all replicas */
@@ -522,17 +525,23 @@ int pg_mlp_adam(float *params, float *grads, float *m1, float *m2, float lr, flo
  * (global cell = cell0 + local cell), sort, permute, and split positions on each
  * replica's grid; pg_bin_particles for every replica at once.  cells->ncells = total
  * cells, cell_start/cell_count sized as for pg_bin_particles.  ws:
- * pg_workspace_bytes(n, total cells). */
+ * pg_workspace_bytes(n, total cells).  pos_hi/pos_lo may be NULL with fixed-point
+ * positions (then only pos_fx is written).  With e->rebuild set, only the flagged
+ * replicas are binned (see pg_ensemble). */
 int pg_ensemble_bin(const pg_ensemble *e, pg_particles *p, pg_cells *cells, pg_workspace ws, pg_status *status,
                     void *stream);
 
-/* Full Verlet lists within r_list for every replica (27- or 125-cell stencil per
- * the replica's reach), exact FP64 acceptance as pg_build_neighbor_lists, in the
- * tpa-interleaved layout; records pos_ref / ref_hi / ref_lo. */
+/* Verlet lists within r_list for every replica (the stencil of each replica's reach
+ * and reach_x), exact FP64 acceptance as pg_build_neighbor_lists, in the
+ * tpa-interleaved layout (full or half lists per e->half), or pair-cluster half lists
+ * when list->pair_table is set (every replica grid then needs 2 reach + 1 cells per
+ * axis, else status->overflow bit 5); records pos_ref and ref_fx (or ref_hi / ref_lo).
+ * With e->rebuild set, only the flagged replicas' rows are built. */
 int pg_ensemble_build_lists(const pg_ensemble *e, pg_particles *p, const pg_cells *cells, pg_neighbor_list *list,
                             double r_list2, pg_status *status, void *stream);
 
-/* Mixed-precision LJ forces for every replica, tpa threads per particle, full lists:
+/* Mixed-precision LJ forces for every replica, tpa threads per particle (pair-cluster
+ * lists: one thread per row), full or half lists:
  * FP32 on fixed-point positions (p->pos_fx, each replica's box 2^32 units, used when set)
  * or on compensated positions.  Pairs within a relative 1e-5 of the cutoff
  * are decided by the FP64 test, as in pg_lj_force, through a queue in ws (scratch, at
