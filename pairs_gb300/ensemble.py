@@ -153,6 +153,10 @@ class Ensemble:
         self.status_ptr = C.c_void_p(t["status"].data_ptr())
         self.nstatus = len(words)
         self.flags_ptr = C.c_void_p(t["status"].data_ptr() + 4 * self.nstatus)
+        # the build's status is copied to pinned memory behind the build, so that the
+        # force pass is queued before the host waits for it
+        self.status_host = torch.empty(len(words) + self.nrep, dtype=torch.int32).pin_memory()
+        self.status_event = torch.cuda.Event()
         t["thermo"] = z((2 * self.nrep,), f64)
         self.e = A.PgEnsemble()
         self.e.nreplicas = self.nrep
@@ -172,8 +176,7 @@ class Ensemble:
         self._max_nb = int(neighbor_capacity or 112)
         self.configure(tpa, block, reach, pair_lists=pair_lists)
         with torch.cuda.stream(self.stream):
-            self.rebuild()
-            self._force(0)                     # step 0: forces only (the reference's skip_first)
+            self.rebuild(then=lambda: self._force(0))    # step 0: forces only (the reference's skip_first)
         self.ts = 1
         self._pending = False                  # no final half kick is owed for step 0
 
@@ -290,15 +293,25 @@ class Ensemble:
         self._flags = s[self.nstatus:]
         return A.PgStatus.from_buffer_copy(s[: self.nstatus].tobytes())
 
-    def rebuild(self, partial=False):
+    def _wait_status(self):
+        """The status copied by the last snapshot (the host waits for that copy only)."""
+        self.status_event.synchronize()
+        self.host_syncs += 1
+        s = self.status_host.numpy()
+        self._flags = s[self.nstatus:].copy()
+        return A.PgStatus.from_buffer_copy(s[: self.nstatus].tobytes())
+
+    def rebuild(self, partial=False, then=None):
         """Bin and list every replica again, or with partial=True (and the ensemble's
-        `partial` option) only those selected by displacement."""
+        `partial` option) only those selected by displacement.  then, if given, queues the
+        work that uses the new lists (the force pass) before the host waits for the
+        build's status; it is queued again if the lists had to grow."""
         # the status resets below are torch ops: they must run on the stream the
         # library's kernels run on, whichever stream the caller has current
         with torch.cuda.stream(self.stream):
-            self._rebuild(partial and self.partial and not self._full_next)
+            self._rebuild(partial and self.partial and not self._full_next, then)
 
-    def _rebuild(self, partial):
+    def _rebuild(self, partial, then=None):
         by = C.byref
         self.p.guard = None
         if partial:
@@ -313,14 +326,22 @@ class Ensemble:
                 self.t["status"][2] = 0
                 A.call("pg_ensemble_build_lists", by(self.e), by(self.p), by(self.cells), by(self.list),
                        self.r_list2, self.status_ptr, self.sh)
-                st = self.read_status()
+                self.status_host.copy_(self.t["status"], non_blocking=True)
+                self.status_event.record(self.stream)
+                if then is not None:
+                    then()
+                st = self._wait_status()
                 if st.nonfinite:
                     raise A.PairsError("non-finite particle position met while binning")
                 if st.overflow & 32:
                     raise A.PairsError("a replica's cell grid is too small for pair-cluster lists")
                 if st.overflow & 2:
-                    # new (empty) list arrays: every replica is binned and listed again
+                    # new (empty) list arrays: every replica is binned and listed again (the
+                    # force pass queued on the short lists is redone; half lists add into
+                    # the force, so it starts from zero again)
                     self._alloc_list(int(st.max_neighbors * 1.15) + 8)
+                    if then is not None and self.half:
+                        self.t["force32"].zero_()
                     if self.e.rebuild:
                         self.e.rebuild = None
                         self.t["status"][self.nstatus:] = 1
@@ -392,8 +413,9 @@ class Ensemble:
                     # after step 0 otherwise, which owes no final half kick)
                     self._integrate(self.ts, 2 if self._pending else 1)
                     if self.policy == "every" or self.read_status().guard_tripped != INT32_MAX:
-                        self.rebuild(partial=True)
-                    self._force(self.ts)
+                        self.rebuild(partial=True, then=lambda: self._force(self.ts))
+                    else:
+                        self._force(self.ts)
                     self.ts += 1
                     self._pending = True
                     continue
@@ -409,8 +431,7 @@ class Ensemble:
                     # positions are those of step start + g; rebuild, then its force
                     self.ts = start + g
                     self._cycle = max(1, self.ts - self._build_ts)
-                    self.rebuild(partial=True)
-                    self._force(self.ts)
+                    self.rebuild(partial=True, then=lambda: self._force(self.ts))
                     self.ts += 1
                 else:
                     self.ts = start + k

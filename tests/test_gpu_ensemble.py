@@ -399,3 +399,40 @@ def test_select_flags_the_displaced_replicas():
         t["pos_fx"][i, 1] += int(round(0.1 / unit))
     assert np.array_equal(select(0.09 ** 2), [0, 0, 1, 0])
     assert np.array_equal(select(0.11 ** 2), [0, 0, 0, 0])
+
+
+@pytest.mark.parametrize("pairs", [False, True])
+def test_tiny_capacity_regrows_in_full_and_partial_builds(pairs):
+    """A list capacity of 4 overflows at the first build: the lists grow, the force pass
+    queued on the short lists is redone, and the forces equal the oracle's.  An overflow
+    inside a partial rebuild bins and lists every replica again (the grown arrays start
+    empty), and the forces again equal the oracle's."""
+    from pairs_gb300.ensemble import Ensemble
+    reps = replicas()
+    kw = dict(reach=2, pair_lists=True) if pairs else dict(tpa=2, half=True)
+    ens = Ensemble(reps, neighbor_capacity=4, **kw)
+    ens.synchronize()
+    assert ens._max_nb > 4
+
+    def check():
+        for r, st in enumerate(reps):
+            pos, vel, f = ens.replica_state(r)
+            sim = olj.Sim(dict(st, pos=pos, vel=vel), every=1, exact_sync=True)
+            sim.step()
+            assert rms_rel(f, sim.state()[2]) < 2e-5, r
+
+    check()
+    ens.run(12)
+    ens.synchronize()
+    grown = ens._max_nb
+    # a partial rebuild of every moved replica into lists of capacity 4 (the arrays stay
+    # as large as they are: the kernels stop writing at the capacity)
+    ens.list.max_neighbors = 4
+    ens.select2 = 0.0
+    builds = ens.nbuilds
+    with torch.cuda.stream(ens.stream):
+        ens.t["force32"].zero_()
+        ens.rebuild(partial=True, then=lambda: ens._force(ens.ts))
+    ens.synchronize()
+    assert ens.nbuilds == builds + 1 and ens._max_nb >= 0.9 * grown
+    check()
