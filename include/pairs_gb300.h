@@ -495,6 +495,13 @@ int pg_mlp_param_count(void);
 int pg_cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t steps_since_build,
                      double dt, double half_skin, float *features, void *stream);
 
+/* pg_cell_features of a state just binned by pg_bin_particles, before any force pass:
+ * every per-particle array is in the new order except the forces, which the binning
+ * leaves in the old one; perm is that binning's permutation (pg_bin_permutation:
+ * perm[k] = index before the binning of particle k).  The cells are the new ones. */
+int pg_cell_features_binned(const pg_particles *p, const pg_cells *cells, const int32_t *perm, int precision,
+                            int32_t steps_since_build, double dt, double half_skin, float *features, void *stream);
+
 /* The cells of one sample (no counterpart in the reference): the ncells feature rows
  * are split into k contiguous groups and each group's row with the largest feature 0
  * (fastest particle) is copied to out[k][4].  ncells >= k. */

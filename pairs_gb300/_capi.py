@@ -173,6 +173,8 @@ SIGNATURES = {
     "pg_mlp_softmin": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.c_void_p]),
     "pg_bin_permutation": (C.c_void_p, [C.c_int32, C.c_int32, PgWorkspace]),
     "pg_cell_select": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "pg_cell_features_binned": (C.c_int, [P(PgParticles), P(PgCells), C.c_void_p, C.c_int, C.c_int32, C.c_double,
+                                          C.c_double, C.c_void_p, C.c_void_p]),
     "pg_mlp_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_int,
                                   C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
     "pg_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_float,

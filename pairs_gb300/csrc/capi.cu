@@ -23,7 +23,7 @@ int integrate_mixed(const pg_box *box, pg_particles *p, double dt, int kicks, in
                     double half_skin2, int32_t step, pg_status *status, cudaStream_t st);
 int compute_thermo(const pg_box *box, const pg_particles *p, double *out, double *partials,
                    cudaStream_t st);
-int cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t since, double dt,
+int cell_features(const pg_particles *p, const pg_cells *cells, const int32_t *perm, int precision, int32_t since, double dt,
                   double half_skin, float *feat, cudaStream_t st);
 int mlp_forward(const float *params, const float *feat, int32_t ncells, float *out, cudaStream_t st);
 int mlp_softmin(const float *out, int32_t ncells, float temperature, float *result, cudaStream_t st);
@@ -240,7 +240,13 @@ int pg_dem_euler(pg_dem_particles *d, const pg_dem_params *prm, int precision, d
 
 int pg_cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t steps_since_build,
                      double dt, double half_skin, float *features, void *stream) {
-    return pg::cell_features(p, cells, precision, steps_since_build, dt, half_skin, features, S(stream));
+    return pg::cell_features(p, cells, nullptr, precision, steps_since_build, dt, half_skin, features, S(stream));
+}
+
+int pg_cell_features_binned(const pg_particles *p, const pg_cells *cells, const int32_t *perm, int precision,
+                            int32_t steps_since_build, double dt, double half_skin, float *features, void *stream) {
+    if(!perm) { return PG_ERR_ARGUMENT; }
+    return pg::cell_features(p, cells, perm, precision, steps_since_build, dt, half_skin, features, S(stream));
 }
 
 int pg_cell_select(const float *features, int32_t ncells, int32_t k, float *out, void *stream) {

@@ -34,7 +34,11 @@ constexpr int kFeat = 4;   // f0, f1, f2, valid
 // cell) before one of them publishes it.  The accumulators live in the feature rows
 // themselves (zeroed first); k_cell_finish turns them into the features.  (A kernel
 // with 16 lanes per cell of ~10 particles took 39 us at 1M atoms in 110k cells.)
-__global__ void __launch_bounds__(256) k_cell_accum(pg_particles p, pg_cells cells, int precision, float *feat) {
+// With perm (a binning's permutation, perm[k] = index before the binning of particle k),
+// the state was just binned: every array is in the new order except the forces, which
+// the binning leaves in the old one.
+__global__ void __launch_bounds__(256) k_cell_accum(pg_particles p, pg_cells cells, int precision,
+                                                    const int32_t *perm, float *feat) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = i < p.n ? cells.particle_cell[i] : -1;
     const bool live = c >= 0 && c < cells.ncells;
@@ -43,11 +47,12 @@ __global__ void __launch_bounds__(256) k_cell_accum(pg_particles p, pg_cells cel
         const D4 v = ld_d4(p.vel, i);
         vv = (float) (v.x * v.x + v.y * v.y + v.z * v.z);
         float fx, fy, fz;
+        const int fi = perm != nullptr ? perm[i] : i;
         if(precision == PG_MIXED) {
-            const float4 f = ld_f4(p.force32, i);
+            const float4 f = ld_f4(p.force32, fi);
             fx = f.x; fy = f.y; fz = f.z;
         } else {
-            const D4 f = ld_d4(p.force, i);
+            const D4 f = ld_d4(p.force, fi);
             fx = (float) f.x; fy = (float) f.y; fz = (float) f.z;
         }
         fm = sqrtf(fx * fx + fy * fy + fz * fz) / (float) p.mass[i];
@@ -343,14 +348,14 @@ __global__ void k_adam(float *params, float *grads, float *m1, float *m2, int n,
 
 // ---------------------------------------------------------------- host side
 
-int cell_features(const pg_particles *p, const pg_cells *cells, int precision, int32_t since, double dt,
-                  double half_skin, float *feat, cudaStream_t st) {
+int cell_features(const pg_particles *p, const pg_cells *cells, const int32_t *perm, int precision, int32_t since,
+                  double dt, double half_skin, float *feat, cudaStream_t st) {
     if(!p || !cells || !feat || !p->vel || !p->mass) { return PG_ERR_ARGUMENT; }
     if(precision == PG_MIXED ? !p->force32 : !p->force) { return PG_ERR_ARGUMENT; }
     if(!cells->particle_cell || !cells->cell_count || cells->ncells <= 0) { return PG_ERR_ARGUMENT; }
     const float ts = (float) since, fdt = (float) dt, ihs = (float) (1.0 / half_skin);
     cudaMemsetAsync(feat, 0, (size_t) cells->ncells * kFeat * sizeof(float), st);
-    if(p->n > 0) { k_cell_accum<<<blocks_for(p->n), 256, 0, st>>>(*p, *cells, precision, feat); note_launch(); }
+    if(p->n > 0) { k_cell_accum<<<blocks_for(p->n), 256, 0, st>>>(*p, *cells, precision, perm, feat); note_launch(); }
     k_cell_finish<<<blocks_for(cells->ncells), 256, 0, st>>>(*cells, ts, fdt, ihs, feat); note_launch();
     return launch_status();
 }

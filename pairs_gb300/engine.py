@@ -356,14 +356,16 @@ class LJEngine:
 
     # ------------------------------------------------------------------ modules
 
-    def rebuild(self, pre_bin=None, then=None):
+    def rebuild(self, pre_bin=None, then=None, post_bin=None):
         """Bin + sort + Verlet build, growing the list until it fits.  Returns the
         step at which the guard had tripped before this build (INT32_MAX if none).
         pre_bin, if given, queues work on the state before the particles are
-        re-sorted (the learned schedule's features and prediction).  then, if given,
-        queues the work that uses the new list (the force pass) before the host waits
-        for the build's status, so the host's bookkeeping overlaps it; it is queued
-        again if the build has to be repeated."""
+        re-sorted.  post_bin, if given, queues work on the binned state beside the list
+        build (the learned schedule's features and prediction, on its own stream) and
+        returns an event that later work on the engine's stream waits for, or None.
+        then, if given, queues the work that uses the new list (the force pass) before
+        the host waits for the build's status, so the host's bookkeeping overlaps it;
+        it is queued again if the build has to be repeated."""
         by = C.byref
         if pre_bin is not None:
             pre_bin()
@@ -371,6 +373,7 @@ class LJEngine:
         st_dev[0:1].bitwise_and_(BARRIER_TIMEOUT)       # overflow (a barrier timeout stays to be seen)
         st_dev[1:3].zero_()                             # max_cell_count, max_neighbors
         A.call("pg_bin_particles", by(self.box), by(self.p), by(self.cells), self.ws, self.status_ptr, self.sh)
+        side = post_bin() if post_bin is not None else None
         guard = None
         first = True
         while True:
@@ -388,6 +391,8 @@ class LJEngine:
             early = then is not None and not self.tiles
             if early:
                 self.list.steps_since_build = 0
+                if side is not None:
+                    self.stream.wait_event(side)
                 then()
             st = self._wait_status()
             guard = self._guard_abs(st.guard_tripped) if guard is None else guard
@@ -414,6 +419,8 @@ class LJEngine:
         self.list.steps_since_build = 0
         self.since_build = 0
         self.nbuilds += 1
+        if side is not None:
+            self.stream.wait_event(side)
         if then is not None and not early:
             then()
         return guard
@@ -512,7 +519,7 @@ class LJEngine:
         are x(s) and the build is the one step s needed: rewind to s."""
         if ts != 0 and ts != self.next_rebuild:
             return False
-        s = self.rebuild(pre_bin=self._schedule_hook(), then=self.force)
+        s = self.rebuild(post_bin=self._schedule_hook(), then=self.force)
         tripped_at = None
         if ts > 0 and s <= ts:
             tripped_at = s
@@ -523,12 +530,12 @@ class LJEngine:
         return True
 
     def _schedule_hook(self):
-        """The learned schedule's work at a list build (features of the pre-build
-        state, and the prediction once trained), or None."""
+        """The learned schedule's work at a list build (features of the binned state,
+        and the prediction once trained, beside the list build), or None."""
         sch = self.schedule
         if sch is None:
             return None
-        return lambda: sch.sample_at_build(predict=sch.trained)
+        return lambda: sch.sample_after_bin(predict=sch.trained)
 
     def _after_rebuild_schedule(self, ts, tripped_at):
         """Close the finished cycle and choose the next rebuild step."""
@@ -606,7 +613,7 @@ class LJEngine:
         if built:
             pass                                        # the rebuild queued the force pass
         elif rebuild:
-            self.rebuild(pre_bin=self._schedule_hook() if self.speculative else None, then=self.force)
+            self.rebuild(post_bin=self._schedule_hook() if self.speculative else None, then=self.force)
             self._cycle_start = ts
             if self.speculative:
                 self._after_rebuild_schedule(ts, tripped_at)

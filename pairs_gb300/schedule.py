@@ -13,10 +13,11 @@ when the host rebuilds and synchronises:
   forward / soft-minimum / backward / Adam kernels.
 * Inference: right after every rebuild the network predicts R for the new cycle;
   the host enqueues steps up to the predicted trip without reading anything back,
-  then rebuilds proactively.  At a build only the sample's features run on the
-  engine's stream, before the particles are re-sorted; the forward pass, soft minimum
-  and the copy of the prediction to the host run on a side stream while the build
-  proceeds (the learned policy's time at 1M atoms: 0.3114 -> 0.3083 ms per step).  If the guard tripped earlier, every force and
+  then rebuilds proactively.  At a build the sample's features (of the state just
+  binned: velocities in the new order, forces read through the binning's
+  permutation), the forward pass, the soft minimum and the copy of the prediction to
+  the host run on a side stream beside the list build; the force pass, which
+  overwrites the forces, waits for them.  If the guard tripped earlier, every force and
   integration pass after the trip did nothing (pg_particles.guard), so the host
   rewinds to the trip step, rebuilds there and continues: a misprediction costs
   skipped launches, never a wrong force.
@@ -151,27 +152,38 @@ class LearnedSchedule:
         self.features_into(slot)
         self.pending.append((slot, step))
 
-    def sample_at_build(self, predict):
-        """Features of the state at a list rebuild, taken before the particles are
-        re-sorted (so velocities and forces still belong to the same particles), as
-        the first sample of the new cycle (steps since the build = 0).  With
-        `predict`, also queue the network's prediction; its value is copied to host
-        memory with the rebuild's own status read.  Returns the sample's slot."""
+    def sample_after_bin(self, predict):
+        """Features of the state at a list rebuild, as the first sample of the new
+        cycle (steps since the build = 0), taken on the side stream right after the
+        binning: velocities are in the new order, the forces still in the old one and
+        read through the binning's permutation (pg_cell_features_binned), so each
+        particle's velocity and force stay together.  With `predict`, also the
+        network's prediction, copied to host memory.  Returns the event the engine's
+        later work (the force pass, which overwrites the forces) waits for."""
+        e = self.e
         slot = self._slot()
         self._side_done()
-        self.features_into(slot, since=0)
+        self.ev_feat.record(e.stream)
+        self.side.wait_event(self.ev_feat)
+        perm = A.load().pg_bin_permutation(e.n, e.cells.ncells, e.ws)
+        if not perm:
+            raise A.PairsError("the binning workspace holds no permutation")
+        A.call("pg_cell_features_binned", C.byref(e.p), C.byref(e.cells), C.c_void_p(perm), e.precision, 0, e.dt,
+               0.5 * e.skin, self._ptr(self.feat_all), self.side_h)
+        if self.ncells == self.ncells_all:
+            with torch.cuda.stream(self.side):
+                self.feat[slot].copy_(self.feat_all)
+        else:
+            A.call("pg_cell_select", self._ptr(self.feat_all), self.ncells_all, self.ncells, self._ptr(self.feat[slot]),
+                   self.side_h)
         if predict:
-            # the network runs beside the binning and list build, which follow on the
-            # engine's stream; only the features precede them
-            self.ev_feat.record(self.e.stream)
-            self.side.wait_event(self.ev_feat)
             self.predict_log(slot, stream=self.side_h)
             with torch.cuda.stream(self.side):
                 self.result_host.copy_(self.result, non_blocking=True)
-            self.ev_pred.record(self.side)
-            self._side_busy = True
+        self.ev_pred.record(self.side)
+        self._side_busy = True
         self._next = slot
-        return slot
+        return self.ev_pred
 
     def open_cycle(self, step):
         """Start the new cycle with the sample taken at its build."""
@@ -293,9 +305,9 @@ class EMASchedule:
         self._next = None
         self._start = None
 
-    def sample_at_build(self, predict):
+    def sample_after_bin(self, predict):
         self._next = 0
-        return 0
+        return None
 
     def open_cycle(self, step):
         self._start = step

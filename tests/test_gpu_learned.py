@@ -225,3 +225,41 @@ def test_cell_features_match_a_host_computation(half):
             want[c] = (0.0, 0.0, 7 / 20, 0.0)
     assert (count > 0).mean() > 0.9
     assert np.allclose(got, want, rtol=2e-6, atol=1e-9)
+
+
+def test_binned_features_pair_each_velocity_with_its_force():
+    """pg_cell_features_binned right after a binning: velocities and masses are in the
+    new order, the forces still in the old one and read through the permutation; the
+    features equal a host computation on the new cells with each particle's own force."""
+    from pairs_gb300.engine import LJEngine
+    st = lattice.copper_fcc_lattice(16, 16, 16)
+    e = LJEngine(st, precision="mixed", half=True, policy="guard")
+    e.run(30)
+    e.settle()
+    torch.cuda.synchronize()
+    uid_old = e.t["uid"][: e.n].cpu().numpy().copy()
+    frc_old = e.t["force32"][: e.n, :3].cpu().numpy().astype(np.float64)
+    force_of_uid = np.empty_like(frc_old)
+    force_of_uid[uid_old] = frc_old
+    e.rebuild()                                   # bin (new order) and build; no force pass
+    perm = A.load().pg_bin_permutation(e.n, e.cells.ncells, e.ws)
+    nc = e.cells.ncells
+    feat = torch.zeros((nc, 4), dtype=torch.float32, device="cuda")
+    A.call("pg_cell_features_binned", C.byref(e.p), C.byref(e.cells), C.c_void_p(perm), e.precision, 0, e.dt,
+           0.5 * e.skin, C.c_void_p(feat.data_ptr()), e.sh)
+    torch.cuda.synchronize()
+    got = feat.cpu().numpy()
+    uid = e.t["uid"][: e.n].cpu().numpy()
+    start = e.t["cell_start"][:nc].cpu().numpy()
+    count = e.t["cell_count"][:nc].cpu().numpy()
+    vel = e.t["vel"][: e.n, :3].cpu().numpy()
+    mass = e.t["mass"][: e.n].cpu().numpy()
+    frc = force_of_uid[uid]
+    hs = 0.5 * e.skin
+    vmag = np.sqrt((vel ** 2).sum(axis=1))
+    acc = np.sqrt((frc ** 2).sum(axis=1)) / mass
+    want = np.zeros_like(got)
+    for c in range(nc):
+        b, k = start[c], count[c]
+        want[c] = (vmag[b:b + k].max() * e.dt / hs, acc[b:b + k].mean() * e.dt ** 2 / hs, 0.0, 1.0) if k else 0.0
+    assert np.allclose(got, want, rtol=2e-6, atol=1e-9)
