@@ -252,19 +252,27 @@ class LearnedSchedule:
             return None
         batch = self.labels if recent is None else self.labels[-recent:]
         ns = len(batch)
-        for _ in range(steps):
-            self.loss.zero_()
-            for slot, target, cens in batch:
-                self.predict_log(slot)
-                A.call("pg_mlp_backward", self._ptr(self.params), self._ptr(self.feat[slot]), self._ptr(self.out),
-                       self.ncells, self._ptr(self.result), float(target), int(cens), self.temperature,
-                       self._ptr(self.grads), self._ptr(self.loss), e.sh)
-            self.adam_t += 1
-            A.call("pg_mlp_adam", self._ptr(self.params), self._ptr(self.grads), self._ptr(self.m1),
-                   self._ptr(self.m2), self.lr, 0.9, 0.999, 1e-8, self.adam_t, 1.0 / ns, e.sh)
+        # on the side stream, beside the steps; after the engine's stream has written the
+        # samples (mid-cycle features are taken there)
+        self.ev_feat.record(e.stream)
+        self.side.wait_event(self.ev_feat)
+        with torch.cuda.stream(self.side):
+            for _ in range(steps):
+                self.loss.zero_()
+                for slot, target, cens in batch:
+                    self.predict_log(slot, stream=self.side_h)
+                    A.call("pg_mlp_backward", self._ptr(self.params), self._ptr(self.feat[slot]),
+                           self._ptr(self.out), self.ncells, self._ptr(self.result), float(target), int(cens),
+                           self.temperature, self._ptr(self.grads), self._ptr(self.loss), self.side_h)
+                self.adam_t += 1
+                A.call("pg_mlp_adam", self._ptr(self.params), self._ptr(self.grads), self._ptr(self.m1),
+                       self._ptr(self.m2), self.lr, 0.9, 0.999, 1e-8, self.adam_t, 1.0 / ns, self.side_h)
+        self.ev_pred.record(self.side)
+        self._side_busy = True
         self.trained = True
         if not log:
             return None
+        self.ev_pred.synchronize()
         final = float(self.loss.item()) / ns
         self.train_log.append(final)
         return final
